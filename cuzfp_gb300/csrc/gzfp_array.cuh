@@ -1,0 +1,219 @@
+// gzfp_array.cuh -- array-level pieces of the codec: block geometry, the
+// gather / scatter of one block with zfp's edge padding, and the bit writer /
+// reader over the fixed-rate stream.  Like gzfp_block.cuh these are
+// host+device so the CPU tests run the exact per-thread code of the kernels.
+#pragma once
+
+#include "gzfp_block.cuh"
+
+namespace gzfp {
+
+// Geometry of a contiguous a[nz][ny][nx] field cut into 4^D blocks; unused
+// axes have size 1.  Blocks are numbered x fastest, then y, then z, the order
+// of zfp's block loops (Z/src/template/compress.c:60-104).
+struct Geom {
+  uint32_t nx, ny, nz;
+  uint32_t bx, by, bz;  // blocks per axis
+  uint64_t nblocks;
+};
+
+GZ_HD void block_coords(const Geom& g, uint64_t b, uint32_t& ix, uint32_t& iy, uint32_t& iz) {
+  uint64_t r = b / g.bx;
+  ix = (uint32_t)(b - r * g.bx);
+  uint64_t s = r / g.by;
+  iy = (uint32_t)(r - s * g.by);
+  iz = (uint32_t)s;
+}
+
+// zfp's pad_block (Z/src/template/encode.c:55-74) as an index map: with c
+// valid values along an axis, padded position p reads position map(c, p):
+// c = 3 -> {0,1,2,0}, c = 2 -> {0,1,1,0}, c = 1 -> {0,0,0,0}.  Padding is
+// applied x, then y, then z, each copying already padded values, so the
+// 3D result is separable.
+GZ_HD uint32_t pad_index(uint32_t c, uint32_t p) {
+  const uint32_t lut = c >= 4 ? 0xE4u : c == 3 ? 0x24u : c == 2 ? 0x14u : 0x00u;
+  return (lut >> (2 * p)) & 3u;
+}
+
+GZ_HD uint32_t valid_count(uint32_t n, uint32_t i) {
+  uint32_t c = n - 4 * i;
+  return c > 4 ? 4 : c;
+}
+
+template <typename T>
+GZ_HD typename FT<T>::UInt load_bits(const T* p) {
+  typedef typename FT<T>::UInt UInt;
+#if defined(__CUDA_ARCH__)
+  return (UInt)__ldg((const UInt*)p);
+#else
+  UInt v;
+  __builtin_memcpy(&v, p, sizeof v);
+  return v;
+#endif
+}
+
+// Gather block (ix, iy, iz) as raw IEEE bits, padded at partial edges.
+template <int D, typename T>
+GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
+                  typename FT<T>::UInt* raw) {
+  const uint32_t cx = valid_count(g.nx, ix);
+  const uint32_t cy = D >= 2 ? valid_count(g.ny, iy) : 1;
+  const uint32_t cz = D >= 3 ? valid_count(g.nz, iz) : 1;
+  const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
+  const T* base = in + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
+  constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
+  if (cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4)) {
+#pragma unroll
+    for (int z = 0; z < DZ; z++)
+#pragma unroll
+      for (int y = 0; y < DY; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++) raw[16 * z + 4 * y + x] = load_bits(base + x + y * sy + z * sz);
+  } else {
+#pragma unroll
+    for (int z = 0; z < DZ; z++)
+#pragma unroll
+      for (int y = 0; y < DY; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++)
+          raw[16 * z + 4 * y + x] =
+              load_bits(base + pad_index(cx, x) + pad_index(cy, y) * sy + pad_index(cz, z) * sz);
+  }
+}
+
+// Store the valid part of block (ix, iy, iz) (Z/src/template/decode3.c:6-25).
+template <int D, typename T>
+GZ_HD void scatter(T* out, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
+                   const typename FT<T>::UInt* raw) {
+  typedef typename FT<T>::UInt UInt;
+  const uint32_t cx = valid_count(g.nx, ix);
+  const uint32_t cy = D >= 2 ? valid_count(g.ny, iy) : 1;
+  const uint32_t cz = D >= 3 ? valid_count(g.nz, iz) : 1;
+  const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
+  UInt* base = (UInt*)out + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
+  constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
+#pragma unroll
+  for (int z = 0; z < DZ; z++)
+#pragma unroll
+    for (int y = 0; y < DY; y++)
+#pragma unroll
+      for (int x = 0; x < 4; x++)
+        if ((uint32_t)x < cx && (uint32_t)y < cy && (uint32_t)z < cz)
+          base[x + y * sy + z * sz] = raw[16 * z + 4 * y + x];
+}
+
+// ------------------------------------------------------------- bit writer
+// Writes one block's bits, LSB first into 64-bit words, starting at absolute
+// bit `pos` of the stream (Z/src/inline/bitstream.c:258-283 word layout).
+// Words that another block also touches (the first and last word when the
+// block does not start / end on a word boundary) go through `Words::merge`,
+// every other word through `Words::store`.
+template <class Words>
+struct BitWriter {
+  Words words;
+  uint64_t wi;      // index of the word being filled
+  uint64_t acc;     // its pending bits
+  uint32_t fill;    // number of pending bits
+  uint64_t first;   // index of a shared first word, or ~0
+  uint64_t last;    // index of a shared last word, or ~0
+
+  GZ_HD BitWriter(Words w, uint64_t pos, uint32_t maxbits) : words(w) {
+    wi = pos >> 6;
+    fill = (uint32_t)(pos & 63);
+    acc = 0;
+    uint64_t end = pos + maxbits;
+    first = fill ? wi : ~0ull;
+    last = (end & 63) ? (end >> 6) : ~0ull;
+  }
+  GZ_HD void emit() {
+    if (wi == first || wi == last)
+      words.merge(wi, acc);
+    else
+      words.store(wi, acc);
+    wi++;
+  }
+  // append the low n (<= 64) bits of v; v has no bits at or above n
+  GZ_HD void put(uint64_t v, uint32_t n) {
+    acc |= shl64(v, fill);
+    uint32_t f = fill + n;
+    if (f >= 64) {
+      emit();
+      acc = shr64(v, 64 - fill);
+      fill = f - 64;
+    } else {
+      fill = f;
+    }
+  }
+  GZ_HD void zeros(uint32_t n) {
+    while (n >= 64) {
+      put(0, 64);
+      n -= 64;
+    }
+    if (n) put(0, n);
+  }
+  // the block ends mid-word: hand over the partial last word
+  GZ_HD void finish() {
+    if (fill) emit();
+  }
+};
+
+// ------------------------------------------------------------- bit reader
+template <class Words>
+struct BitReader {
+  Words words;
+  uint64_t wi;
+  uint64_t w0, w1;
+  uint32_t off;
+
+  GZ_HD BitReader(Words w, uint64_t pos) : words(w) {
+    wi = pos >> 6;
+    off = (uint32_t)(pos & 63);
+    w0 = words.load(wi);
+    w1 = words.load(wi + 1);
+  }
+  GZ_HD uint64_t peek64() const { return off ? (w0 >> off) | (w1 << (64 - off)) : w0; }
+  GZ_HD void skip(uint32_t n) {  // n <= 64
+    off += n;
+    if (off >= 64) {
+      off -= 64;
+      wi++;
+      w0 = w1;
+      w1 = words.load(wi + 1);
+    }
+  }
+  GZ_HD uint64_t read(uint32_t n) {  // n <= 64
+    if (n == 0) return 0;
+    uint64_t v = peek64() & lowmask64(n);
+    skip(n);
+    return v;
+  }
+};
+
+// ------------------------------------------------------- per-block drivers
+
+template <int D, typename T, class Words>
+GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words) {
+  typedef typename FT<T>::UInt UInt;
+  constexpr int BS = 1 << (2 * D);
+  uint32_t ix, iy, iz;
+  block_coords(g, b, ix, iy, iz);
+  UInt raw[BS];
+  gather<D, T>(in, g, ix, iy, iz, raw);
+  BitWriter<Words> w(words, b * (uint64_t)maxbits, maxbits);
+  encode_block<D, T>(raw, maxbits, w);
+  w.finish();
+}
+
+template <int D, typename T, class Words>
+GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words words) {
+  typedef typename FT<T>::UInt UInt;
+  constexpr int BS = 1 << (2 * D);
+  uint32_t ix, iy, iz;
+  block_coords(g, b, ix, iy, iz);
+  BitReader<Words> r(words, b * (uint64_t)maxbits);
+  UInt raw[BS];
+  decode_block<D, T>(r, maxbits, raw);
+  scatter<D, T>(out, g, ix, iy, iz, raw);
+}
+
+}  // namespace gzfp

@@ -1,0 +1,650 @@
+// gzfp_block.cuh -- per-block ZFP fixed-rate codec, one thread per block.
+//
+// Every function here works on one 4^d block held in registers.  It is
+// written once and compiled for sm_103a by nvcc (the product kernels in
+// gzfp_kernels.cu); the same source also builds for the host so the CPU
+// test suite can check the block logic against the oracle without a GPU.
+//
+// Arithmetic follows zfp 0.5.0 as vendored by cuZFP
+// (src/thirdparty_builtin/zfp-0.5.0, abbreviated Z/) step for step; the GPU
+// formulation differs in how the work is organised, not in what is computed:
+//   * the common exponent is read from the IEEE exponent fields instead of
+//     frexp (Z/src/template/encode.c:10-33);
+//   * f64 quantisation shifts the significand instead of multiplying by
+//     ldexp(1, 62 - emax) (encode.c:36-52), because GB300's FP64 pipe runs
+//     at a small fraction of its integer rate; the result is identical;
+//   * bit planes are obtained by transposing 32x32 (or SIMD 16x16 / 4x4)
+//     bit matrices in registers instead of the per-plane gather loop of
+//     encode_ints (encode.c:133-137);
+//   * the group-test coder of encode_ints / decode_ints (encode.c:122-151,
+//     Z/src/template/decode.c:73-105) is evaluated one run of zeros at a
+//     time with count-trailing-zeros instead of one bit at a time.
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define GZ_HD __host__ __device__ __forceinline__
+#else
+#define GZ_HD inline
+#endif
+
+namespace gzfp {
+
+// ------------------------------------------------------------ bit helpers
+
+GZ_HD uint64_t shr64(uint64_t v, uint32_t s) { return s < 64 ? v >> s : 0; }
+GZ_HD uint64_t shl64(uint64_t v, uint32_t s) { return s < 64 ? v << s : 0; }
+GZ_HD uint64_t lowmask64(uint32_t n) { return n >= 64 ? ~0ull : (1ull << n) - 1; }
+
+// number of trailing zeros; 64 for zero
+GZ_HD uint32_t ctz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__clzll((long long)__brevll(x));
+#else
+  return x ? (uint32_t)__builtin_ctzll(x) : 64u;
+#endif
+}
+GZ_HD uint32_t ctz32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__clz((int)__brev(x));
+#else
+  return x ? (uint32_t)__builtin_ctz(x) : 32u;
+#endif
+}
+// number of leading zeros; 64 for zero
+GZ_HD uint32_t clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__clzll((long long)x);
+#else
+  return x ? (uint32_t)__builtin_clzll(x) : 64u;
+#endif
+}
+
+GZ_HD uint32_t lo32(uint64_t v) { return (uint32_t)v; }
+GZ_HD uint32_t hi32(uint64_t v) { return (uint32_t)(v >> 32); }
+
+// ----------------------------------------------------------- scalar traits
+
+template <typename T>
+struct FT;
+
+template <>
+struct FT<float> {
+  typedef uint32_t UInt;
+  typedef int32_t Int;
+  static constexpr int P = 32;       // integer precision
+  static constexpr int EBITS = 8;    // exponent bits (Z/src/traitsf.h)
+  static constexpr int EBIAS = 127;  // (1 << (EBITS - 1)) - 1
+  static constexpr int MANT = 23;    // stored significand bits
+  static constexpr int EMAXF = 127;  // largest finite unbiased exponent
+  static constexpr uint32_t NB = 0xaaaaaaaau;  // negabinary mask
+};
+
+template <>
+struct FT<double> {
+  typedef uint64_t UInt;
+  typedef int64_t Int;
+  static constexpr int P = 64;
+  static constexpr int EBITS = 11;  // Z/src/traitsd.h
+  static constexpr int EBIAS = 1023;
+  static constexpr int MANT = 52;
+  static constexpr int EMAXF = 1023;
+  static constexpr uint64_t NB = 0xaaaaaaaaaaaaaaaaull;
+};
+
+constexpr int kMinExp = -1074;  // ZFP_MIN_EXP (Z/inc/zfp.h:80)
+
+// ------------------------------------------------------------ permutations
+// Coefficient orders of Z/src/template/codec{1,2,3}.c (perm_1/2/3): a fixed
+// part of the stream format, so the tables are kept value for value.
+
+template <int D>
+struct Perm;
+template <>
+struct Perm<1> {
+  static GZ_HD constexpr int at(int i) { return i; }
+};
+template <>
+struct Perm<2> {
+  static GZ_HD constexpr int at(int i) {
+    switch (i) {
+      case 0: return 0; case 1: return 1; case 2: return 4; case 3: return 5; case 4: return 2; case 5: return 8;
+      case 6: return 6; case 7: return 9; case 8: return 3; case 9: return 12; case 10: return 10; case 11: return 7;
+      case 12: return 13; case 13: return 11; case 14: return 14; case 15: return 15;
+      default: return 0;
+    }
+  }
+};
+template <>
+struct Perm<3> {
+  static GZ_HD constexpr int at(int i) {
+    switch (i) {
+      case 0: return 0; case 1: return 1; case 2: return 4; case 3: return 16; case 4: return 20; case 5: return 17;
+      case 6: return 5; case 7: return 2; case 8: return 8; case 9: return 32; case 10: return 21; case 11: return 6;
+      case 12: return 18; case 13: return 24; case 14: return 9; case 15: return 33; case 16: return 36; case 17: return 3;
+      case 18: return 12; case 19: return 48; case 20: return 22; case 21: return 25; case 22: return 37; case 23: return 40;
+      case 24: return 34; case 25: return 10; case 26: return 7; case 27: return 19; case 28: return 28; case 29: return 13;
+      case 30: return 49; case 31: return 52; case 32: return 41; case 33: return 38; case 34: return 26; case 35: return 23;
+      case 36: return 29; case 37: return 53; case 38: return 11; case 39: return 35; case 40: return 44; case 41: return 14;
+      case 42: return 50; case 43: return 56; case 44: return 42; case 45: return 27; case 46: return 39; case 47: return 45;
+      case 48: return 30; case 49: return 54; case 50: return 57; case 51: return 60; case 52: return 51; case 53: return 15;
+      case 54: return 43; case 55: return 46; case 56: return 58; case 57: return 61; case 58: return 55; case 59: return 31;
+      case 60: return 62; case 61: return 59; case 62: return 47; case 63: return 63;
+      default: return 0;
+    }
+  }
+};
+
+
+// ----------------------------------------------------------------- lifting
+// zfp's lifting steps (Z/src/template/encode.c:77-103, decode.c:28-54) in
+// two's-complement wrap-around arithmetic with arithmetic right shifts.
+
+template <typename Int>
+struct Unsigned;
+template <>
+struct Unsigned<int32_t> {
+  typedef uint32_t T;
+};
+template <>
+struct Unsigned<int64_t> {
+  typedef uint64_t T;
+};
+
+template <typename Int>
+GZ_HD Int wadd(Int a, Int b) {
+  typedef typename Unsigned<Int>::T U;
+  return (Int)((U)a + (U)b);
+}
+template <typename Int>
+GZ_HD Int wsub(Int a, Int b) {
+  typedef typename Unsigned<Int>::T U;
+  return (Int)((U)a - (U)b);
+}
+template <typename Int>
+GZ_HD Int wshl1(Int a) {
+  typedef typename Unsigned<Int>::T U;
+  return (Int)((U)a << 1);
+}
+
+template <typename Int>
+GZ_HD void fwd_lift(Int& x, Int& y, Int& z, Int& w) {
+  x = wadd(x, w); x >>= 1; w = wsub(w, x);
+  z = wadd(z, y); z >>= 1; y = wsub(y, z);
+  x = wadd(x, z); x >>= 1; z = wsub(z, x);
+  w = wadd(w, y); w >>= 1; y = wsub(y, w);
+  w = wadd(w, (Int)(y >> 1)); y = wsub(y, (Int)(w >> 1));
+}
+
+template <typename Int>
+GZ_HD void inv_lift(Int& x, Int& y, Int& z, Int& w) {
+  y = wadd(y, (Int)(w >> 1)); w = wsub(w, (Int)(y >> 1));
+  y = wadd(y, w); w = wshl1(w); w = wsub(w, y);
+  z = wadd(z, x); x = wshl1(x); x = wsub(x, z);
+  y = wadd(y, z); z = wshl1(z); z = wsub(z, y);
+  w = wadd(w, x); x = wshl1(x); x = wsub(x, w);
+}
+
+// decorrelating transform: lines along x (stride 1), y (stride 4), z (16)
+template <int D, typename Int>
+GZ_HD void fwd_xform(Int* q) {
+  constexpr int L = 1 << (2 * (D - 1));  // lines per axis
+#pragma unroll
+  for (int a = 0; a < D; a++) {
+    const int s = 1 << (2 * a);
+#pragma unroll
+    for (int l = 0; l < L; l++) {
+      const int base = (l % s) + (l / s) * s * 4;
+      fwd_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
+    }
+  }
+}
+
+template <int D, typename Int>
+GZ_HD void inv_xform(Int* q) {
+  constexpr int L = 1 << (2 * (D - 1));
+#pragma unroll
+  for (int a = D - 1; a >= 0; a--) {
+    const int s = 1 << (2 * a);
+#pragma unroll
+    for (int l = 0; l < L; l++) {
+      const int base = (l % s) + (l / s) * s * 4;
+      inv_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
+    }
+  }
+}
+
+// ------------------------------------------------------ bit-matrix transpose
+// Transposes every N x N bit tile held in N 32-bit words (N = 4, 16 or 32;
+// 32/N tiles side by side in each word): afterwards bit c of word r in tile
+// g equals bit r of word c in tile g before.  Recursive block swap; the
+// 16- and 8-bit stages are byte permutes.
+
+GZ_HD uint32_t perm_bytes(uint32_t a, uint32_t b, uint32_t sel) {
+#if defined(__CUDA_ARCH__)
+  return __byte_perm(a, b, sel);
+#else
+  uint64_t v = ((uint64_t)b << 32) | a;
+  uint32_t r = 0;
+  for (int i = 0; i < 4; i++) r |= (uint32_t)((v >> (8 * ((sel >> (4 * i)) & 7))) & 0xff) << (8 * i);
+  return r;
+#endif
+}
+
+template <int N>
+GZ_HD void transpose_tiles(uint32_t* t) {
+  if constexpr (N > 16) {
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      uint32_t a = t[k], b = t[k + 16];
+      t[k] = perm_bytes(a, b, 0x5410);       // a.lo16 | b.lo16 << 16
+      t[k + 16] = perm_bytes(a, b, 0x7632);  // a.hi16 | b.hi16 << 16
+    }
+  }
+  if constexpr (N > 8) {
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      if (k & 8) continue;
+      uint32_t a = t[k], b = t[k + 8];
+      t[k] = perm_bytes(a, b, 0x6240);      // bytes a0 b0 a2 b2
+      t[k + 8] = perm_bytes(a, b, 0x7351);  // bytes a1 b1 a3 b3
+    }
+  }
+#pragma unroll
+  for (int j = (N > 4 ? 4 : N / 2); j > 0; j >>= 1) {
+    const uint32_t m = j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u : 0x55555555u;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      if (k & j) continue;
+      uint32_t a = t[k], b = t[k + j];
+      t[k] = (a & m) | ((b << j) & ~m);
+      t[k + j] = ((a >> j) & m) | (b & ~m);
+    }
+  }
+}
+
+// ------------------------------------------------------- transposed planes
+// Bit planes of the 4^D negabinary coefficients.  For integer precision P the
+// coefficients are cut into P/32 32-bit slices G; slice G of coefficient i
+// goes to word tw[G * BS + i] and each run of N = min(BS, 32) words is
+// transposed tile by tile.  Plane k (bit k of every coefficient) is then
+// found in slice G = k / 32 at row (k % 32) % N, tile (k % 32) / N; for
+// BS = 64 the two 32-coefficient halves sit in consecutive runs of 32 words.
+
+template <int D, int P>
+struct Planes {
+  static constexpr int BS = 1 << (2 * D);
+  static constexpr int N = BS < 32 ? BS : 32;
+  static constexpr int NW = BS * (P / 32);
+  uint32_t tw[NW];
+
+  template <typename UInt>
+  GZ_HD void load(const UInt* u, int G) {
+#pragma unroll
+    for (int i = 0; i < BS; i++) tw[G * BS + i] = (uint32_t)((uint64_t)u[i] >> (32 * G));
+  }
+  GZ_HD void transpose(int G) {
+#pragma unroll
+    for (int h = 0; h < BS / N; h++) transpose_tiles<N>(tw + G * BS + h * N);
+  }
+  GZ_HD uint64_t plane(int k) const {
+    const int G = k / 32, kk = k % 32;
+    if constexpr (BS == 64) {
+      return (uint64_t)tw[G * 64 + kk] | ((uint64_t)tw[G * 64 + 32 + kk] << 32);
+    } else {
+      const int r = kk % N, g = kk / N;
+      return (tw[G * BS + r] >> (g * N)) & ((1u << N) - 1);
+    }
+  }
+  GZ_HD void set_plane(int k, uint64_t x) {
+    const int G = k / 32, kk = k % 32;
+    if constexpr (BS == 64) {
+      tw[G * 64 + kk] = (uint32_t)x;
+      tw[G * 64 + 32 + kk] = (uint32_t)(x >> 32);
+    } else {
+      const int r = kk % N, g = kk / N;
+      tw[G * BS + r] |= (uint32_t)x << (g * N);
+    }
+  }
+  template <typename UInt>
+  GZ_HD void store(UInt* u) const {
+#pragma unroll
+    for (int i = 0; i < BS; i++) {
+      uint64_t v = tw[i];
+      if (P == 64) v |= (uint64_t)tw[BS + i] << 32;
+      u[i] = (UInt)v;
+    }
+  }
+};
+
+// ------------------------------------------------------ plane (de)coder
+// One bit plane of the embedded coder of encode_ints (Z/src/template/
+// encode.c:122-151): the first n bits verbatim, then group tests -- a 1 if
+// any bit is left, followed by the run of zeros up to and including the next
+// one bit (a one in the last position is implied) -- and a final 0 test.
+// Output stops when the block's bit budget is spent, exactly where the
+// bit-serial coder stops.
+
+template <int BS, class W>
+GZ_HD void encode_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
+  uint32_t m = n < bits ? n : bits;
+  w.put(x & lowmask64(m), m);
+  bits -= m;
+  uint64_t y = shr64(x, n);
+  while (n < (uint32_t)BS && bits) {
+    if (y == 0) {
+      w.put(0, 1);
+      bits--;
+      break;
+    }
+    uint32_t t = ctz64(y);
+    uint32_t lim = BS - 1 - n;
+    uint64_t pat;
+    uint32_t len, adv;
+    if (t < lim) {  // test 1, t zeros, the one
+      pat = 1u | (2ull << t);
+      len = t + 2;
+      adv = t + 1;
+    } else {  // test 1, zeros up to the implied one in the last position
+      pat = 1;
+      len = lim + 1;
+      adv = BS - n;
+    }
+    uint32_t l = len < bits ? len : bits;
+    w.put(pat & lowmask64(l), l);
+    bits -= l;
+    y = shr64(y, adv);
+    n += adv;
+  }
+}
+
+// Inverse of encode_plane, matching decode_ints (Z/src/template/
+// decode.c:73-105) bit for bit, including its rule that a run cut off by
+// the budget still deposits a one at the current position.
+template <int BS, class R>
+GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
+  uint32_t m = n < bits ? n : bits;
+  uint64_t x = r.read(m);
+  bits -= m;
+  while (n < (uint32_t)BS && bits) {
+    uint64_t w = r.peek64();
+    bits--;
+    if (!(w & 1)) {
+      r.skip(1);
+      break;
+    }
+    uint32_t t = ctz64(w >> 1);
+    uint32_t lim = BS - 1 - n;
+    if (lim > bits) lim = bits;
+    if (t < lim) {
+      r.skip(t + 2);
+      bits -= t + 1;
+      n += t;
+    } else {
+      r.skip(lim + 1);
+      bits -= lim;
+      n += lim;
+    }
+    x |= 1ull << n;
+    n++;
+  }
+  return x;
+}
+
+// --------------------------------------------------------- float <-> bits
+
+GZ_HD float bits_f32(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float f;
+  __builtin_memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+GZ_HD uint32_t f32_bits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t b;
+  __builtin_memcpy(&b, &f, 4);
+  return b;
+#endif
+}
+GZ_HD double bits_f64(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double f;
+  __builtin_memcpy(&f, &b, 8);
+  return f;
+#endif
+}
+GZ_HD uint64_t f64_bits(double f) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(f);
+#else
+  uint64_t b;
+  __builtin_memcpy(&b, &f, 8);
+  return b;
+#endif
+}
+
+// IEEE multiply then truncating float -> int32 conversion that saturates and
+// maps NaN to 0 (cvt.rzi.s32.f32 semantics)
+GZ_HD int32_t mul_to_i32(float s, float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rz(__fmul_rn(s, x));
+#else
+  volatile float v = s * x;
+  float p = v;
+  if (p != p) return 0;
+  if (p >= 2147483648.0f) return INT32_MAX;
+  if (p < -2147483648.0f) return INT32_MIN;
+  return (int32_t)p;
+#endif
+}
+
+GZ_HD float i32_scaled(int32_t q, float s) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(__int2float_rn(q), s);
+#else
+  volatile float v = (float)q * s;
+  return v;
+#endif
+}
+
+GZ_HD double i64_scaled(int64_t q, double s) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(__ll2double_rn(q), s);
+#else
+  volatile double v = (double)q * s;
+  return v;
+#endif
+}
+
+// 2^e as a float / double, exact (denormal or zero below the normal range,
+// as ldexp rounds it)
+GZ_HD float pow2f(int e) {
+  if (e > 127) return bits_f32(0x7f800000u);
+  if (e >= -126) return bits_f32((uint32_t)(e + 127) << 23);
+  if (e >= -149) return bits_f32(1u << (e + 149));
+  return 0.0f;
+}
+GZ_HD double pow2d(int e) {
+  if (e > 1023) return bits_f64(0x7ff0000000000000ull);
+  if (e >= -1022) return bits_f64((uint64_t)(e + 1023) << 52);
+  if (e >= -1074) return bits_f64(1ull << (e + 1074));
+  return 0.0;
+}
+
+// ------------------------------------------------------------- quantise
+// Block-floating-point conversion of Z/src/template/encode.c:36-52:
+// q = (Int)(x * 2^(P-2-emax)).
+
+// f32: the scale multiply is exact, so the hardware float path is used.
+GZ_HD void quantize(const uint32_t* raw, int32_t* q, int n, int emax) {
+  const float s = pow2f(30 - emax);
+  for (int i = 0; i < n; i++) q[i] = mul_to_i32(s, bits_f32(raw[i]));
+}
+
+// f64: shift the significand into place (exact), except in the regime where
+// 2^(62-emax) overflows to +inf, where zfp's product is +-inf or NaN and the
+// conversion saturates (see the oracle's header on defined behaviour).
+GZ_HD void quantize(const uint64_t* raw, int64_t* q, int n, int emax) {
+  if (emax >= 62 - 1023) {
+    const int maxE = emax + 1022;  // biased exponent field of the largest value
+#pragma unroll
+    for (int i = 0; i < n; i++) {
+      uint64_t a = raw[i] & 0x7fffffffffffffffull;
+      uint32_t E = (uint32_t)(a >> 52);
+      uint64_t M = (a & 0xfffffffffffffull) | (E ? (1ull << 52) : 0);
+      int d = maxE - (int)(E ? E : 1);  // >= 0
+      uint64_t mag = d <= 9 ? M << (9 - d) : shr64(M, (uint32_t)(d - 9));
+      q[i] = (raw[i] >> 63) ? (int64_t)(0 - mag) : (int64_t)mag;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < n; i++) {
+      uint64_t a = raw[i] & 0x7fffffffffffffffull;
+      q[i] = a == 0 ? 0 : (raw[i] >> 63) ? INT64_MIN : INT64_MAX;
+    }
+  }
+}
+
+// ----------------------------------------------------------- dequantise
+// Inverse of quantize (Z/src/template/decode.c:9-25): x = (Scalar)q * 2^(emax-(P-2)).
+
+GZ_HD void dequantize(const int32_t* q, uint32_t* raw, int n, int emax) {
+  const float s = pow2f(emax - 30);
+  for (int i = 0; i < n; i++) raw[i] = f32_bits(i32_scaled(q[i], s));
+}
+
+// f64: round-to-nearest-even int64 -> double done in integer arithmetic and
+// the power-of-two scale folded into the exponent, wherever the result is a
+// normal number for every q (-960 <= emax <= 1022); otherwise the FP64 unit.
+GZ_HD void dequantize(const int64_t* q, uint64_t* raw, int n, int emax) {
+  if (emax >= -960 && emax <= 1022) {
+#pragma unroll
+    for (int i = 0; i < n; i++) {
+      uint64_t sign = (uint64_t)q[i] & 0x8000000000000000ull;
+      uint64_t a = sign ? 0 - (uint64_t)q[i] : (uint64_t)q[i];
+      uint32_t lz = clz64(a);
+      uint64_t norm = a << (lz & 63);
+      uint64_t mant = norm >> 11;
+      uint32_t rb = (uint32_t)norm & 0x7ffu;
+      uint64_t up = (rb > 0x400u || (rb == 0x400u && (mant & 1))) ? 1 : 0;
+      uint64_t biased = (uint64_t)(int64_t)(emax - (int)lz + 1024);
+      uint64_t b = ((biased - 1) << 52) + mant + up;
+      raw[i] = a ? (b | sign) : 0;
+    }
+  } else {
+    const double s = pow2d(emax - 62);
+    for (int i = 0; i < n; i++) raw[i] = f64_bits(i64_scaled(q[i], s));
+  }
+}
+
+// ------------------------------------------------------------- block codec
+
+// Encode one block of raw IEEE bit patterns (gathered and padded) into
+// exactly maxbits bits (Z/src/template/encode.c:154-234).
+template <int D, typename T, class W>
+GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w) {
+  typedef FT<T> F;
+  typedef typename F::UInt UInt;
+  typedef typename F::Int Int;
+  constexpr int BS = 1 << (2 * D);
+  constexpr int P = F::P;
+
+  // largest exponent field and a nonzero test, from the IEEE bits
+  uint32_t maxh = 0, orl = 0;
+#pragma unroll
+  for (int i = 0; i < BS; i++) {
+    uint32_t h = (uint32_t)((uint64_t)raw[i] >> (P - 32)) & 0x7fffffffu;
+    maxh = h > maxh ? h : maxh;
+    if (P == 64) orl |= (uint32_t)raw[i];
+  }
+  if ((maxh | orl) == 0) {  // all zero: one 0 bit, zero padding
+    w.zeros(maxbits);
+    return;
+  }
+  const int maxE = (int)(maxh >> (F::MANT - (P - 32)));
+  const int emax = maxE - (F::EBIAS - 1);  // frexp exponent, >= 1 - EBIAS
+  int prec = emax - kMinExp + 2 * D + 2;
+  prec = prec < 0 ? 0 : prec > P ? P : prec;
+  const uint32_t e = (uint32_t)(emax + F::EBIAS);
+  w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
+
+  Int q[BS];
+  quantize(raw, q, BS, emax);
+  fwd_xform<D>(q);
+
+  UInt u[BS];
+#pragma unroll
+  for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
+
+  const uint32_t budget = maxbits - (F::EBITS + 1);
+  uint32_t bits = budget;
+  const int kmin = P - prec;
+  Planes<D, P> pl;
+  pl.load(u, P / 32 - 1);
+  pl.transpose(P / 32 - 1);
+  if (P == 64) pl.load(u, 0);
+  uint32_t n = 0;
+#pragma unroll
+  for (int k = P - 1; k >= 0; k--) {
+    if (k < kmin || bits == 0) break;
+    if (P == 64 && k == 31) pl.transpose(0);
+    encode_plane<BS>(pl.plane(k), n, bits, w);
+  }
+  w.zeros(bits);
+}
+
+// Decode one block from a reader positioned at its first bit into raw IEEE
+// bit patterns (Z/src/template/decode.c:137-165).
+template <int D, typename T, class R>
+GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw) {
+  typedef FT<T> F;
+  typedef typename F::UInt UInt;
+  typedef typename F::Int Int;
+  constexpr int BS = 1 << (2 * D);
+  constexpr int P = F::P;
+
+  uint64_t head = r.peek64();
+  if (!(head & 1)) {
+#pragma unroll
+    for (int i = 0; i < BS; i++) raw[i] = 0;
+    return;
+  }
+  r.skip(F::EBITS + 1);
+  const int emax = (int)((head >> 1) & ((1u << F::EBITS) - 1)) - F::EBIAS;
+  int prec = emax - kMinExp + 2 * D + 2;
+  prec = prec < 0 ? 0 : prec > P ? P : prec;
+  const int kmin = P - prec;
+  uint32_t bits = maxbits - (F::EBITS + 1);
+
+  Planes<D, P> pl;
+#pragma unroll
+  for (int i = 0; i < Planes<D, P>::NW; i++) pl.tw[i] = 0;
+  uint32_t n = 0;
+  bool low = false;  // any plane below 32 decoded
+#pragma unroll
+  for (int k = P - 1; k >= 0; k--) {
+    if (k < kmin || bits == 0) break;
+    pl.set_plane(k, decode_plane<BS>(n, bits, r));
+    if (k < 32) low = true;
+  }
+  pl.transpose(P / 32 - 1);
+  if (P == 64 && low) pl.transpose(0);
+  UInt u[BS];
+  pl.store(u);
+
+  Int q[BS];
+#pragma unroll
+  for (int i = 0; i < BS; i++) q[Perm<D>::at(i)] = (Int)((u[i] ^ (UInt)F::NB) - (UInt)F::NB);
+  inv_xform<D>(q);
+  dequantize(q, raw, BS, emax);
+}
+
+}  // namespace gzfp

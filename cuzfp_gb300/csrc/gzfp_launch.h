@@ -1,0 +1,22 @@
+// gzfp_launch.h -- internal launcher interface between the host API
+// (gzfp_api.cu) and the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gzfp_array.cuh"
+
+namespace gzfp {
+
+// Launch the plain-path encoder / decoder for `dims` (1..3) on stream `s`.
+cudaError_t launch_encode_f32(int dims, const float* in, const Geom& g, uint32_t maxbits,
+                              uint64_t* out, uint64_t nwords, cudaStream_t s);
+cudaError_t launch_encode_f64(int dims, const double* in, const Geom& g, uint32_t maxbits,
+                              uint64_t* out, uint64_t nwords, cudaStream_t s);
+cudaError_t launch_decode_f32(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
+                              uint32_t maxbits, float* out, cudaStream_t s);
+cudaError_t launch_decode_f64(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
+                              uint32_t maxbits, double* out, cudaStream_t s);
+
+}  // namespace gzfp

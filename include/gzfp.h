@@ -1,0 +1,95 @@
+/*
+ * gzfp.h -- C ABI of the GB300 ZFP fixed-rate codec (libgzfp.so).
+ *
+ * Drop-in replacement for the compress / decompress path of cuZFP
+ * (src/cuZFP/cuZFP.h:9-10, implemented in src/cuZFP/cuZFP.cu:174-269): the
+ * same inputs -- array pointer, dimensions, scalar type and rate in bits per
+ * value -- and the same fixed-rate stream as zfp 0.5.0's zfp_compress with
+ * zfp_stream_set_rate(..., wra = 0), bit for bit.
+ *
+ * Plain C types only: pointers, sizes and an opaque CUDA stream handle
+ * (a cudaStream_t passed as void*, NULL = the legacy default stream).
+ * Every function returns a status code and never aborts.
+ *
+ * Pointers may be device or host memory, as in cuZFP (is_gpu_ptr,
+ * src/cuZFP/pointers.cuh:12-22).  When both the array and the stream buffer
+ * are device (or managed) memory the call is asynchronous on `cuda_stream`
+ * and touches nothing else.  When either is host memory the library stages
+ * it through a device workspace it owns, copies results back and
+ * synchronises `cuda_stream` before returning.
+ */
+#ifndef GZFP_H
+#define GZFP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* scalar types: the values of zfp_type (src/cuZFP/zfp_structs.h:31-37) */
+#define GZFP_TYPE_INT32 1
+#define GZFP_TYPE_INT64 2
+#define GZFP_TYPE_FLOAT 3
+#define GZFP_TYPE_DOUBLE 4
+
+/* status codes */
+#define GZFP_OK 0
+#define GZFP_ERR_ARG 1         /* bad dimensions, type, rate, or null pointer */
+#define GZFP_ERR_UNSUPPORTED 2 /* a field or mode this path does not handle */
+#define GZFP_ERR_CAPACITY 3    /* output buffer smaller than needed */
+#define GZFP_ERR_CUDA 4        /* a CUDA runtime call failed; see gzfp_last_error */
+
+/* Library version, major * 10000 + minor * 100 + patch. */
+int gzfp_version(void);
+
+/* Static description of a status code. */
+const char* gzfp_status_string(int status);
+
+/* Detail of the last failure on the calling thread ("" if none). */
+const char* gzfp_last_error(void);
+
+/* Bits per block for `rate` bits per value on a `dims`-dimensional field:
+   floor(4^dims * rate + 0.5), at least 1 + exponent bits.  Replaces
+   stream_set_rate (src/cuZFP/zfp_structs.h:46-76), computed as zfp 0.5.0's
+   zfp_stream_set_rate with wra = 0 (zfp-0.5.0/src/zfp.c:405-430).  Returns 0
+   for an unsupported type or dims outside 1..3. */
+unsigned gzfp_rate_to_maxbits(int type, unsigned dims, double rate);
+
+/* Exact size in bytes of the compressed stream: ceil(blocks * maxbits / 64)
+   64-bit words (zfp_compress's return value, zfp-0.5.0/src/zfp.c:603-630).
+   ny = 0 (and nz = 0) selects 1D, nz = 0 selects 2D.  0 on bad arguments. */
+size_t gzfp_stream_size(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits);
+
+/* Worst-case buffer size as computed by zfp_stream_maximum_size
+   (src/cuZFP/zfp_structs.h:222-251) for a fixed-rate stream of `maxbits`
+   bits per block; includes zfp's 148 header bits. */
+size_t gzfp_maximum_size(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits);
+
+/* Compress the contiguous array a[nz][ny][nx] at `rate` bits per value into
+   `stream` (capacity bytes).  On success *out_bytes (if not NULL) receives
+   the stream size.  Replaces cuZFP::compress (src/cuZFP/cuZFP.cu:174-210). */
+int gzfp_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                  const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                  void* cuda_stream);
+
+/* Decompress `bytes` bytes of `stream` into the contiguous array `data`.
+   Replaces cuZFP::decompress (src/cuZFP/cuZFP.cu:212-269). */
+int gzfp_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                    const void* stream, size_t bytes, void* data, void* cuda_stream);
+
+/* As gzfp_compress / gzfp_decompress, with the block size given directly in
+   bits (zfp_stream.maxbits), as cuZFP's internal::encode / internal::decode
+   take it (src/cuZFP/cuZFP.cu:26-105).  Any maxbits >= 1 + exponent bits
+   (9 for float, 12 for double) up to 1<<20 is accepted. */
+int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                       const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                       void* cuda_stream);
+int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                         const void* stream, size_t bytes, void* data, void* cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GZFP_H */

@@ -1,0 +1,161 @@
+"""Python access to the parity checkers (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module.  It wraps:
+
+* the CPU restatement of zfp 0.5.0 fixed-rate mode (oracle/zfp_oracle.c,
+  built to oracle/_build/libzfp_oracle.so by ``make -C oracle port``), and
+* when present, the reference's own zfp 0.5.0 compiled from the reference
+  tree (oracle/_ref/libzfpref.so, ``make -C oracle ref``), plus its
+  regression fields (oracle/_ref/libzfpfields.so).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libzfp_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libzfpref.so")
+FIELDS_LIB = os.path.join(HERE, "_ref", "libzfpfields.so")
+REF_TREE = os.environ.get("GZFP_REFERENCE_ROOT", "/root/reference")
+
+FLOAT, DOUBLE = 3, 4
+
+_A = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_double]
+
+
+def build_port() -> str:
+    """Compile the restatement (gcc); returns the library path."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref() -> bool:
+    """Compile the reference's zfp sources when the reference tree exists."""
+    if not os.path.isdir(os.path.join(REF_TREE, "src", "thirdparty_builtin", "zfp-0.5.0")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "fields", f"REF_ROOT={REF_TREE}"], check=True)
+    return True
+
+
+_port = None
+_ref = None
+
+
+def port() -> ctypes.CDLL:
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_LIB) or (
+                os.path.getmtime(PORT_LIB) < os.path.getmtime(os.path.join(HERE, "zfp_oracle.c"))):
+            build_port()
+        lib = ctypes.CDLL(PORT_LIB)
+        lib.gzo_compress.restype = ctypes.c_size_t
+        lib.gzo_compress.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                          ctypes.c_int]
+        lib.gzo_decompress.restype = ctypes.c_int
+        lib.gzo_decompress.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                            ctypes.c_int]
+        lib.gzo_stream_bytes.restype = ctypes.c_size_t
+        lib.gzo_stream_bytes.argtypes = _A
+        lib.gzo_maxbits.restype = ctypes.c_uint
+        lib.gzo_maxbits.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        _port = lib
+    return _port
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        lib = ctypes.CDLL(REF_LIB)
+        lib.zref_compress.restype = ctypes.c_size_t
+        lib.zref_compress.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        lib.zref_decompress.restype = ctypes.c_int
+        lib.zref_decompress.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        lib.zref_maximum_size.restype = ctypes.c_size_t
+        lib.zref_maximum_size.argtypes = _A
+        lib.zref_set_rate_bits.restype = ctypes.c_uint
+        lib.zref_set_rate_bits.argtypes = [ctypes.c_int, ctypes.c_uint, ctypes.c_double]
+        _ref = lib
+    return _ref
+
+
+def type_code(dtype) -> int:
+    dt = np.dtype(dtype)
+    if dt == np.float32:
+        return FLOAT
+    if dt == np.float64:
+        return DOUBLE
+    raise ValueError(f"unsupported dtype {dt}")
+
+
+def dims3(shape) -> tuple[int, int, int]:
+    s = tuple(int(v) for v in shape)[::-1]
+    return (s + (0, 0))[:3]
+
+
+def stream_bytes(shape, dtype, rate: float) -> int:
+    nx, ny, nz = dims3(shape)
+    return int(port().gzo_stream_bytes(type_code(dtype), nx, ny, nz, float(rate)))
+
+
+def compress(a: np.ndarray, rate: float, nthreads: int = 1) -> np.ndarray:
+    """Oracle stream (uint64 words) of a C-contiguous 1-3D float array."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    n = stream_bytes(a.shape, a.dtype, rate)
+    out = np.zeros(max(n // 8, 1), np.uint64)
+    got = port().gzo_compress(type_code(a.dtype), nx, ny, nz, float(rate), a.ctypes.data,
+                              out.ctypes.data, out.nbytes, int(nthreads))
+    if got != n:
+        raise RuntimeError("oracle compress failed")
+    return out[: n // 8]
+
+
+def decompress(words: np.ndarray, shape, dtype, rate: float, nthreads: int = 1) -> np.ndarray:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    out = np.zeros(tuple(shape), dtype)
+    nx, ny, nz = dims3(shape)
+    ok = port().gzo_decompress(type_code(dtype), nx, ny, nz, float(rate), words.ctypes.data,
+                               words.nbytes, out.ctypes.data, int(nthreads))
+    if not ok:
+        raise RuntimeError("oracle decompress failed")
+    return out
+
+
+def ref_compress(a: np.ndarray, rate: float) -> np.ndarray:
+    """Stream produced by the reference's own zfp 0.5.0 build."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    t = type_code(a.dtype)
+    cap = int(ref().zref_maximum_size(t, nx, ny, nz, float(rate)))
+    buf = np.zeros(cap // 8 + 1, np.uint64)
+    n = ref().zref_compress(t, nx, ny, nz, float(rate), a.ctypes.data, buf.ctypes.data, cap)
+    return buf[: n // 8]
+
+
+def ref_decompress(words: np.ndarray, shape, dtype, rate: float) -> np.ndarray:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    out = np.zeros(tuple(shape), dtype)
+    nx, ny, nz = dims3(shape)
+    ref().zref_decompress(type_code(dtype), nx, ny, nz, float(rate), words.ctypes.data,
+                          words.nbytes, out.ctypes.data)
+    return out
+
+
+def ref_fields():
+    """The reference's regression input arrays (Z/tests/fields.c), as
+    (float32[3, 4096], float64[3, 4096]); None when not built."""
+    if not os.path.exists(FIELDS_LIB):
+        return None
+    lib = ctypes.CDLL(FIELDS_LIB)
+    af = np.ctypeslib.as_array((ctypes.c_float * (3 * 4096)).in_dll(lib, "array_float"))
+    ad = np.ctypeslib.as_array((ctypes.c_double * (3 * 4096)).in_dll(lib, "array_double"))
+    return af.reshape(3, 4096).copy(), ad.reshape(3, 4096).copy()

@@ -1,0 +1,568 @@
+/*
+ * zfp_oracle.c -- CPU restatement of the zfp 0.5.0 fixed-rate codec.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA
+ * codec in cuzfp_gb300/csrc and the timed CPU baseline ("port") of bench.py.
+ * Nothing in the product library links, loads or calls it.
+ *
+ * It restates, in independent code, the algorithm of the zfp 0.5.0 sources
+ * vendored by cuZFP under src/thirdparty_builtin/zfp-0.5.0 (abbreviated Z/):
+ *
+ *   rate -> bits per block          Z/src/zfp.c:405-430  (wra = 0)
+ *   exponent / exponent_block       Z/src/template/encode.c:10-33
+ *   fwd_cast (block floating point) Z/src/template/encode.c:36-52
+ *   pad_block                       Z/src/template/encode.c:55-74
+ *   fwd_lift                        Z/src/template/encode.c:77-103
+ *   int2uint / fwd_order            Z/src/template/encode.c:106-119
+ *   encode_ints (bit-plane coder)   Z/src/template/encode.c:122-151
+ *   encode_block / zfp_encode_block Z/src/template/encode.c:154-234
+ *   precision()                     Z/src/template/codec{1,2,3}.c
+ *   perm_1 / perm_2 / perm_3        Z/src/template/codec{1,2,3}.c
+ *   fwd_xform / gather_partial      Z/src/template/encode{1,2,3}.c
+ *   block loops (z, y, x order)     Z/src/template/compress.c:1-104
+ *   inverse path                    Z/src/template/decode.c:9-165,
+ *                                   Z/src/template/decode{1,2,3}.c,
+ *                                   Z/src/template/decompress.c
+ *   bit stream (LSB-first u64)      Z/src/inline/bitstream.c:195-373
+ *   stream_flush / returned size    Z/src/zfp.c:603-630
+ *
+ * Parity is pinned two ways (see tests/test_oracle.py): against a build of
+ * the reference's own zfp sources (oracle/_ref, built by oracle/Makefile in
+ * a checkout that has the reference) and against committed golden streams in
+ * tests/golden that were produced by that build.
+ *
+ * Defined behaviour where zfp 0.5.0 relies on C undefined behaviour: when a
+ * block's largest magnitude is so small that the quantisation scale
+ * 2^(P-2-emax) overflows to +inf (f32: emax < -97, f64: emax < -961), zfp
+ * casts +-inf / NaN to an integer.  This restatement performs the IEEE-754
+ * saturating conversion (+inf -> INT_MAX, -inf -> INT_MIN, NaN -> 0), which is
+ * what the reference computes on AArch64 hosts and what CUDA's cvt.rzi does.
+ * An x86-64 build of zfp 0.5.0 yields INT_MIN for every value instead.
+ * Non-finite inputs (inf, NaN) are outside the codec's domain.
+ *
+ * The multi-threaded entry points split the block sequence into chunks of a
+ * multiple of 64 blocks, so every chunk starts on a 64-bit word boundary of
+ * the fixed-rate stream; output is byte-identical to the serial path.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define GZO_FLOAT 3  /* zfp_type_float  (Z/inc/zfp.h:107-113) */
+#define GZO_DOUBLE 4 /* zfp_type_double */
+#define GZO_MIN_EXP (-1074)
+
+/* ---------------------------------------------------------------- bits --- */
+
+typedef struct {
+  uint64_t* words; /* word array */
+  size_t pos;      /* next word index */
+  uint64_t acc;    /* pending bits (LSB first) */
+  unsigned fill;   /* number of pending bits, < 64 */
+} wbits;
+
+static void w_init(wbits* w, uint64_t* words, size_t bitoff) {
+  /* bitoff is a multiple of 64 for every caller */
+  w->words = words;
+  w->pos = bitoff / 64;
+  w->acc = 0;
+  w->fill = 0;
+}
+
+/* append the low n (0..64) bits of v */
+static void w_put(wbits* w, uint64_t v, unsigned n) {
+  if (n == 0) return;
+  if (n < 64) v &= ((uint64_t)1 << n) - 1;
+  w->acc |= v << w->fill;
+  if (w->fill + n >= 64) {
+    w->words[w->pos++] = w->acc;
+    unsigned used = 64 - w->fill; /* bits of v consumed by that word */
+    w->acc = used < 64 ? v >> used : 0;
+    w->fill = w->fill + n - 64;
+  } else {
+    w->fill += n;
+  }
+}
+
+static void w_zeros(wbits* w, size_t n) {
+  while (n >= 64) { w_put(w, 0, 64); n -= 64; }
+  w_put(w, 0, (unsigned)n);
+}
+
+static void w_flush(wbits* w) {
+  if (w->fill) { w->words[w->pos++] = w->acc; w->acc = 0; w->fill = 0; }
+}
+
+typedef struct {
+  const uint64_t* words;
+  size_t bit; /* absolute bit position of the next bit */
+} rbits;
+
+static uint64_t r_get(rbits* r, unsigned n) {
+  if (n == 0) return 0;
+  size_t wi = r->bit / 64;
+  unsigned sh = (unsigned)(r->bit % 64);
+  uint64_t v = r->words[wi] >> sh;
+  if (sh && sh + n > 64) v |= r->words[wi + 1] << (64 - sh);
+  r->bit += n;
+  if (n < 64) v &= ((uint64_t)1 << n) - 1;
+  return v;
+}
+
+/* --------------------------------------------------------- permutations --- */
+
+/* sequency order of the coefficients: sort (i,j,k) by i+j+k, then by
+   i^2+j^2+k^2; the exact tie order is that of Z/src/template/codec3.c:4-88 and
+   codec2.c:4-30 and is reproduced here as index tables */
+static const unsigned char PERM1[4] = {0, 1, 2, 3};
+static const unsigned char PERM2[16] = {0, 1, 4, 5, 2, 8, 6, 9, 3, 12, 10, 7, 13, 11, 14, 15};
+static const unsigned char PERM3[64] = {
+    0,  1,  4,  16, 20, 17, 5,  2,  8,  32, 21, 6,  18, 24, 9,  33,
+    36, 3,  12, 48, 22, 25, 37, 40, 34, 10, 7,  19, 28, 13, 49, 52,
+    41, 38, 26, 23, 29, 53, 11, 35, 44, 14, 50, 56, 42, 27, 39, 45,
+    30, 54, 57, 60, 51, 15, 43, 46, 58, 61, 55, 31, 62, 59, 47, 63};
+
+static const unsigned char* perm_for(int dims) {
+  return dims == 1 ? PERM1 : dims == 2 ? PERM2 : PERM3;
+}
+
+/* ------------------------------------------------------------ lifting ---- */
+
+/* Lifting steps in wrap-around integer arithmetic; ">>" is the arithmetic
+   shift of zfp's signed Int (Z/src/template/encode.c:77-103,
+   decode.c:28-54).  Wrapping only matters for streams that do not come from
+   the encoder, where zfp's signed overflow is undefined in C. */
+#define ADD64(a, b) ((int64_t)((uint64_t)(a) + (uint64_t)(b)))
+#define SUB64(a, b) ((int64_t)((uint64_t)(a) - (uint64_t)(b)))
+#define SHL64(a) ((int64_t)((uint64_t)(a) << 1))
+#define ADD32(a, b) ((int32_t)((uint32_t)(a) + (uint32_t)(b)))
+#define SUB32(a, b) ((int32_t)((uint32_t)(a) - (uint32_t)(b)))
+#define SHL32(a) ((int32_t)((uint32_t)(a) << 1))
+
+static void lift_fwd(int64_t* p, int s) {
+  int64_t x = p[0], y = p[s], z = p[2 * s], w = p[3 * s];
+  x = ADD64(x, w); x >>= 1; w = SUB64(w, x);
+  z = ADD64(z, y); z >>= 1; y = SUB64(y, z);
+  x = ADD64(x, z); x >>= 1; z = SUB64(z, x);
+  w = ADD64(w, y); w >>= 1; y = SUB64(y, w);
+  w = ADD64(w, y >> 1); y = SUB64(y, w >> 1);
+  p[0] = x; p[s] = y; p[2 * s] = z; p[3 * s] = w;
+}
+
+static void lift_inv(int64_t* p, int s) {
+  int64_t x = p[0], y = p[s], z = p[2 * s], w = p[3 * s];
+  y = ADD64(y, w >> 1); w = SUB64(w, y >> 1);
+  y = ADD64(y, w); w = SHL64(w); w = SUB64(w, y);
+  z = ADD64(z, x); x = SHL64(x); x = SUB64(x, z);
+  y = ADD64(y, z); z = SHL64(z); z = SUB64(z, y);
+  w = ADD64(w, x); x = SHL64(x); x = SUB64(x, w);
+  p[0] = x; p[s] = y; p[2 * s] = z; p[3 * s] = w;
+}
+
+static void lift_fwd32(int32_t* p, int s) {
+  int32_t x = p[0], y = p[s], z = p[2 * s], w = p[3 * s];
+  x = ADD32(x, w); x >>= 1; w = SUB32(w, x);
+  z = ADD32(z, y); z >>= 1; y = SUB32(y, z);
+  x = ADD32(x, z); x >>= 1; z = SUB32(z, x);
+  w = ADD32(w, y); w >>= 1; y = SUB32(y, w);
+  w = ADD32(w, y >> 1); y = SUB32(y, w >> 1);
+  p[0] = x; p[s] = y; p[2 * s] = z; p[3 * s] = w;
+}
+
+static void lift_inv32(int32_t* p, int s) {
+  int32_t x = p[0], y = p[s], z = p[2 * s], w = p[3 * s];
+  y = ADD32(y, w >> 1); w = SUB32(w, y >> 1);
+  y = ADD32(y, w); w = SHL32(w); w = SUB32(w, y);
+  z = ADD32(z, x); x = SHL32(x); x = SUB32(x, z);
+  y = ADD32(y, z); z = SHL32(z); z = SUB32(z, y);
+  w = ADD32(w, x); x = SHL32(x); x = SUB32(x, w);
+  p[0] = x; p[s] = y; p[2 * s] = z; p[3 * s] = w;
+}
+
+/* the 1D/2D/3D transforms: x lines (stride 1), then y (stride 4), then z
+   (stride 16); the inverse runs z, y, x */
+static void xform(void* blk, int dims, int wide, int inverse) {
+  int n = 1 << (2 * dims);
+  int lines = n / 4;
+  int axis, a, l;
+  for (a = 0; a < dims; a++) {
+    axis = inverse ? dims - 1 - a : a;
+    int stride = 1 << (2 * axis);
+    for (l = 0; l < lines; l++) {
+      /* l enumerates the coordinates other than `axis` */
+      int lo = l % stride;
+      int hi = l / stride;
+      int base = lo + hi * stride * 4;
+      if (wide) {
+        int64_t* p = (int64_t*)blk + base;
+        if (inverse) lift_inv(p, stride); else lift_fwd(p, stride);
+      } else {
+        int32_t* p = (int32_t*)blk + base;
+        if (inverse) lift_inv32(p, stride); else lift_fwd32(p, stride);
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------- params ---- */
+
+typedef struct {
+  int type, dims;
+  unsigned nx, ny, nz; /* per-axis sizes (1 for unused axes) */
+  unsigned bx, by, bz; /* blocks per axis */
+  unsigned maxbits;
+  int P;      /* bits per integer: 32 or 64 */
+  int ebits;  /* exponent bits: 8 or 11 */
+  int ebias;  /* 127 or 1023 */
+} params;
+
+unsigned gzo_maxbits(int type, int dims, double rate) {
+  unsigned n = 1u << (2 * dims);
+  unsigned bits = (unsigned)floor(n * rate + 0.5);
+  unsigned lo = type == GZO_FLOAT ? 9u : 12u;
+  return bits < lo ? lo : bits;
+}
+
+static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
+  if (type != GZO_FLOAT && type != GZO_DOUBLE) return 0;
+  if (nx == 0) return 0;
+  p->dims = nz ? 3 : ny ? 2 : 1;
+  if (nz && !ny) return 0;
+  p->type = type;
+  p->nx = nx; p->ny = ny ? ny : 1; p->nz = nz ? nz : 1;
+  p->bx = (p->nx + 3) / 4; p->by = (p->ny + 3) / 4; p->bz = (p->nz + 3) / 4;
+  p->maxbits = gzo_maxbits(type, p->dims, rate);
+  p->P = type == GZO_FLOAT ? 32 : 64;
+  p->ebits = type == GZO_FLOAT ? 8 : 11;
+  p->ebias = (1 << (p->ebits - 1)) - 1;
+  return 1;
+}
+
+size_t gzo_stream_bytes(int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
+  params p;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  uint64_t blocks = (uint64_t)p.bx * p.by * p.bz;
+  return (size_t)((blocks * p.maxbits + 63) / 64 * 8);
+}
+
+/* ------------------------------------------------------------- encoder --- */
+
+/* IEEE-754 saturating float->int conversion (see the header comment) */
+static int64_t sat_i64(double v) {
+  if (v != v) return 0;
+  if (v >= 9223372036854775808.0) return INT64_MAX;
+  if (v < -9223372036854775808.0) return INT64_MIN;
+  return (int64_t)v;
+}
+static int32_t sat_i32(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483648.0f) return INT32_MAX;
+  if (v < -2147483648.0f) return INT32_MIN;
+  return (int32_t)v;
+}
+
+/* the embedded bit-plane coder; returns bits written (<= budget) */
+static unsigned encode_planes(wbits* w, unsigned budget, int intprec, int kmin,
+                              const uint64_t* u, int size) {
+  unsigned bits = budget;
+  int k = intprec, n = 0;
+  while (bits && k-- > kmin) {
+    uint64_t x = 0;
+    int i;
+    for (i = 0; i < size; i++) x |= ((u[i] >> k) & 1u) << i;
+    /* first n bits of the plane go out verbatim */
+    unsigned m = (unsigned)n < bits ? (unsigned)n : bits;
+    bits -= m;
+    w_put(w, x, m);
+    x = m < 64 ? x >> m : 0;
+    /* group tests: is anything left in the plane?  then a unary run up to
+       the next one bit; a one in the last position is implied */
+    while (n < size && bits) {
+      bits--;
+      unsigned any = x != 0;
+      w_put(w, any, 1);
+      if (!any) break;
+      while (n < size - 1 && bits) {
+        bits--;
+        unsigned b = (unsigned)(x & 1u);
+        w_put(w, b, 1);
+        if (b) break;
+        x >>= 1;
+        n++;
+      }
+      x >>= 1;
+      n++;
+    }
+  }
+  return budget - bits;
+}
+
+static void encode_block(wbits* w, const params* p, const void* fblock) {
+  int size = 1 << (2 * p->dims);
+  int i;
+  /* largest magnitude -> common exponent (frexp convention) */
+  int emax;
+  if (p->type == GZO_FLOAT) {
+    const float* f = (const float*)fblock;
+    float mx = 0;
+    for (i = 0; i < size; i++) { float a = fabsf(f[i]); if (mx < a) mx = a; }
+    if (mx > 0) { int e; frexpf(mx, &e); emax = e < 1 - p->ebias ? 1 - p->ebias : e; }
+    else emax = -p->ebias;
+  } else {
+    const double* f = (const double*)fblock;
+    double mx = 0;
+    for (i = 0; i < size; i++) { double a = fabs(f[i]); if (mx < a) mx = a; }
+    if (mx > 0) { int e; frexp(mx, &e); emax = e < 1 - p->ebias ? 1 - p->ebias : e; }
+    else emax = -p->ebias;
+  }
+  int prec = emax - GZO_MIN_EXP + 2 * p->dims + 2;
+  if (prec < 0) prec = 0;
+  if (prec > p->P) prec = p->P;
+  unsigned e = prec ? (unsigned)(emax + p->ebias) : 0;
+  if (!e) {
+    /* all-zero block: one 0 bit, then zero padding up to maxbits */
+    w_zeros(w, p->maxbits);
+    return;
+  }
+  unsigned hbits = (unsigned)p->ebits + 1;
+  w_put(w, 2 * (uint64_t)e + 1, hbits);
+  uint64_t u[64];
+  const unsigned char* perm = perm_for(p->dims);
+  if (p->type == GZO_FLOAT) {
+    int32_t q[64];
+    const float* f = (const float*)fblock;
+    float s = ldexpf(1.0f, p->P - 2 - emax);
+    for (i = 0; i < size; i++) q[i] = sat_i32(s * f[i]);
+    xform(q, p->dims, 0, 0);
+    for (i = 0; i < size; i++)
+      u[i] = (uint32_t)(((uint32_t)q[perm[i]] + 0xaaaaaaaau) ^ 0xaaaaaaaau);
+  } else {
+    int64_t q[64];
+    const double* f = (const double*)fblock;
+    double s = ldexp(1.0, p->P - 2 - emax);
+    for (i = 0; i < size; i++) q[i] = sat_i64(s * f[i]);
+    xform(q, p->dims, 1, 0);
+    for (i = 0; i < size; i++)
+      u[i] = ((uint64_t)q[perm[i]] + 0xaaaaaaaaaaaaaaaaull) ^ 0xaaaaaaaaaaaaaaaaull;
+  }
+  unsigned budget = p->maxbits - hbits;
+  unsigned used = encode_planes(w, budget, p->P, p->P - prec, u, size);
+  w_zeros(w, budget - used);
+}
+
+/* pad rule of Z/src/template/encode.c:55-74 expressed as an index map */
+static unsigned padmap(unsigned n, unsigned i) {
+  static const unsigned char map[5][4] = {
+      {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 1, 1, 0}, {0, 1, 2, 0}, {0, 1, 2, 3}};
+  return map[n][i];
+}
+
+static void gather(const params* p, const void* data, unsigned bx, unsigned by, unsigned bz,
+                   void* blk) {
+  unsigned cx = p->nx - 4 * bx, cy = p->ny - 4 * by, cz = p->nz - 4 * bz;
+  cx = cx > 4 ? 4 : cx; cy = cy > 4 ? 4 : cy; cz = cz > 4 ? 4 : cz;
+  unsigned dz = p->dims == 3 ? 4 : 1, dy = p->dims >= 2 ? 4 : 1;
+  unsigned x, y, z;
+  for (z = 0; z < dz; z++)
+    for (y = 0; y < dy; y++)
+      for (x = 0; x < 4; x++) {
+        size_t gx = 4 * bx + padmap(cx, x);
+        size_t gy = p->dims >= 2 ? 4 * by + padmap(cy, y) : 0;
+        size_t gz = p->dims == 3 ? 4 * bz + padmap(cz, z) : 0;
+        size_t idx = gx + p->nx * (gy + (size_t)p->ny * gz);
+        unsigned o = x + 4 * y + 16 * z;
+        if (p->type == GZO_FLOAT) ((float*)blk)[o] = ((const float*)data)[idx];
+        else ((double*)blk)[o] = ((const double*)data)[idx];
+      }
+}
+
+/* ------------------------------------------------------------- decoder --- */
+
+static void decode_planes(rbits* r, unsigned budget, int intprec, int kmin, uint64_t* u,
+                          int size) {
+  unsigned bits = budget;
+  int k = intprec, n = 0, i;
+  for (i = 0; i < size; i++) u[i] = 0;
+  while (bits && k-- > kmin) {
+    unsigned m = (unsigned)n < bits ? (unsigned)n : bits;
+    bits -= m;
+    uint64_t x = r_get(r, m);
+    while (n < size && bits) {
+      bits--;
+      if (!r_get(r, 1)) break;
+      while (n < size - 1 && bits) {
+        bits--;
+        if (r_get(r, 1)) break;
+        n++;
+      }
+      /* a one at position n: read, implied by position, or assumed when the
+         budget ran out (Z/src/template/decode.c:94-98) */
+      x += (uint64_t)1 << n;
+      n++;
+    }
+    for (i = 0; x; i++, x >>= 1) u[i] += (x & 1u) << k;
+  }
+}
+
+static void decode_block(rbits* r, const params* p, void* fblock) {
+  int size = 1 << (2 * p->dims);
+  int i;
+  size_t start = r->bit;
+  if (!r_get(r, 1)) {
+    if (p->type == GZO_FLOAT) for (i = 0; i < size; i++) ((float*)fblock)[i] = 0;
+    else for (i = 0; i < size; i++) ((double*)fblock)[i] = 0;
+    r->bit = start + p->maxbits;
+    return;
+  }
+  unsigned hbits = (unsigned)p->ebits + 1;
+  int emax = (int)r_get(r, (unsigned)p->ebits) - p->ebias;
+  int prec = emax - GZO_MIN_EXP + 2 * p->dims + 2;
+  if (prec < 0) prec = 0;
+  if (prec > p->P) prec = p->P;
+  uint64_t u[64];
+  decode_planes(r, p->maxbits - hbits, p->P, p->P - prec, u, size);
+  r->bit = start + p->maxbits;
+  const unsigned char* perm = perm_for(p->dims);
+  if (p->type == GZO_FLOAT) {
+    int32_t q[64];
+    for (i = 0; i < size; i++)
+      q[perm[i]] = (int32_t)(((uint32_t)u[i] ^ 0xaaaaaaaau) - 0xaaaaaaaau);
+    xform(q, p->dims, 0, 1);
+    float s = ldexpf(1.0f, emax - (p->P - 2));
+    for (i = 0; i < size; i++) ((float*)fblock)[i] = s * (float)q[i];
+  } else {
+    int64_t q[64];
+    for (i = 0; i < size; i++)
+      q[perm[i]] = (int64_t)((u[i] ^ 0xaaaaaaaaaaaaaaaaull) - 0xaaaaaaaaaaaaaaaaull);
+    xform(q, p->dims, 1, 1);
+    double s = ldexp(1.0, emax - (p->P - 2));
+    for (i = 0; i < size; i++) ((double*)fblock)[i] = s * (double)q[i];
+  }
+}
+
+static void scatter(const params* p, void* data, unsigned bx, unsigned by, unsigned bz,
+                    const void* blk) {
+  unsigned cx = p->nx - 4 * bx, cy = p->ny - 4 * by, cz = p->nz - 4 * bz;
+  cx = cx > 4 ? 4 : cx; cy = cy > 4 ? 4 : cy; cz = cz > 4 ? 4 : cz;
+  if (p->dims < 3) cz = 1;
+  if (p->dims < 2) cy = 1;
+  unsigned x, y, z;
+  for (z = 0; z < cz; z++)
+    for (y = 0; y < cy; y++)
+      for (x = 0; x < cx; x++) {
+        size_t idx = (4 * bx + x) + p->nx * ((4 * by + y) + (size_t)p->ny * (4 * bz + z));
+        unsigned o = x + 4 * y + 16 * z;
+        if (p->type == GZO_FLOAT) ((float*)data)[idx] = ((const float*)blk)[o];
+        else ((double*)data)[idx] = ((const double*)blk)[o];
+      }
+}
+
+/* ------------------------------------------------------------- drivers --- */
+
+typedef struct {
+  const params* p;
+  const void* data;
+  void* out;
+  uint64_t* stream;
+  const uint64_t* istream;
+  uint64_t b0, b1; /* block range [b0, b1) */
+} job;
+
+static void* encode_range(void* arg) {
+  job* j = (job*)arg;
+  const params* p = j->p;
+  wbits w;
+  w_init(&w, j->stream, (size_t)(j->b0 * p->maxbits));
+  double blk[64];
+  uint64_t b;
+  for (b = j->b0; b < j->b1; b++) {
+    unsigned bx = (unsigned)(b % p->bx);
+    unsigned by = (unsigned)((b / p->bx) % p->by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p->bx * p->by));
+    gather(p, j->data, bx, by, bz, blk);
+    encode_block(&w, p, blk);
+  }
+  w_flush(&w);
+  return 0;
+}
+
+static void* decode_range(void* arg) {
+  job* j = (job*)arg;
+  const params* p = j->p;
+  rbits r;
+  r.words = j->istream;
+  r.bit = (size_t)(j->b0 * p->maxbits);
+  double blk[64];
+  uint64_t b;
+  for (b = j->b0; b < j->b1; b++) {
+    unsigned bx = (unsigned)(b % p->bx);
+    unsigned by = (unsigned)((b / p->bx) % p->by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p->bx * p->by));
+    decode_block(&r, p, blk);
+    scatter(p, j->out, bx, by, bz, blk);
+  }
+  return 0;
+}
+
+static void run_jobs(const params* p, job* proto, uint64_t nblocks, int nthreads,
+                     void* (*fn)(void*)) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  /* chunks of a multiple of 64 blocks start on word boundaries */
+  uint64_t per = (nblocks + (uint64_t)nthreads - 1) / (uint64_t)nthreads;
+  per = (per + 63) / 64 * 64;
+  if (per == 0) per = 64;
+  pthread_t th[256];
+  job jobs[256];
+  int t, started = 0;
+  for (t = 0; t < nthreads; t++) {
+    jobs[t] = *proto;
+    jobs[t].b0 = per * (uint64_t)t;
+    jobs[t].b1 = jobs[t].b0 + per;
+    if (jobs[t].b0 >= nblocks) break;
+    if (jobs[t].b1 > nblocks) jobs[t].b1 = nblocks;
+  }
+  started = t;
+  if (started == 1) { fn(&jobs[0]); return; }
+  for (t = 0; t < started; t++) pthread_create(&th[t], 0, fn, &jobs[t]);
+  for (t = 0; t < started; t++) pthread_join(th[t], 0);
+  (void)p;
+}
+
+/* Compress a contiguous a[nz][ny][nx] array (ny = nz = 0 for 1D, nz = 0 for
+   2D) at `rate` bits per value.  Returns the stream size in bytes (a whole
+   number of 64-bit words), or 0 on a bad argument or short buffer. */
+size_t gzo_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                    const void* data, void* stream, size_t capacity, int nthreads) {
+  params p;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  size_t bytes = gzo_stream_bytes(type, nx, ny, nz, rate);
+  if (capacity < bytes) return 0;
+  uint64_t nblocks = (uint64_t)p.bx * p.by * p.bz;
+  job proto;
+  memset(&proto, 0, sizeof proto);
+  proto.p = &p;
+  proto.data = data;
+  proto.stream = (uint64_t*)stream;
+  run_jobs(&p, &proto, nblocks, nthreads, encode_range);
+  return bytes;
+}
+
+/* Decompress a stream made by gzo_compress (or zfp 0.5.0 in fixed-rate mode)
+   into a contiguous array.  Returns 1 on success, 0 on a bad argument. */
+int gzo_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                   const void* stream, size_t bytes, void* data, int nthreads) {
+  params p;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  if (bytes < gzo_stream_bytes(type, nx, ny, nz, rate)) return 0;
+  uint64_t nblocks = (uint64_t)p.bx * p.by * p.bz;
+  job proto;
+  memset(&proto, 0, sizeof proto);
+  proto.p = &p;
+  proto.out = data;
+  proto.istream = (const uint64_t*)stream;
+  run_jobs(&p, &proto, nblocks, nthreads, decode_range);
+  return 1;
+}

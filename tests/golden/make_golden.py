@@ -1,0 +1,94 @@
+"""Regenerate the golden fixtures from the reference's own zfp 0.5.0 build.
+
+Run in a checkout that has the reference tree (the build reads its zfp
+sources):  python tests/golden/make_golden.py
+Writes tests/golden/small_cases.npz and tests/golden/manifest.json.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as orc  # noqa: E402
+from tests import cases, golden_io  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def main() -> None:
+    if not orc.build_ref():
+        raise SystemExit("reference tree not found; cannot regenerate golden fixtures")
+    # small cases, stored in full
+    rng = np.random.default_rng(20261203)
+    arrays = {}
+    k = 0
+    while k < 24:
+        a, rate = cases.random_case(rng, max_edge=(200, 24, 10))
+        if cases.has_saturating_blocks(a):
+            continue
+        s = orc.ref_compress(a, rate)
+        d = orc.ref_decompress(s, a.shape, a.dtype, rate)
+        nm = f"rand{k:02d}_{a.ndim}d_{a.dtype.name}"
+        arrays[nm + "__input"] = a
+        arrays[nm + "__stream"] = s
+        arrays[nm + "__output"] = d
+        arrays[nm + "__rate"] = np.array(rate)
+        k += 1
+    for i, (a, rate) in enumerate(cases.edge_cases()):
+        if cases.has_saturating_blocks(a):
+            continue
+        s = orc.ref_compress(a, rate)
+        d = orc.ref_decompress(s, a.shape, a.dtype, rate)
+        nm = f"edge{i:02d}_{a.ndim}d_{a.dtype.name}"
+        arrays[nm + "__input"] = a
+        arrays[nm + "__stream"] = s
+        arrays[nm + "__output"] = d
+        arrays[nm + "__rate"] = np.array(rate)
+    np.savez_compressed(os.path.join(OUT, "small_cases.npz"), **arrays)
+
+    # generated cases, stored as digests
+    specs = []
+    for dt in ("float32", "float64"):
+        for d in (1, 2, 3):
+            rates = (2, 8, 32) if dt == "float32" else (1, 4, 16, 64)
+            for r in rates:
+                specs.append({"name": f"testzfp_{d}d_{dt}_r{r}", "gen": "testzfp", "dims": d,
+                              "dtype": dt, "rate": r})
+    specs.append({"name": "smooth_noisy_64cube_f32_r16", "gen": "smooth_noisy_3d", "n": 64,
+                  "seed": 0, "dtype": "float32", "rate": 16})
+    for r in (8, 16, 32):
+        specs.append({"name": f"sinusoids_36cube_f64_r{r}", "gen": "sinusoids",
+                      "shape": [36, 37, 38], "count": 16, "kmax": 32, "seed": 1,
+                      "dtype": "float64", "rate": r})
+    for r in (4, 12, 24):
+        specs.append({"name": f"walk_1d_f32_r{r}", "gen": "random_walk", "n": 100003, "seed": 2,
+                      "dtype": "float32", "rate": r})
+        specs.append({"name": f"sinusoids_2d_f32_r{r}", "gen": "sinusoids", "shape": [253, 255],
+                      "count": 8, "kmax": 64, "seed": 3, "dtype": "float32", "rate": r})
+        specs.append({"name": f"sinusoids_2d_f64_r{r}", "gen": "sinusoids", "shape": [127, 126],
+                      "count": 8, "kmax": 64, "seed": 4, "dtype": "float64", "rate": r})
+    for sp in specs:
+        a = golden_io.generate(sp)
+        s = orc.ref_compress(a, sp["rate"])
+        d = orc.ref_decompress(s, a.shape, a.dtype, sp["rate"])
+        sp["shape_out"] = list(a.shape)
+        sp["input_sha256"] = golden_io.sha(a)
+        sp["stream_bytes"] = int(s.nbytes)
+        sp["stream_sha256"] = golden_io.sha(s)
+        sp["output_sha256"] = golden_io.sha(d)
+    with open(os.path.join(OUT, "manifest.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py",
+                   "reference": "zfp 0.5.0 as vendored by cuZFP (src/thirdparty_builtin/zfp-0.5.0),"
+                                " built by oracle/Makefile",
+                   "cases": specs}, f, indent=1)
+    print(f"{len([k for k in arrays if k.endswith('__rate')])} small cases, {len(specs)} manifest cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+// host_codec.cpp -- test-only host build of the per-thread kernel code.
+//
+// Compiles cuzfp_gb300/csrc/gzfp_array.cuh (the exact per-block code that the
+// CUDA kernels run, one block per thread) for the CPU and runs it block by
+// block, so the CPU test suite can compare the kernel logic with the oracle
+// without a GPU.  It is never part of the product library.
+#include <stddef.h>
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+
+#include "../../cuzfp_gb300/csrc/gzfp_array.cuh"
+
+namespace {
+
+struct HostWords {
+  uint64_t* out;       // writer target (pre-zeroed)
+  const uint64_t* in;  // reader source
+  uint64_t n;          // words available
+  void store(uint64_t i, uint64_t v) { out[i] = v; }
+  void merge(uint64_t i, uint64_t v) { out[i] |= v; }
+  uint64_t load(uint64_t i) const { return i < n ? in[i] : 0; }
+};
+
+bool geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
+  if (!nx || (nz && !ny)) return false;
+  dims = nz ? 3 : ny ? 2 : 1;
+  g.nx = nx; g.ny = ny ? ny : 1; g.nz = nz ? nz : 1;
+  g.bx = (g.nx + 3) / 4; g.by = (g.ny + 3) / 4; g.bz = (g.nz + 3) / 4;
+  g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  return true;
+}
+
+unsigned maxbits_for(int type, int dims, double rate) {
+  unsigned bits = (unsigned)floor((1 << (2 * dims)) * rate + 0.5);
+  unsigned lo = type == 3 ? 9u : 12u;
+  return bits < lo ? lo : bits;
+}
+
+template <int D, typename T>
+void enc(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out, uint64_t words) {
+  HostWords w{out, nullptr, words};
+  for (uint64_t b = 0; b < g.nblocks; b++) gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w);
+}
+
+template <int D, typename T>
+void dec(const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbits, void* data) {
+  HostWords w{nullptr, in, words};
+  for (uint64_t b = 0; b < g.nblocks; b++) gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w);
+}
+
+}  // namespace
+
+extern "C" size_t hc_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                              const void* data, uint64_t* out, size_t cap) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || (type != 3 && type != 4)) return 0;
+  unsigned maxbits = maxbits_for(type, dims, rate);
+  uint64_t words = (g.nblocks * maxbits + 63) / 64;
+  if (cap < words * 8) return 0;
+  memset(out, 0, words * 8);
+  if (type == 3) {
+    if (dims == 1) enc<1, float>(data, g, maxbits, out, words);
+    if (dims == 2) enc<2, float>(data, g, maxbits, out, words);
+    if (dims == 3) enc<3, float>(data, g, maxbits, out, words);
+  } else {
+    if (dims == 1) enc<1, double>(data, g, maxbits, out, words);
+    if (dims == 2) enc<2, double>(data, g, maxbits, out, words);
+    if (dims == 3) enc<3, double>(data, g, maxbits, out, words);
+  }
+  return words * 8;
+}
+
+extern "C" int hc_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                             const uint64_t* in, size_t bytes, void* data) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || (type != 3 && type != 4)) return 0;
+  unsigned maxbits = maxbits_for(type, dims, rate);
+  uint64_t words = bytes / 8;
+  if (type == 3) {
+    if (dims == 1) dec<1, float>(in, words, g, maxbits, data);
+    if (dims == 2) dec<2, float>(in, words, g, maxbits, data);
+    if (dims == 3) dec<3, float>(in, words, g, maxbits, data);
+  } else {
+    if (dims == 1) dec<1, double>(in, words, g, maxbits, data);
+    if (dims == 2) dec<2, double>(in, words, g, maxbits, data);
+    if (dims == 3) dec<3, double>(in, words, g, maxbits, data);
+  }
+  return 1;
+}

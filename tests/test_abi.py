@@ -1,0 +1,109 @@
+"""The C ABI library without a GPU: it loads, exports every function that
+include/*.h declares, and its size / rate helpers and argument checks agree
+with the reference.  No call here reaches a CUDA kernel."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions() -> list[str]:
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        if 'extern "C"' not in src:
+            continue
+        body = src.split('extern "C"', 1)[1]
+        names += re.findall(r"\b(gzfp_\w+)\s*\(", body)
+    return sorted(set(names))
+
+
+def test_library_exports_declared_symbols(gz):
+    lib = ctypes.CDLL(gz.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_version_and_status_strings(gz):
+    assert gz.version() >= 10000
+    lib = gz._lib
+    for st in range(5):
+        assert lib.gzfp_status_string(st)
+
+
+def test_rate_to_maxbits_matches_reference(gz, ref):
+    for t in (3, 4):
+        for dims in (1, 2, 3):
+            for rate in (0, 0.1, 0.5, 1, 2, 2.25, 3.3, 4, 7.99, 8, 12, 16, 17.7, 24, 32, 64):
+                assert gz._lib.gzfp_rate_to_maxbits(t, dims, rate) == \
+                    ref.ref().zref_set_rate_bits(t, dims, rate), (t, dims, rate)
+
+
+def test_maximum_size_matches_reference(gz, ref):
+    for t in (3, 4):
+        for shape in ((1,), (17,), (5, 9), (64, 64), (3, 4, 5), (33, 17, 9)):
+            nx, ny, nz = ref.dims3(shape)
+            for rate in (1, 4, 8, 16, 32, 64, 100):
+                mb = ref.ref().zref_set_rate_bits(t, len(shape), rate)
+                assert gz._lib.gzfp_maximum_size(t, nx, ny, nz, mb) == \
+                    ref.ref().zref_maximum_size(t, nx, ny, nz, rate), (t, shape, rate)
+
+
+def test_stream_size_matches_oracle(gz, orc):
+    for t, dt in ((3, np.float32), (4, np.float64)):
+        for shape in ((1,), (1023,), (5, 9), (3, 4, 5), (512, 512, 512)):
+            nx, ny, nz = orc.dims3(shape)
+            for rate in (1, 4, 12, 16, 24, 32):
+                mb = gz._lib.gzfp_rate_to_maxbits(t, len(shape), rate)
+                assert gz.stream_size(t, nx, ny, nz, mb) == orc.stream_bytes(shape, dt, rate)
+
+
+def _compress_status(gz, t, nx, ny, nz, rate, data=1, stream=1, cap=1 << 30):
+    out = ctypes.c_size_t(0)
+    return gz._lib.gzfp_compress(t, nx, ny, nz, rate, data, stream, cap, ctypes.byref(out), None)
+
+
+def test_argument_errors_without_device(gz):
+    """Checks that fail before any CUDA call."""
+    assert _compress_status(gz, 9, 4, 4, 4, 8.0) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 1, 4, 4, 4, 8.0) == gz.GZFP_ERR_UNSUPPORTED
+    assert _compress_status(gz, 2, 4, 4, 4, 8.0) == gz.GZFP_ERR_UNSUPPORTED
+    assert _compress_status(gz, 3, 0, 4, 4, 8.0) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 3, 4, 0, 4, 8.0) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 3, 4, 4, 4, -1.0) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 3, 4, 4, 4, float("nan")) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 3, 4, 4, 4, 8.0, data=0) == gz.GZFP_ERR_ARG
+    assert _compress_status(gz, 4, 8, 8, 8, 16.0, cap=1016) == gz.GZFP_ERR_CAPACITY
+    assert gz._lib.gzfp_last_error()
+    st = gz._lib.gzfp_decompress(3, 16, 16, 0, 8.0, 1, 8, 1, None)
+    assert st == gz.GZFP_ERR_ARG  # stream shorter than the compressed size
+    st = gz._lib.gzfp_compress_bits(3, 4, 4, 4, 8, 1, 1, 1 << 20, None, None)
+    assert st == gz.GZFP_ERR_ARG  # fewer bits than the block header
+
+
+def test_python_mirror_errors(gz):
+    zfp = gz.zfp_stream()
+    with pytest.raises(gz.GzfpError):
+        gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 4)
+    gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 3)
+    assert zfp.maxbits == zfp.minbits == 512
+    f = gz.zfp_field_3d(None, gz.zfp_type.float, 4, 4, 4)
+    f.sx = 2
+    with pytest.raises(gz.GzfpError) as e:
+        gz.compress(zfp, f)
+    assert e.value.status == gz.GZFP_ERR_UNSUPPORTED
+    assert gz.zfp_field_dimensionality(gz.zfp_field_2d(None, gz.zfp_type.double, 3, 5)) == 2
+    assert abs(gz.stream_set_rate(zfp, 2.0, gz.zfp_type.float, 1) - 2.25) < 1e-12

@@ -1,0 +1,174 @@
+"""CUDA codec parity: the kernels, called through the C ABI, against the
+oracle on the same seeded inputs -- bit-exact streams and bit-exact
+decompressed arrays -- and against the reference's golden fixtures."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests import cases, golden_io, zfp_pins
+
+pytestmark = pytest.mark.gpu
+
+
+def to_dev(a: np.ndarray, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def gpu_compress(gz, a: np.ndarray, rate: float, cuda) -> np.ndarray:
+    w = gz.compress_tensor(to_dev(a, cuda), rate)
+    return w.cpu().numpy().view(np.uint64)
+
+
+def gpu_decompress(gz, words: np.ndarray, shape, dtype, rate: float, cuda) -> np.ndarray:
+    import torch
+    tw = torch.from_numpy(np.ascontiguousarray(words).view(np.int64)).to(cuda)
+    tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+    return gz.decompress_tensor(tw, shape, tdt, rate).cpu().numpy()
+
+
+def same_bits(x: np.ndarray, y: np.ndarray) -> bool:
+    return x.shape == y.shape and np.array_equal(x.view(np.uint8), y.view(np.uint8))
+
+
+def test_random_cases(gz, orc, cuda):
+    rng = np.random.default_rng(4242)
+    for _ in range(300):
+        a, rate = cases.random_case(rng)
+        s = orc.compress(a, rate)
+        assert np.array_equal(gpu_compress(gz, a, rate, cuda), s), (a.shape, a.dtype, rate)
+        assert same_bits(gpu_decompress(gz, s, a.shape, a.dtype, rate, cuda),
+                         orc.decompress(s, a.shape, a.dtype, rate)), (a.shape, a.dtype, rate)
+
+
+def test_edge_cases(gz, orc, cuda):
+    for a, rate in cases.edge_cases():
+        s = orc.compress(a, rate)
+        assert np.array_equal(gpu_compress(gz, a, rate, cuda), s), (a.shape, a.dtype, rate)
+        assert same_bits(gpu_decompress(gz, s, a.shape, a.dtype, rate, cuda),
+                         orc.decompress(s, a.shape, a.dtype, rate))
+
+
+def test_arbitrary_streams(gz, orc, cuda):
+    """Decoding random words exercises budget cut-offs in every plane."""
+    rng = np.random.default_rng(17)
+    for shape in ((64,), (13, 9), (8, 7, 6), (21, 22, 23)):
+        for dt in (np.float32, np.float64):
+            for rate in (1, 2.5, 8, 16, 33):
+                n = orc.stream_bytes(shape, dt, rate) // 8
+                w = rng.integers(0, 2 ** 63, n, dtype=np.int64).astype(np.uint64) << np.uint64(1)
+                w |= rng.integers(0, 2, n, dtype=np.int64).astype(np.uint64)
+                assert same_bits(gpu_decompress(gz, w, shape, dt, rate, cuda),
+                                 orc.decompress(w, shape, dt, rate)), (shape, dt, rate)
+
+
+def test_golden_small(gz, cuda):
+    for c in golden_io.load_all():
+        a = c["input"]
+        assert np.array_equal(gpu_compress(gz, a, c["rate"], cuda), c["stream"]), c["name"]
+        assert same_bits(gpu_decompress(gz, c["stream"], a.shape, a.dtype, c["rate"], cuda),
+                         c["output"]), c["name"]
+
+
+def test_golden_manifest(gz, cuda):
+    for sp in golden_io.manifest():
+        a = golden_io.generate(sp)
+        assert golden_io.sha(a) == sp["input_sha256"], sp["name"]
+        s = gpu_compress(gz, a, sp["rate"], cuda)
+        assert golden_io.sha(s) == sp["stream_sha256"], sp["name"]
+        d = gpu_decompress(gz, s, a.shape, a.dtype, sp["rate"], cuda)
+        assert golden_io.sha(d) == sp["output_sha256"], sp["name"]
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_testzfp_pins(gz, cuda, dt, d):
+    """Fixed-rate size and max-error pins of zfp-0.5.0/tests/testzfp.cpp."""
+    f = zfp_pins.field(dt, d)
+    for rate, tol in zfp_pins.rate_pins(dt, d):
+        s = gpu_compress(gz, f, rate, cuda)
+        zfp = gz.zfp_stream()
+        actual = gz.stream_set_rate(zfp, rate, gz.zfp_type.float if dt == np.float32
+                                    else gz.zfp_type.double, d)
+        assert s.nbytes == zfp_pins.expected_bytes(actual, f.size)
+        g = gpu_decompress(gz, s, f.shape, f.dtype, rate, cuda)
+        assert float(np.max(np.abs(f - g))) <= tol
+
+
+def test_host_and_pinned_pointers(gz, orc, cuda):
+    """cuZFP's host-pointer path: arrays and streams in host memory."""
+    import torch
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((19, 23, 29)).astype(np.float64)
+    rate = 12.0
+    s_ref = orc.compress(a, rate)
+    for pinned in (False, True):
+        src = torch.from_numpy(a)
+        if pinned:
+            src = src.pin_memory()
+        zfp = gz.zfp_stream()
+        gz.stream_set_rate(zfp, rate, gz.zfp_type.double, 3)
+        buf = torch.zeros(gz.zfp_stream_maximum_size(zfp, gz.zfp_field_3d(None, gz.zfp_type.double,
+                                                                          29, 23, 19)) // 8,
+                          dtype=torch.int64)
+        if pinned:
+            buf = buf.pin_memory()
+        zfp.stream = buf
+        n = gz.compress(zfp, gz.zfp_field_3d(src, gz.zfp_type.double, 29, 23, 19))
+        assert n == s_ref.nbytes
+        assert np.array_equal(buf.numpy().view(np.uint64)[: n // 8], s_ref)
+        out = torch.zeros(a.shape, dtype=torch.float64)
+        if pinned:
+            out = out.pin_memory()
+        gz.decompress(zfp, gz.zfp_field_3d(out, gz.zfp_type.double, 29, 23, 19))
+        assert same_bits(out.numpy(), orc.decompress(s_ref, a.shape, a.dtype, rate))
+
+
+def test_mixed_pointers(gz, orc, cuda):
+    """Device array with a host stream, and the reverse."""
+    import torch
+    a = np.linspace(-3, 7, 40 * 41, dtype=np.float32).reshape(40, 41)
+    rate = 9.0
+    s_ref = orc.compress(a, rate)
+    zfp = gz.zfp_stream()
+    gz.stream_set_rate(zfp, rate, gz.zfp_type.float, 2)
+    host_buf = np.zeros(s_ref.size, np.uint64)
+    zfp.stream = host_buf
+    gz.compress(zfp, gz.zfp_field_2d(to_dev(a, cuda), gz.zfp_type.float, 41, 40))
+    assert np.array_equal(host_buf, s_ref)
+    dev_out = torch.zeros((40, 41), dtype=torch.float32, device=cuda)
+    gz.decompress(zfp, gz.zfp_field_2d(dev_out, gz.zfp_type.float, 41, 40))
+    assert same_bits(dev_out.cpu().numpy(), orc.decompress(s_ref, a.shape, a.dtype, rate))
+
+
+def test_user_stream_async(gz, orc, cuda):
+    """Device buffers on a caller's stream: the call is asynchronous and the
+    result is complete once that stream is synchronised."""
+    import torch
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal((64, 64, 64)).astype(np.float32)
+    s_ref = orc.compress(a, 16.0)
+    st = torch.cuda.Stream()
+    x = to_dev(a, cuda)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        w = gz.compress_tensor(x, 16.0, cuda_stream=st)
+        y = gz.decompress_tensor(w, a.shape, torch.float32, 16.0, cuda_stream=st)
+    st.synchronize()
+    assert np.array_equal(w.cpu().numpy().view(np.uint64), s_ref)
+    assert same_bits(y.cpu().numpy(), orc.decompress(s_ref, a.shape, a.dtype, 16.0))
+
+
+def test_errors(gz, cuda):
+    import torch
+    x = torch.zeros((4, 4, 4), dtype=torch.float64, device=cuda)
+    small = torch.zeros(4, dtype=torch.int64, device=cuda)
+    with pytest.raises(gz.GzfpError) as e:
+        gz.compress_tensor(x, 16.0, out=small)
+    assert e.value.status == gz.GZFP_ERR_CAPACITY
+    with pytest.raises(gz.GzfpError):
+        gz.compress_tensor(torch.zeros(4, dtype=torch.int32, device=cuda), 8.0)
+    # the context stays usable after rejected calls
+    w = gz.compress_tensor(x, 16.0)
+    assert int(w.abs().sum()) == 0

@@ -1,0 +1,67 @@
+"""The kernels' per-thread code (gzfp_block.cuh / gzfp_array.cuh), built
+for the host, against the oracle and the golden fixtures.  CPU only; the
+same source runs on the GPU in the `gpu` tests."""
+from __future__ import annotations
+
+import numpy as np
+
+from tests import cases, golden_io
+
+
+def hc_compress(lib, orc, a, rate):
+    nx, ny, nz = orc.dims3(a.shape)
+    n = orc.stream_bytes(a.shape, a.dtype, rate)
+    out = np.zeros(max(n // 8, 1), np.uint64)
+    got = lib.hc_compress(orc.type_code(a.dtype), nx, ny, nz, float(rate), a.ctypes.data,
+                          out.ctypes.data, out.nbytes)
+    assert got == n
+    return out[: n // 8]
+
+
+def hc_decompress(lib, orc, s, shape, dtype, rate):
+    out = np.zeros(shape, dtype)
+    nx, ny, nz = orc.dims3(shape)
+    assert lib.hc_decompress(orc.type_code(dtype), nx, ny, nz, float(rate), s.ctypes.data,
+                             s.nbytes, out.ctypes.data)
+    return out
+
+
+def test_random_cases(hostcodec, orc):
+    rng = np.random.default_rng(99)
+    for _ in range(500):
+        a, rate = cases.random_case(rng)
+        s = orc.compress(a, rate)
+        assert np.array_equal(hc_compress(hostcodec, orc, a, rate), s), (a.shape, a.dtype, rate)
+        d = orc.decompress(s, a.shape, a.dtype, rate)
+        h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
+        assert np.array_equal(d.view(np.uint8), h.view(np.uint8)), (a.shape, a.dtype, rate)
+
+
+def test_edge_cases(hostcodec, orc):
+    for a, rate in cases.edge_cases():
+        s = orc.compress(a, rate)
+        assert np.array_equal(hc_compress(hostcodec, orc, a, rate), s), (a.shape, a.dtype, rate)
+        h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
+        d = orc.decompress(s, a.shape, a.dtype, rate)
+        assert np.array_equal(d.view(np.uint8), h.view(np.uint8))
+
+
+def test_arbitrary_streams(hostcodec, orc):
+    rng = np.random.default_rng(11)
+    for shape in ((64,), (13, 9), (8, 7, 6)):
+        for dt in (np.float32, np.float64):
+            for rate in (1, 2.5, 8, 16, 33):
+                n = orc.stream_bytes(shape, dt, rate) // 8
+                w = rng.integers(0, 2 ** 63, n, dtype=np.int64).astype(np.uint64) << np.uint64(1)
+                w |= rng.integers(0, 2, n, dtype=np.int64).astype(np.uint64)
+                d = orc.decompress(w, shape, dt, rate)
+                h = hc_decompress(hostcodec, orc, w, shape, dt, rate)
+                assert np.array_equal(d.view(np.uint8), h.view(np.uint8)), (shape, dt, rate)
+
+
+def test_golden(hostcodec, orc):
+    for c in golden_io.load_all():
+        a = c["input"]
+        assert np.array_equal(hc_compress(hostcodec, orc, a, c["rate"]), c["stream"]), c["name"]
+        h = hc_decompress(hostcodec, orc, c["stream"], a.shape, a.dtype, c["rate"])
+        assert np.array_equal(h.view(np.uint8), c["output"].view(np.uint8)), c["name"]

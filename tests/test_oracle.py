@@ -1,0 +1,120 @@
+"""The oracle (CPU restatement of zfp 0.5.0 fixed-rate mode) pinned against
+the reference: its own zfp build, its regression checksums and fixed-rate
+pins, and the committed golden streams.  CPU only."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests import cases, golden_io, zfp_pins
+
+
+def test_oracle_matches_reference_random(ref):
+    rng = np.random.default_rng(1234)
+    checked = 0
+    for _ in range(400):
+        a, rate = cases.random_case(rng)
+        if cases.has_saturating_blocks(a):
+            continue
+        s_ref = ref.ref_compress(a, rate)
+        s_orc = ref.compress(a, rate)
+        assert np.array_equal(s_ref, s_orc), (a.shape, a.dtype, rate)
+        d_ref = ref.ref_decompress(s_ref, a.shape, a.dtype, rate)
+        d_orc = ref.decompress(s_ref, a.shape, a.dtype, rate)
+        assert np.array_equal(d_ref.view(np.uint8), d_orc.view(np.uint8)), (a.shape, rate)
+        checked += 1
+    assert checked > 300
+
+
+def test_oracle_matches_reference_edges(ref):
+    for a, rate in cases.edge_cases():
+        if cases.has_saturating_blocks(a):
+            continue
+        s_ref = ref.ref_compress(a, rate)
+        assert np.array_equal(s_ref, ref.compress(a, rate)), (a.shape, a.dtype, rate)
+        d_ref = ref.ref_decompress(s_ref, a.shape, a.dtype, rate)
+        assert np.array_equal(d_ref.view(np.uint8),
+                              ref.decompress(s_ref, a.shape, a.dtype, rate).view(np.uint8))
+
+
+def test_oracle_decodes_arbitrary_streams_like_reference(ref):
+    """Random words are legal fixed-rate streams; both decoders must agree
+    on them too (exercises budget cut-offs and the 'assumed one' rule)."""
+    rng = np.random.default_rng(7)
+    for dims, shape in ((1, (64,)), (2, (12, 12)), (3, (8, 8, 8))):
+        for dt in (np.float32, np.float64):
+            for rate in (1, 4, 9.5, 16, 40):
+                n = ref.stream_bytes(shape, dt, rate) // 8
+                w = rng.integers(0, 2 ** 63, n, dtype=np.int64).astype(np.uint64)
+                w ^= rng.integers(0, 2, n, dtype=np.int64).astype(np.uint64) << np.uint64(63)
+                d_ref = ref.ref_decompress(w, shape, dt, rate)
+                d_orc = ref.decompress(w, shape, dt, rate)
+                assert np.array_equal(d_ref.view(np.uint8), d_orc.view(np.uint8)), (shape, dt, rate)
+
+
+def test_multithreaded_oracle_is_byte_identical(orc):
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        a, rate = cases.random_case(rng, max_edge=(5000, 120, 30))
+        s1 = orc.compress(a, rate, 1)
+        for t in (2, 3, 7):
+            assert np.array_equal(s1, orc.compress(a, rate, t))
+            assert np.array_equal(orc.decompress(s1, a.shape, a.dtype, rate, 1).view(np.uint8),
+                                  orc.decompress(s1, a.shape, a.dtype, rate, t).view(np.uint8))
+
+
+def test_testzfp_fields_match_reference_fixture(ref):
+    """The regenerated regression fields equal the reference's fixture."""
+    fx = ref.ref_fields()
+    if fx is None:
+        pytest.skip("reference fields not built")
+    for t, dt in enumerate((np.float32, np.float64)):
+        for d in (1, 2, 3):
+            assert np.array_equal(zfp_pins.field(dt, d).ravel(), fx[t][d - 1])
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_testzfp_checksums(dt, d):
+    """Input checksums of Z/tests/testzfp.cpp:475-486 (Jenkins hash)."""
+    f = zfp_pins.field(dt, d)
+    assert zfp_pins.jenkins(f.tobytes()) == zfp_pins.CHECKSUM[np.dtype(dt).name][d - 1]
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_testzfp_fixed_rate_pins(orc, dt, d):
+    """Fixed-rate pins of Z/tests/testzfp.cpp:92-178 with the error table of
+    :498-509: compressed size and max error."""
+    f = zfp_pins.field(dt, d)
+    for rate, tol in zfp_pins.rate_pins(dt, d):
+        s = orc.compress(f, rate)
+        # the test compares with the rate zfp_stream_set_rate reports back
+        actual = orc.port().gzo_maxbits(orc.type_code(dt), d, rate) / 4 ** d
+        assert s.nbytes == zfp_pins.expected_bytes(actual, f.size)
+        g = orc.decompress(s, f.shape, f.dtype, rate)
+        assert float(np.max(np.abs(f - g))) <= tol
+
+
+def test_golden_streams(orc):
+    """Committed streams and outputs made by the reference's own build."""
+    n = 0
+    for case in golden_io.load_all():
+        s = orc.compress(case["input"], case["rate"])
+        assert np.array_equal(s, case["stream"]), case["name"]
+        d = orc.decompress(case["stream"], case["input"].shape, case["input"].dtype, case["rate"])
+        assert np.array_equal(d.view(np.uint8), case["output"].view(np.uint8)), case["name"]
+        n += 1
+    assert n >= 10
+
+
+def test_golden_manifest(orc):
+    """Generated inputs (digest-checked) against the reference's digests."""
+    from tests import golden_io
+    for sp in golden_io.manifest():
+        a = golden_io.generate(sp)
+        assert golden_io.sha(a) == sp["input_sha256"], sp["name"]
+        s = orc.compress(a, sp["rate"])
+        assert s.nbytes == sp["stream_bytes"] and golden_io.sha(s) == sp["stream_sha256"], sp["name"]
+        d = orc.decompress(s, a.shape, a.dtype, sp["rate"])
+        assert golden_io.sha(d) == sp["output_sha256"], sp["name"]
