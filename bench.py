@@ -48,7 +48,15 @@ def parse():
     p.add_argument("--impl", default="gzfp", choices=["gzfp", "reference"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    return p.parse_args()
+    p.add_argument("--edge", type=int, default=512,
+                   help="cube edge of the field (smaller cases for profiling)")
+    p.add_argument("--rate", type=float, default=16.0)
+    args = p.parse_args()
+    global SHAPE, RATE, WORKLOAD
+    SHAPE = (args.edge,) * 3
+    RATE = args.rate
+    WORKLOAD = f"3d_f64_{args.edge}cube_sinusoids16_rate{args.rate:g}"
+    return args
 
 
 def dist_env():

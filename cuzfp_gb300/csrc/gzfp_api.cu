@@ -45,7 +45,15 @@ bool make_geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) 
   g.by = (g.ny + 3) / 4;
   g.bz = (g.nz + 3) / 4;
   g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  g.vec = 0;
   return true;
+}
+
+// Rows of full blocks move as one vector when every row start is aligned:
+// 16 bytes for float, 32 for double.
+uint32_t rows_vectorizable(const void* p, unsigned nx, int type) {
+  const uintptr_t a = type == GZFP_TYPE_FLOAT ? 16 : 32;
+  return (nx % 4 == 0 && (uintptr_t)p % a == 0) ? 1u : 0u;
 }
 
 bool is_device_pointer(const void* p) {
@@ -190,6 +198,7 @@ int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned
     // blocks share boundary words, which the kernel ORs into a zeroed stream
     if ((e = cudaMemsetAsync(d_stream, 0, bytes, s))) return cuda_fail(e, "cudaMemsetAsync(stream)");
   }
+  g.vec = rows_vectorizable(d_data, nx, type);
   if (type == GZFP_TYPE_FLOAT)
     e = gzfp::launch_encode_f32(dims, (const float*)d_data, g, maxbits, d_stream, nwords, s);
   else
@@ -243,6 +252,7 @@ int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsign
     if ((e = reserve(ws.field, ws.field_cap, field_bytes))) return cuda_fail(e, "cudaMalloc(field workspace)");
     d_data = ws.field;
   }
+  g.vec = rows_vectorizable(d_data, nx, type);
   if (type == GZFP_TYPE_FLOAT)
     e = gzfp::launch_decode_f32(dims, d_stream, nwords, g, maxbits, (float*)d_data, s);
   else

@@ -15,6 +15,7 @@ struct Geom {
   uint32_t nx, ny, nz;
   uint32_t bx, by, bz;  // blocks per axis
   uint64_t nblocks;
+  uint32_t vec;  // rows of full blocks may be moved as one 16/32-byte vector
 };
 
 GZ_HD void block_coords(const Geom& g, uint64_t b, uint32_t& ix, uint32_t& iy, uint32_t& iz) {
@@ -52,6 +53,41 @@ GZ_HD typename FT<T>::UInt load_bits(const T* p) {
 #endif
 }
 
+// Four consecutive values of a row as one vector access (device only; the
+// caller guarantees 16-byte (float) / 32-byte (double) alignment).
+GZ_HD void load_row(const float* p, uint32_t* r) {
+#if defined(__CUDA_ARCH__)
+  asm("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "l"(p));
+#else
+  __builtin_memcpy(r, p, 16);
+#endif
+}
+GZ_HD void load_row(const double* p, uint64_t* r) {
+#if defined(__CUDA_ARCH__)
+  asm("ld.global.nc.v4.u64 {%0,%1,%2,%3}, [%4];"
+      : "=l"(r[0]), "=l"(r[1]), "=l"(r[2]), "=l"(r[3]) : "l"(p));
+#else
+  __builtin_memcpy(r, p, 32);
+#endif
+}
+GZ_HD void store_row(float* p, const uint32_t* r) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};"
+               :: "l"(p), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]) : "memory");
+#else
+  __builtin_memcpy(p, r, 16);
+#endif
+}
+GZ_HD void store_row(double* p, const uint64_t* r) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("st.global.v4.u64 [%0], {%1,%2,%3,%4};"
+               :: "l"(p), "l"(r[0]), "l"(r[1]), "l"(r[2]), "l"(r[3]) : "memory");
+#else
+  __builtin_memcpy(p, r, 32);
+#endif
+}
+
 // Gather block (ix, iy, iz) as raw IEEE bits, padded at partial edges.
 template <int D, typename T>
 GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
@@ -62,7 +98,13 @@ GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t
   const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
   const T* base = in + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
   constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
-  if (cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4)) {
+  const bool full = cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4);
+  if (full && g.vec) {
+#pragma unroll
+    for (int z = 0; z < DZ; z++)
+#pragma unroll
+      for (int y = 0; y < DY; y++) load_row(base + y * sy + z * sz, raw + 16 * z + 4 * y);
+  } else if (full) {
 #pragma unroll
     for (int z = 0; z < DZ; z++)
 #pragma unroll
@@ -92,6 +134,13 @@ GZ_HD void scatter(T* out, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
   const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
   UInt* base = (UInt*)out + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
   constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
+  if (g.vec && cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4)) {
+#pragma unroll
+    for (int z = 0; z < DZ; z++)
+#pragma unroll
+      for (int y = 0; y < DY; y++) store_row(out + 4ull * ix + (4ull * iy + y) * sy + (4ull * iz + z) * sz, raw + 16 * z + 4 * y);
+    return;
+  }
 #pragma unroll
   for (int z = 0; z < DZ; z++)
 #pragma unroll
@@ -134,11 +183,11 @@ struct BitWriter {
   }
   // append the low n (<= 64) bits of v; v has no bits at or above n
   GZ_HD void put(uint64_t v, uint32_t n) {
-    acc |= shl64(v, fill);
-    uint32_t f = fill + n;
+    acc |= v << fill;  // fill < 64
+    const uint32_t f = fill + n;
     if (f >= 64) {
       emit();
-      acc = shr64(v, 64 - fill);
+      acc = (v >> 1) >> (63 - fill);  // the bits of v that did not fit
       fill = f - 64;
     } else {
       fill = f;
@@ -171,7 +220,7 @@ struct BitReader {
     w0 = words.load(wi);
     w1 = words.load(wi + 1);
   }
-  GZ_HD uint64_t peek64() const { return off ? (w0 >> off) | (w1 << (64 - off)) : w0; }
+  GZ_HD uint64_t peek64() const { return (w0 >> off) | ((w1 << 1) << (63 - off)); }
   GZ_HD void skip(uint32_t n) {  // n <= 64
     off += n;
     if (off >= 64) {
@@ -191,8 +240,9 @@ struct BitReader {
 
 // ------------------------------------------------------- per-block drivers
 
-template <int D, typename T, class Words>
-GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words) {
+template <int D, typename T, bool SPILL, class Words, class PS>
+GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words,
+                      PS& ps, const Ctx& c) {
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   uint32_t ix, iy, iz;
@@ -200,19 +250,21 @@ GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, 
   UInt raw[BS];
   gather<D, T>(in, g, ix, iy, iz, raw);
   BitWriter<Words> w(words, b * (uint64_t)maxbits, maxbits);
-  encode_block<D, T>(raw, maxbits, w);
+  encode_block<D, T, SPILL>(raw, maxbits, w, ps, c,
+                            [&](UInt* r2) { gather<D, T>(in, g, ix, iy, iz, r2); });
   w.finish();
 }
 
-template <int D, typename T, class Words>
-GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words words) {
+template <int D, typename T, class Words, class PS>
+GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words words, PS& ps,
+                      const Ctx& c) {
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   uint32_t ix, iy, iz;
   block_coords(g, b, ix, iy, iz);
   BitReader<Words> r(words, b * (uint64_t)maxbits);
   UInt raw[BS];
-  decode_block<D, T>(r, maxbits, raw);
+  decode_block<D, T>(r, maxbits, raw, ps, c);
   scatter<D, T>(out, g, ix, iy, iz, raw);
 }
 

@@ -61,6 +61,7 @@ GZ_HD uint32_t clz64(uint64_t x) {
 #endif
 }
 
+GZ_HD uint32_t umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
 GZ_HD uint32_t lo32(uint64_t v) { return (uint32_t)v; }
 GZ_HD uint32_t hi32(uint64_t v) { return (uint32_t)(v >> 32); }
 
@@ -138,57 +139,44 @@ struct Perm<3> {
 
 
 // ----------------------------------------------------------------- lifting
+
+// Per-launch context (reserved; carries no state today).
+struct Ctx {
+  uint32_t one, m1;
+};
+
+// wrap-around integer arithmetic (zfp's signed overflow is undefined in C;
+// these steps never overflow on streams the encoder produced)
+GZ_HD int32_t add_(int32_t a, int32_t b, const Ctx&) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+GZ_HD int32_t sub_(int32_t a, int32_t b, const Ctx&) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+GZ_HD int32_t shl1_(int32_t a) { return (int32_t)((uint32_t)a << 1); }
+GZ_HD int64_t add_(int64_t a, int64_t b, const Ctx&) { return (int64_t)((uint64_t)a + (uint64_t)b); }
+GZ_HD int64_t sub_(int64_t a, int64_t b, const Ctx&) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+GZ_HD int64_t shl1_(int64_t a) { return (int64_t)((uint64_t)a << 1); }
+
 // zfp's lifting steps (Z/src/template/encode.c:77-103, decode.c:28-54) in
 // two's-complement wrap-around arithmetic with arithmetic right shifts.
-
 template <typename Int>
-struct Unsigned;
-template <>
-struct Unsigned<int32_t> {
-  typedef uint32_t T;
-};
-template <>
-struct Unsigned<int64_t> {
-  typedef uint64_t T;
-};
-
-template <typename Int>
-GZ_HD Int wadd(Int a, Int b) {
-  typedef typename Unsigned<Int>::T U;
-  return (Int)((U)a + (U)b);
-}
-template <typename Int>
-GZ_HD Int wsub(Int a, Int b) {
-  typedef typename Unsigned<Int>::T U;
-  return (Int)((U)a - (U)b);
-}
-template <typename Int>
-GZ_HD Int wshl1(Int a) {
-  typedef typename Unsigned<Int>::T U;
-  return (Int)((U)a << 1);
+GZ_HD void fwd_lift(Int& x, Int& y, Int& z, Int& w, const Ctx& c) {
+  x = add_(x, w, c); x >>= 1; w = sub_(w, x, c);
+  z = add_(z, y, c); z >>= 1; y = sub_(y, z, c);
+  x = add_(x, z, c); x >>= 1; z = sub_(z, x, c);
+  w = add_(w, y, c); w >>= 1; y = sub_(y, w, c);
+  w = add_(w, (Int)(y >> 1), c); y = sub_(y, (Int)(w >> 1), c);
 }
 
 template <typename Int>
-GZ_HD void fwd_lift(Int& x, Int& y, Int& z, Int& w) {
-  x = wadd(x, w); x >>= 1; w = wsub(w, x);
-  z = wadd(z, y); z >>= 1; y = wsub(y, z);
-  x = wadd(x, z); x >>= 1; z = wsub(z, x);
-  w = wadd(w, y); w >>= 1; y = wsub(y, w);
-  w = wadd(w, (Int)(y >> 1)); y = wsub(y, (Int)(w >> 1));
-}
-
-template <typename Int>
-GZ_HD void inv_lift(Int& x, Int& y, Int& z, Int& w) {
-  y = wadd(y, (Int)(w >> 1)); w = wsub(w, (Int)(y >> 1));
-  y = wadd(y, w); w = wshl1(w); w = wsub(w, y);
-  z = wadd(z, x); x = wshl1(x); x = wsub(x, z);
-  y = wadd(y, z); z = wshl1(z); z = wsub(z, y);
-  w = wadd(w, x); x = wshl1(x); x = wsub(x, w);
+GZ_HD void inv_lift(Int& x, Int& y, Int& z, Int& w, const Ctx& c) {
+  y = add_(y, (Int)(w >> 1), c); w = sub_(w, (Int)(y >> 1), c);
+  y = add_(y, w, c); w = shl1_(w); w = sub_(w, y, c);
+  z = add_(z, x, c); x = shl1_(x); x = sub_(x, z, c);
+  y = add_(y, z, c); z = shl1_(z); z = sub_(z, y, c);
+  w = add_(w, x, c); x = shl1_(x); x = sub_(x, w, c);
 }
 
 // decorrelating transform: lines along x (stride 1), y (stride 4), z (16)
 template <int D, typename Int>
-GZ_HD void fwd_xform(Int* q) {
+GZ_HD void fwd_xform(Int* q, const Ctx& c) {
   constexpr int L = 1 << (2 * (D - 1));  // lines per axis
 #pragma unroll
   for (int a = 0; a < D; a++) {
@@ -196,13 +184,13 @@ GZ_HD void fwd_xform(Int* q) {
 #pragma unroll
     for (int l = 0; l < L; l++) {
       const int base = (l % s) + (l / s) * s * 4;
-      fwd_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
+      fwd_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s], c);
     }
   }
 }
 
 template <int D, typename Int>
-GZ_HD void inv_xform(Int* q) {
+GZ_HD void inv_xform(Int* q, const Ctx& c) {
   constexpr int L = 1 << (2 * (D - 1));
 #pragma unroll
   for (int a = D - 1; a >= 0; a--) {
@@ -210,7 +198,7 @@ GZ_HD void inv_xform(Int* q) {
 #pragma unroll
     for (int l = 0; l < L; l++) {
       const int base = (l % s) + (l / s) * s * 4;
-      inv_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
+      inv_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s], c);
     }
   }
 }
@@ -359,6 +347,88 @@ GZ_HD void encode_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
   }
 }
 
+// encode_plane when at least 2*BS+1 bits of budget remain, so that no part
+// of the plane's code can be cut off: no clipping, and each run of zeros,
+// its one and the following group test go out as one field.
+template <int BS, class W>
+GZ_HD void encode_plane_fast(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
+  if (n == (uint32_t)BS) {  // every coefficient significant: the plane verbatim
+    w.put(x, BS);
+    bits -= BS;
+    return;
+  }
+  uint32_t used = n + 1;
+  if (n) w.put(x & ((1ull << n) - 1), n);
+  uint64_t y = x >> n;
+  if (y == 0) {  // group test: nothing left in this plane
+    w.put(0, 1);
+    bits -= used;
+    return;
+  }
+  w.put(1, 1);
+  uint32_t pos = n;
+  for (;;) {
+    const uint32_t t = ctz64(y);
+    const uint32_t p = pos + t;
+    if (p == (uint32_t)BS - 1) {  // a one in the last position is implied
+      w.put(0, t);
+      used += t;
+      n = BS;
+      break;
+    }
+    y = (y >> t) >> 1;
+    const uint64_t more = y != 0;
+    w.put((1 | (more << 1)) << t, t + 2);  // t zeros, the one, the next group test
+    used += t + 2;
+    pos = p + 1;
+    if (!more) {
+      n = pos;
+      break;
+    }
+  }
+  bits -= used;
+}
+
+// decode_plane when at least 2*BS+1 bits of budget remain.
+template <int BS, class R>
+GZ_HD uint64_t decode_plane_fast(uint32_t& n, uint32_t& bits, R& r) {
+  if (n == (uint32_t)BS) {
+    bits -= BS;
+    return r.read(BS);
+  }
+  uint64_t x = r.read(n);
+  uint32_t used = n + 1;
+  uint64_t w = r.peek64();
+  r.skip(1);
+  if (w & 1) {
+    uint32_t pos = n;
+    for (;;) {
+      w = r.peek64();
+      const uint32_t t = ctz64(w);
+      if (pos + t >= (uint32_t)BS - 1) {  // zeros up to the implied last one
+        const uint32_t c = BS - 1 - pos;
+        r.skip(c);
+        used += c;
+        x |= 1ull << (BS - 1);
+        n = BS;
+        break;
+      }
+      const uint32_t p = pos + t;
+      x |= 1ull << p;
+      const uint32_t more = (uint32_t)(w >> (t + 1)) & 1u;
+      r.skip(t + 2);
+      used += t + 2;
+      pos = p + 1;
+      if (!more) {
+        n = pos;
+        break;
+      }
+    }
+  }
+  bits -= used;
+  return x;
+}
+
 // Inverse of encode_plane, matching decode_ints (Z/src/template/
 // decode.c:73-105) bit for bit, including its rule that a run cut off by
 // the budget still deposits a one at the current position.
@@ -390,6 +460,19 @@ GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
     n++;
   }
   return x;
+}
+
+// one plane, on the unclipped path while the budget cannot run out in it
+template <int BS, class W>
+GZ_HD void code_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
+  if (bits >= 2 * BS + 1)
+    encode_plane_fast<BS>(x, n, bits, w);
+  else
+    encode_plane<BS>(x, n, bits, w);
+}
+template <int BS, class R>
+GZ_HD uint64_t uncode_plane(uint32_t& n, uint32_t& bits, R& r) {
+  return bits >= 2 * BS + 1 ? decode_plane_fast<BS>(n, bits, r) : decode_plane<BS>(n, bits, r);
 }
 
 // --------------------------------------------------------- float <-> bits
@@ -492,17 +575,41 @@ GZ_HD void quantize(const uint32_t* raw, int32_t* q, int n, int emax) {
 // f64: shift the significand into place (exact), except in the regime where
 // 2^(62-emax) overflows to +inf, where zfp's product is +-inf or NaN and the
 // conversion saturates (see the oracle's header on defined behaviour).
+// With maxE the largest biased exponent, a value of biased exponent E and
+// significand M (53 bits with the hidden one) maps to
+// |q| = (M << 9) >> (maxE - E): M << 9 < 2^62 never loses bits.
 GZ_HD void quantize(const uint64_t* raw, int64_t* q, int n, int emax) {
   if (emax >= 62 - 1023) {
-    const int maxE = emax + 1022;  // biased exponent field of the largest value
+    const uint32_t maxE = (uint32_t)(emax + 1022);  // >= 61
+    uint32_t minE = 0x7ff;
 #pragma unroll
     for (int i = 0; i < n; i++) {
-      uint64_t a = raw[i] & 0x7fffffffffffffffull;
-      uint32_t E = (uint32_t)(a >> 52);
-      uint64_t M = (a & 0xfffffffffffffull) | (E ? (1ull << 52) : 0);
-      int d = maxE - (int)(E ? E : 1);  // >= 0
-      uint64_t mag = d <= 9 ? M << (9 - d) : shr64(M, (uint32_t)(d - 9));
-      q[i] = (raw[i] >> 63) ? (int64_t)(0 - mag) : (int64_t)mag;
+      uint32_t E = (uint32_t)(raw[i] >> 52) & 0x7ffu;
+      minE = E < minE ? E : minE;
+    }
+    if (minE != 0) {  // no zeros or denormals: every value has the hidden one
+#pragma unroll
+      for (int i = 0; i < n; i++) {
+        const uint32_t hi = (uint32_t)(raw[i] >> 32), lo = (uint32_t)raw[i];
+        const uint32_t E = (hi >> 20) & 0x7ffu;
+        const uint32_t d = umin(maxE - E, 63u);
+        const uint64_t M9 = ((uint64_t)((hi & 0xfffffu) | 0x100000u) << 41) | ((uint64_t)lo << 9);
+        const uint64_t mag = M9 >> d;
+        const uint64_t s = (uint64_t)((int64_t)(int32_t)hi >> 31);  // 0 or all ones
+        q[i] = (int64_t)((mag ^ s) - s);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < n; i++) {
+        const uint32_t hi = (uint32_t)(raw[i] >> 32), lo = (uint32_t)raw[i];
+        const uint32_t E = (hi >> 20) & 0x7ffu;
+        const uint32_t d = umin(maxE - (E ? E : 1u), 63u);
+        const uint64_t M9 = ((uint64_t)((hi & 0xfffffu) | (E ? 0x100000u : 0u)) << 41) |
+                            ((uint64_t)lo << 9);
+        const uint64_t mag = M9 >> d;
+        const uint64_t s = (uint64_t)((int64_t)(int32_t)hi >> 31);
+        q[i] = (int64_t)((mag ^ s) - s);
+      }
     }
   } else {
 #pragma unroll
@@ -545,17 +652,76 @@ GZ_HD void dequantize(const int64_t* q, uint64_t* raw, int n, int emax) {
   }
 }
 
-// ------------------------------------------------------------- block codec
+// 4^3 blocks: transpose the 32-bit slice G of the 64 coefficients and put
+// planes 32G .. 32G+31 into store slots 0..31 (slot = plane - 32G).
+template <int G, typename UInt, class PS>
+GZ_HD void planes_to_store(const UInt* u, PS& ps) {
+  uint32_t t[64];
+#pragma unroll
+  for (int i = 0; i < 64; i++) t[i] = (uint32_t)((uint64_t)u[i] >> (32 * G));
+  transpose_tiles<32>(t);
+  transpose_tiles<32>(t + 32);
+#pragma unroll
+  for (int kk = 0; kk < 32; kk++) ps.put(kk, (uint64_t)t[kk] | ((uint64_t)t[32 + kk] << 32));
+}
 
-// Encode one block of raw IEEE bit patterns (gathered and padded) into
-// exactly maxbits bits (Z/src/template/encode.c:154-234).
-template <int D, typename T, class W>
-GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w) {
+// Inverse of planes_to_store: slots base + kk for kk in (lo, hi] hold planes
+// 32G + kk, the others are zero; OR the slice into the coefficients.
+template <int G, typename UInt, class PS>
+GZ_HD void store_to_coeffs(const PS& ps, int base, int lo, int hi, UInt* u) {
+  uint32_t t[64];
+#pragma unroll
+  for (int kk = 0; kk < 32; kk++) {
+    const uint64_t x = (kk > lo && kk <= hi) ? ps.get(base + kk) : 0;
+    t[kk] = (uint32_t)x;
+    t[32 + kk] = (uint32_t)(x >> 32);
+  }
+  transpose_tiles<32>(t);
+  transpose_tiles<32>(t + 32);
+#pragma unroll
+  for (int i = 0; i < 64; i++) u[i] |= (UInt)((uint64_t)t[i] << (32 * G));
+}
+
+// ------------------------------------------------------------- block codec
+// The transposed planes are consumed by a rolled loop, so they live in a
+// per-thread plane store `PS` (shared memory on the GPU, an array on the
+// host): slot i holds a 64-bit value, get(i) / put(i, v).  For 4^3 blocks a
+// slot is one plane of the current 32-plane half; for smaller blocks the
+// slots are the words of Planes::tw.
+
+// Front end of the encoder: block-floating-point conversion, decorrelating
+// transform, sequency reordering and negabinary mapping.
+template <int D, typename T>
+GZ_HD void front_end(const typename FT<T>::UInt* raw, int emax, typename FT<T>::UInt* u,
+                     const Ctx& c) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
   constexpr int BS = 1 << (2 * D);
+  Int q[BS];
+  quantize(raw, q, BS, emax);
+  fwd_xform<D>(q, c);
+#pragma unroll
+  for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
+}
+
+// Encode one block of raw IEEE bit patterns (gathered and padded) into
+// exactly maxbits bits (Z/src/template/encode.c:154-234).
+//
+// 4^3 double blocks are coded one 32-bit slice (32 planes) at a time.  The
+// bottom slice is needed only when the top 32 planes do not use up the
+// budget: with SPILL it is parked in plane-store slots 32..63, otherwise it
+// is recomputed from the input (`regather(raw)` gathers the block again),
+// which keeps the store at 32 slots for the lower rates where the bottom
+// slice is seldom reached.
+template <int D, typename T, bool SPILL, class W, class PS, class Regather>
+GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps,
+                        const Ctx& c, Regather&& regather) {
+  typedef FT<T> F;
+  typedef typename F::UInt UInt;
+  constexpr int BS = 1 << (2 * D);
   constexpr int P = F::P;
+  typedef Planes<D, P> PL;
 
   // largest exponent field and a nonzero test, from the IEEE bits
   uint32_t maxh = 0, orl = 0;
@@ -576,40 +742,77 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w)
   const uint32_t e = (uint32_t)(emax + F::EBIAS);
   w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
 
-  Int q[BS];
-  quantize(raw, q, BS, emax);
-  fwd_xform<D>(q);
-
   UInt u[BS];
-#pragma unroll
-  for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
+  front_end<D, T>(raw, emax, u, c);
 
   const uint32_t budget = maxbits - (F::EBITS + 1);
   uint32_t bits = budget;
   const int kmin = P - prec;
-  Planes<D, P> pl;
-  pl.load(u, P / 32 - 1);
-  pl.transpose(P / 32 - 1);
-  if (P == 64) pl.load(u, 0);
   uint32_t n = 0;
+  int k = P - 1;
+  if constexpr (BS == 64 && P == 64) {
+    if constexpr (SPILL) {
 #pragma unroll
-  for (int k = P - 1; k >= 0; k--) {
-    if (k < kmin || bits == 0) break;
-    if (P == 64 && k == 31) pl.transpose(0);
-    encode_plane<BS>(pl.plane(k), n, bits, w);
+      for (int i = 0; i < 32; i++)
+        ps.put(32 + i, (uint64_t)(uint32_t)u[2 * i] | ((uint64_t)u[2 * i + 1] << 32));
+    }
+    planes_to_store<1>(u, ps);
+#pragma unroll 1
+    for (; k >= 32 && k >= kmin && bits; k--) code_plane<BS>(ps.get(k - 32), n, bits, w);
+    if (k >= kmin && bits) {
+      uint32_t lo[64];
+      if constexpr (SPILL) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const uint64_t v = ps.get(32 + i);
+          lo[2 * i] = (uint32_t)v;
+          lo[2 * i + 1] = (uint32_t)(v >> 32);
+        }
+      } else {
+        UInt raw2[BS], u2[BS];
+        regather(raw2);
+        front_end<D, T>(raw2, emax, u2, c);
+#pragma unroll
+        for (int i = 0; i < BS; i++) lo[i] = (uint32_t)u2[i];
+      }
+      planes_to_store<0>(lo, ps);
+#pragma unroll 1
+      for (; k >= kmin && bits; k--) code_plane<BS>(ps.get(k), n, bits, w);
+    }
+  } else if constexpr (BS == 64) {
+    planes_to_store<0>(u, ps);
+#pragma unroll 1
+    for (; k >= kmin && bits; k--) code_plane<BS>(ps.get(k), n, bits, w);
+  } else {
+    PL pl;
+#pragma unroll
+    for (int G = 0; G < P / 32; G++) {
+      pl.load(u, G);
+      pl.transpose(G);
+    }
+#pragma unroll
+    for (int i = 0; i < PL::NW; i++) ps.put(i, pl.tw[i]);
+#pragma unroll 1
+    for (; k >= kmin && bits; k--) {
+      const int G = k >> 5, kk = k & 31, r = kk % PL::N, g = kk / PL::N;
+      const uint32_t word = (uint32_t)ps.get(G * BS + r);
+      code_plane<BS>((word >> (g * PL::N)) & ((1u << PL::N) - 1), n, bits, w);
+    }
   }
   w.zeros(bits);
 }
 
 // Decode one block from a reader positioned at its first bit into raw IEEE
 // bit patterns (Z/src/template/decode.c:137-165).
-template <int D, typename T, class R>
-GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw) {
+template <int D, typename T, class R, class PS>
+GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& ps,
+                        const Ctx& c) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
   constexpr int BS = 1 << (2 * D);
   constexpr int P = F::P;
+  typedef Planes<D, P> PL;
 
   uint64_t head = r.peek64();
   if (!(head & 1)) {
@@ -624,27 +827,62 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw) {
   const int kmin = P - prec;
   uint32_t bits = maxbits - (F::EBITS + 1);
 
-  Planes<D, P> pl;
-#pragma unroll
-  for (int i = 0; i < Planes<D, P>::NW; i++) pl.tw[i] = 0;
   uint32_t n = 0;
-  bool low = false;  // any plane below 32 decoded
-#pragma unroll
-  for (int k = P - 1; k >= 0; k--) {
-    if (k < kmin || bits == 0) break;
-    pl.set_plane(k, decode_plane<BS>(n, bits, r));
-    if (k < 32) low = true;
-  }
-  pl.transpose(P / 32 - 1);
-  if (P == 64 && low) pl.transpose(0);
+  int k = P - 1;
   UInt u[BS];
-  pl.store(u);
+  if constexpr (BS == 64) {
+    // planes of the top half into the store, then into the coefficients'
+    // top 32-bit slices; the bottom half only if decoding reaches it
+#pragma unroll
+    for (int i = 0; i < BS; i++) u[i] = 0;
+    if constexpr (P == 64) {
+      // top-half planes into the store, folded into the coefficients before
+      // the bottom half reuses the store
+      const int top = k;
+#pragma unroll 1
+      for (; k >= 32 && k >= kmin && bits; k--) ps.put(k - 32, uncode_plane<BS>(n, bits, r));
+      store_to_coeffs<1>(ps, 0, k - 32, top - 32, u);
+      if (k >= kmin && bits) {
+        const int top0 = k;
+#pragma unroll 1
+        for (; k >= kmin && bits; k--) ps.put(k, uncode_plane<BS>(n, bits, r));
+        store_to_coeffs<0>(ps, 0, k, top0, u);
+      }
+    } else {
+      const int top = k;
+#pragma unroll 1
+      for (; k >= kmin && bits; k--) ps.put(k, uncode_plane<BS>(n, bits, r));
+      store_to_coeffs<0>(ps, 0, k, top, u);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < PL::NW; i++) ps.put(i, 0);
+#pragma unroll 1
+    for (; k >= kmin && bits; k--) {
+      const int G = k >> 5, kk = k & 31, rr = kk % PL::N, g = kk / PL::N;
+      const uint64_t x = uncode_plane<BS>(n, bits, r);
+      ps.put(G * BS + rr, ps.get(G * BS + rr) | (x << (g * PL::N)));
+    }
+    PL pl;
+#pragma unroll
+    for (int i = 0; i < PL::NW; i++) pl.tw[i] = (uint32_t)ps.get(i);
+#pragma unroll
+    for (int G = 0; G < P / 32; G++) pl.transpose(G);
+    pl.store(u);
+  }
 
   Int q[BS];
 #pragma unroll
   for (int i = 0; i < BS; i++) q[Perm<D>::at(i)] = (Int)((u[i] ^ (UInt)F::NB) - (UInt)F::NB);
-  inv_xform<D>(q);
+  inv_xform<D>(q, c);
   dequantize(q, raw, BS, emax);
 }
+
+// Plane store backed by a plain array (host builds and tests).
+struct LocalPlanes {
+  uint64_t v[64];
+  GZ_HD uint64_t get(int i) const { return v[i]; }
+  GZ_HD void put(int i, uint64_t x) { v[i] = x; }
+};
 
 }  // namespace gzfp

@@ -6,15 +6,12 @@ namespace gzfp {
 
 cudaError_t launch_decode_f64(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
                               uint32_t maxbits, double* out, cudaStream_t s) {
-  if (g.nblocks == 0) return cudaSuccess;
-  const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   switch (dims) {
-    case 1: decode_kernel<1, double><<<grid, kThreads, 0, s>>>(in, nwords, g, maxbits, out); break;
-    case 2: decode_kernel<2, double><<<grid, kThreads, 0, s>>>(in, nwords, g, maxbits, out); break;
-    case 3: decode_kernel<3, double><<<grid, kThreads, 0, s>>>(in, nwords, g, maxbits, out); break;
+    case 1: return launch_decode_t<1, double>(in, nwords, g, maxbits, out, s);
+    case 2: return launch_decode_t<2, double>(in, nwords, g, maxbits, out, s);
+    case 3: return launch_decode_t<3, double>(in, nwords, g, maxbits, out, s);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace gzfp

@@ -6,15 +6,12 @@ namespace gzfp {
 
 cudaError_t launch_encode_f32(int dims, const float* in, const Geom& g, uint32_t maxbits,
                               uint64_t* out, uint64_t nwords, cudaStream_t s) {
-  if (g.nblocks == 0) return cudaSuccess;
-  const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   switch (dims) {
-    case 1: encode_kernel<1, float><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
-    case 2: encode_kernel<2, float><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
-    case 3: encode_kernel<3, float><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
+    case 1: return launch_encode_t<1, float>(in, g, maxbits, out, nwords, s);
+    case 2: return launch_encode_t<2, float>(in, g, maxbits, out, nwords, s);
+    case 3: return launch_encode_t<3, float>(in, g, maxbits, out, nwords, s);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace gzfp

@@ -6,15 +6,12 @@ namespace gzfp {
 
 cudaError_t launch_encode_f64(int dims, const double* in, const Geom& g, uint32_t maxbits,
                               uint64_t* out, uint64_t nwords, cudaStream_t s) {
-  if (g.nblocks == 0) return cudaSuccess;
-  const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   switch (dims) {
-    case 1: encode_kernel<1, double><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
-    case 2: encode_kernel<2, double><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
-    case 3: encode_kernel<3, double><<<grid, kThreads, 0, s>>>(in, g, maxbits, out, nwords); break;
+    case 1: return launch_encode_t<1, double>(in, g, maxbits, out, nwords, s);
+    case 2: return launch_encode_t<2, double>(in, g, maxbits, out, nwords, s);
+    case 3: return launch_encode_t<3, double>(in, g, maxbits, out, nwords, s);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace gzfp

@@ -1,9 +1,14 @@
 // gzfp_kernels.cuh -- the plain-path CUDA kernels: one thread per zfp block.
 //
-// Encode: gather 4^D values (coalesced across the warp: consecutive threads
-// own consecutive blocks along x), run the block codec in registers and
+// Encode: gather 4^D values (consecutive threads own consecutive blocks, so
+// a warp's row loads are contiguous), run the block codec in registers,
 // write the block's bits into its fixed-rate slot [b*maxbits, (b+1)*maxbits).
 // Decode: the inverse, reading the slot and storing the valid values.
+//
+// Shared memory per CTA: each thread's plane store (the coder walks planes in
+// a rolled loop), and for decoding, when every block fills whole 64-bit
+// words ("staged" mode, maxbits % 64 == 0), a word buffer into which the
+// warp loads its 32 consecutive stream slots with coalesced loads.
 //
 // Replaces cuZFP's cudaEncode / cudaEncode1 / cudaEncode2 and cudaDecode /
 // cudaDecode1 / cudaDecode2 (src/cuZFP/encode{1,2,3}.cuh, decode{1,2,3}.cuh).
@@ -15,11 +20,30 @@
 
 namespace gzfp {
 
-constexpr int kThreads = 128;  // threads (= blocks) per CTA
+constexpr int kThreads = 128;            // threads (= blocks) per CTA
+constexpr int kStride = kThreads + 1;    // staged word buffer row pitch (words)
+constexpr uint32_t kMaxStagedWords = 64; // staged decode up to 4096-bit blocks
+// 4^3 double blocks of more than this many bits park their bottom 32-bit
+// slice in shared memory instead of recomputing it when it is reached
+constexpr uint32_t kSpillBits = 1100;
 
-// Stream word access for the writer / reader.  `merge` ORs a word that two
-// neighbouring zfp blocks share (only when maxbits is not a multiple of 64;
-// the stream is zeroed first in that case).
+// dynamic shared memory of a CTA: the plane store (32 or 64 slots of 8
+// bytes per thread) and, for staged decode, the word buffer
+inline size_t smem_bytes(int slots, bool staged, uint32_t words_per_block) {
+  size_t b = (size_t)slots * kThreads * 8;
+  if (staged) b += (size_t)words_per_block * kStride * 8;
+  return b;
+}
+
+// per-thread plane store in shared memory, slot i at planes[i * kThreads]
+struct SmemPlanes {
+  uint64_t* p;
+  __device__ __forceinline__ uint64_t get(int i) const { return p[i * kThreads]; }
+  __device__ __forceinline__ void put(int i, uint64_t v) { p[i * kThreads] = v; }
+};
+
+// Global stream words.  `merge` ORs a word that neighbouring zfp blocks share
+// (only when maxbits is not a multiple of 64; the stream is zeroed first).
 struct DevWords {
   uint64_t* out;
   const uint64_t* in;
@@ -31,23 +55,114 @@ struct DevWords {
   __device__ __forceinline__ uint64_t load(uint64_t i) const { return i < n ? __ldg(in + i) : 0; }
 };
 
+// One block's slot in the staged word buffer: word j of the block at
+// buf[j * kStride]; words past the slot read as zero.
+struct StagedWords {
+  uint64_t* buf;
+  uint64_t w0;  // global index of the slot's first word
+  uint32_t W;   // words per block
+  __device__ __forceinline__ void store(uint64_t i, uint64_t v) { buf[(i - w0) * kStride] = v; }
+  __device__ __forceinline__ void merge(uint64_t i, uint64_t v) { buf[(i - w0) * kStride] |= v; }
+  __device__ __forceinline__ uint64_t load(uint64_t i) const {
+    uint64_t j = i - w0;
+    return j < W ? buf[j * kStride] : 0;
+  }
+};
+
+// Copy a warp's 32 consecutive slots between the staged buffer (word j of
+// lane t at buf[j * kStride + t]) and the stream, 32 words per step.
+template <bool TO_GLOBAL>
+__device__ __forceinline__ void warp_copy(uint64_t* buf, uint64_t* gwords, uint32_t W,
+                                          uint32_t nblocks_valid) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t total = nblocks_valid * W;
+  uint32_t t = lane / W, j = lane % W;      // slot and word of element `lane`
+  const uint32_t dt = 32 / W, dj = 32 % W;  // advance per step of 32 elements
+  for (uint32_t gi = lane; gi < total; gi += 32) {
+    if (TO_GLOBAL)
+      gwords[gi] = buf[j * kStride + t];
+    else
+      buf[j * kStride + t] = __ldg(gwords + gi);
+    t += dt;
+    j += dj;
+    if (j >= W) {
+      j -= W;
+      t++;
+    }
+  }
+}
+
+// Register budget: the 4^3 double kernels keep a whole block (64 x 64 bits)
+// in registers; 168 registers per thread allow 3 CTAs of 128 threads per SM.
 template <int D, typename T>
-__global__ void __launch_bounds__(kThreads) encode_kernel(const T* __restrict__ in, Geom g,
-                                                          uint32_t maxbits,
-                                                          uint64_t* __restrict__ out,
-                                                          uint64_t nwords) {
+struct MinBlocks {
+  static constexpr int value = (D == 3 && sizeof(T) == 8) ? 3 : 4;
+};
+
+template <int D, typename T, bool SPILL>
+__global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
+    encode_kernel(const T* __restrict__ in, Geom g, uint32_t maxbits, uint64_t* __restrict__ out,
+                  uint64_t nwords, Ctx c) {
+  extern __shared__ uint64_t smem[];
+  SmemPlanes ps{smem + threadIdx.x};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
-  if (b >= g.nblocks) return;
-  encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords});
+  if (b < g.nblocks)
+    encode_one<D, T, SPILL>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps, c);
+}
+
+template <int D, typename T, bool STAGED>
+__global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
+    decode_kernel(const uint64_t* __restrict__ in, uint64_t nwords, Geom g, uint32_t maxbits,
+                  T* __restrict__ out, Ctx c) {
+  extern __shared__ uint64_t smem[];
+  SmemPlanes ps{smem + threadIdx.x};
+  const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+  if (STAGED) {
+    const uint32_t W = maxbits >> 6;
+    uint64_t* buf = smem + 32 * kThreads;
+    const uint64_t b0 = b - (threadIdx.x & 31);
+    if (b0 < g.nblocks) {
+      const uint64_t left = g.nblocks - b0;
+      warp_copy<false>(buf + (threadIdx.x & ~31u), (uint64_t*)in + b0 * W, W,
+                       left < 32 ? (uint32_t)left : 32);
+    }
+    __syncwarp();
+    if (b < g.nblocks)
+      decode_one<D, T>(out, g, b, maxbits, StagedWords{buf + threadIdx.x, b * W, W}, ps, c);
+  } else {
+    if (b < g.nblocks) decode_one<D, T>(out, g, b, maxbits, DevWords{nullptr, in, nwords}, ps, c);
+  }
+}
+
+// kernel launchers shared by the per-type translation units
+template <int D, typename T>
+cudaError_t launch_encode_t(const T* in, const Geom& g, uint32_t maxbits, uint64_t* out,
+                            uint64_t nwords, cudaStream_t s) {
+  if (g.nblocks == 0) return cudaSuccess;
+  const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
+  const Ctx c{1u, 0xffffffffu};
+  const bool spill = D == 3 && sizeof(T) == 8 && maxbits > kSpillBits;
+  const size_t sm = smem_bytes(spill ? 64 : 32, false, 0);
+  auto k = spill ? encode_kernel<D, T, true> : encode_kernel<D, T, false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kThreads, sm, s>>>(in, g, maxbits, out, nwords, c);
+  return cudaGetLastError();
 }
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kThreads) decode_kernel(const uint64_t* __restrict__ in,
-                                                          uint64_t nwords, Geom g,
-                                                          uint32_t maxbits, T* __restrict__ out) {
-  const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
-  if (b >= g.nblocks) return;
-  decode_one<D, T>(out, g, b, maxbits, DevWords{nullptr, in, nwords});
+cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, uint32_t maxbits,
+                            T* out, cudaStream_t s) {
+  if (g.nblocks == 0) return cudaSuccess;
+  const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
+  const Ctx c{1u, 0xffffffffu};
+  const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords;
+  const size_t sm = smem_bytes(32, staged, maxbits >> 6);
+  auto k = staged ? decode_kernel<D, T, true> : decode_kernel<D, T, false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<grid, kThreads, sm, s>>>(in, nwords, g, maxbits, out, c);
+  return cudaGetLastError();
 }
 
 }  // namespace gzfp

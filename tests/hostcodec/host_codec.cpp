@@ -28,6 +28,7 @@ bool geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
   g.nx = nx; g.ny = ny ? ny : 1; g.nz = nz ? nz : 1;
   g.bx = (g.nx + 3) / 4; g.by = (g.ny + 3) / 4; g.bz = (g.nz + 3) / 4;
   g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  g.vec = (nx % 4 == 0);  // memcpy rows on the host: only the index math matters
   return true;
 }
 
@@ -40,13 +41,24 @@ unsigned maxbits_for(int type, int dims, double rate) {
 template <int D, typename T>
 void enc(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out, uint64_t words) {
   HostWords w{out, nullptr, words};
-  for (uint64_t b = 0; b < g.nblocks; b++) gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w);
+  gzfp::LocalPlanes ps;
+  const gzfp::Ctx c{1u, 0xffffffffu};
+  // both lower-slice strategies of the 4^3 double coder must agree
+  for (uint64_t b = 0; b < g.nblocks; b++) {
+    if (b & 1)
+      gzfp::encode_one<D, T, true>((const T*)data, g, b, maxbits, w, ps, c);
+    else
+      gzfp::encode_one<D, T, false>((const T*)data, g, b, maxbits, w, ps, c);
+  }
 }
 
 template <int D, typename T>
 void dec(const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbits, void* data) {
   HostWords w{nullptr, in, words};
-  for (uint64_t b = 0; b < g.nblocks; b++) gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w);
+  gzfp::LocalPlanes ps;
+  const gzfp::Ctx c{1u, 0xffffffffu};
+  for (uint64_t b = 0; b < g.nblocks; b++)
+    gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w, ps, c);
 }
 
 }  // namespace
