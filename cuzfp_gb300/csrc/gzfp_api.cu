@@ -38,15 +38,8 @@ int ebits_of(int type) { return type == GZFP_TYPE_FLOAT ? 8 : 11; }
 bool make_geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
   if (nx == 0 || (nz != 0 && ny == 0)) return false;
   dims = nz ? 3 : ny ? 2 : 1;
-  g.nx = nx;
-  g.ny = ny ? ny : 1;
-  g.nz = nz ? nz : 1;
-  g.bx = (g.nx + 3) / 4;
-  g.by = (g.ny + 3) / 4;
-  g.bz = (g.nz + 3) / 4;
-  g.nblocks = (uint64_t)g.bx * g.by * g.bz;
-  g.vec = 0;
-  return true;
+  g = gzfp::make_geom_blocks(nx, ny ? ny : 1, nz ? nz : 1);
+  return g.nblocks < (1ull << 32);  // block indices are 32-bit on the device
 }
 
 // Rows of full blocks move as one vector when every row start is aligned:
@@ -95,7 +88,7 @@ int check_common(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbi
   if (type != GZFP_TYPE_FLOAT && type != GZFP_TYPE_DOUBLE)
     return fail(GZFP_ERR_ARG, "unknown scalar type");
   if (!make_geom(nx, ny, nz, g, dims))
-    return fail(GZFP_ERR_ARG, "bad dimensions (nx must be > 0; nz > 0 needs ny > 0)");
+    return fail(GZFP_ERR_ARG, "bad dimensions (nx must be > 0; nz > 0 needs ny > 0; under 2^32 blocks)");
   if (maxbits < (unsigned)ebits_of(type) + 1 || maxbits > kMaxBitsLimit)
     return fail(GZFP_ERR_ARG, "bits per block out of range");
   return GZFP_OK;

@@ -11,19 +11,59 @@ namespace gzfp {
 // Geometry of a contiguous a[nz][ny][nx] field cut into 4^D blocks; unused
 // axes have size 1.  Blocks are numbered x fastest, then y, then z, the order
 // of zfp's block loops (Z/src/template/compress.c:60-104).
+// Division of a 32-bit value by a fixed divisor d >= 1 as a multiply-high
+// and a shift (round-up method): n / d = (umulhi(n, m) + n) >> s.
+struct FastDiv {
+  uint32_t d, m, s;
+};
+
+GZ_HD FastDiv make_fastdiv(uint32_t d) {
+  uint32_t s = 0;
+  while ((1ull << s) < d) s++;
+  const uint32_t m = (uint32_t)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return FastDiv{d, m, s};
+}
+
+GZ_HD uint32_t fast_div(uint32_t n, const FastDiv& f) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t hi = __umulhi(n, f.m);
+#else
+  const uint32_t hi = (uint32_t)(((uint64_t)n * f.m) >> 32);
+#endif
+  return (uint32_t)(((uint64_t)hi + n) >> f.s);
+}
+
+// Geometry of a contiguous a[nz][ny][nx] field cut into 4^D blocks (fewer
+// than 2^32 of them); unused axes have size 1.
 struct Geom {
   uint32_t nx, ny, nz;
   uint32_t bx, by, bz;  // blocks per axis
   uint64_t nblocks;
   uint32_t vec;  // rows of full blocks may be moved as one 16/32-byte vector
+  FastDiv dbx, dby;
 };
 
+GZ_HD Geom make_geom_blocks(uint32_t nx, uint32_t ny, uint32_t nz) {
+  Geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.bx = (nx + 3) / 4;
+  g.by = (ny + 3) / 4;
+  g.bz = (nz + 3) / 4;
+  g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  g.vec = 0;
+  g.dbx = make_fastdiv(g.bx);
+  g.dby = make_fastdiv(g.by);
+  return g;
+}
+
 GZ_HD void block_coords(const Geom& g, uint64_t b, uint32_t& ix, uint32_t& iy, uint32_t& iz) {
-  uint64_t r = b / g.bx;
-  ix = (uint32_t)(b - r * g.bx);
-  uint64_t s = r / g.by;
-  iy = (uint32_t)(r - s * g.by);
-  iz = (uint32_t)s;
+  const uint32_t b32 = (uint32_t)b;
+  const uint32_t r = fast_div(b32, g.dbx);
+  ix = b32 - r * g.bx;
+  iz = fast_div(r, g.dby);
+  iy = r - iz * g.by;
 }
 
 // zfp's pad_block (Z/src/template/encode.c:55-74) as an index map: with c
@@ -240,7 +280,7 @@ struct BitReader {
 
 // ------------------------------------------------------- per-block drivers
 
-template <int D, typename T, bool SPILL, class Words, class PS>
+template <int D, typename T, class Words, class PS>
 GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words,
                       PS& ps, const Ctx& c) {
   typedef typename FT<T>::UInt UInt;
@@ -250,8 +290,7 @@ GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, 
   UInt raw[BS];
   gather<D, T>(in, g, ix, iy, iz, raw);
   BitWriter<Words> w(words, b * (uint64_t)maxbits, maxbits);
-  encode_block<D, T, SPILL>(raw, maxbits, w, ps, c,
-                            [&](UInt* r2) { gather<D, T>(in, g, ix, iy, iz, r2); });
+  encode_block<D, T>(raw, maxbits, w, ps, c);
   w.finish();
 }
 

@@ -52,6 +52,13 @@ GZ_HD uint32_t ctz32(uint32_t x) {
   return x ? (uint32_t)__builtin_ctz(x) : 32u;
 #endif
 }
+GZ_HD int popcount64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __popcll(x);
+#else
+  return __builtin_popcountll(x);
+#endif
+}
 // number of leading zeros; 64 for zero
 GZ_HD uint32_t clz64(uint64_t x) {
 #if defined(__CUDA_ARCH__)
@@ -307,13 +314,25 @@ struct Planes {
 };
 
 // ------------------------------------------------------ plane (de)coder
-// One bit plane of the embedded coder of encode_ints (Z/src/template/
-// encode.c:122-151): the first n bits verbatim, then group tests -- a 1 if
-// any bit is left, followed by the run of zeros up to and including the next
-// one bit (a one in the last position is implied) -- and a final 0 test.
-// Output stops when the block's bit budget is spent, exactly where the
-// bit-serial coder stops.
+// The embedded coder of encode_ints / decode_ints (Z/src/template/
+// encode.c:122-151, decode.c:73-105).  Per bit plane x (bit i = bit k of
+// coefficient i) with n coefficients already significant: the first n bits
+// verbatim, then group tests -- a 1 if any bit is left, followed by the run
+// of zeros up to and including the next one (a one in the last position is
+// implied) -- and a final 0 test.  Output stops where the block's bit
+// budget is spent, exactly where the bit-serial coder stops.
+//
+// A plane's group tests have a closed form.  With the m ones above the
+// frontier at relative positions q_0 < ... < q_{m-1}, the one of rank j
+// lands at bit q_j + 1 + j after the first test bit and is followed by a
+// test bit that is 1 except after the last one.  So with the rank spread
+// S = sum_j 2^(q_j + j), the group part is 1 | 2S | 4(S - 2^(q_{m-1}+m-1))
+// and has q_{m-1} + m + 2 bits.  Planes whose code fits one 64-bit word
+// (the common case for smooth data) are coded in one step this way; the
+// rest -- a one in the last position, long codes, the budget running out --
+// take the bit-exact general routines below.
 
+// General one-plane coder (clips at the budget).
 template <int BS, class W>
 GZ_HD void encode_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
   uint32_t m = n < bits ? n : bits;
@@ -347,91 +366,9 @@ GZ_HD void encode_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
   }
 }
 
-// encode_plane when at least 2*BS+1 bits of budget remain, so that no part
-// of the plane's code can be cut off: no clipping, and each run of zeros,
-// its one and the following group test go out as one field.
-template <int BS, class W>
-GZ_HD void encode_plane_fast(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
-  if (n == (uint32_t)BS) {  // every coefficient significant: the plane verbatim
-    w.put(x, BS);
-    bits -= BS;
-    return;
-  }
-  uint32_t used = n + 1;
-  if (n) w.put(x & ((1ull << n) - 1), n);
-  uint64_t y = x >> n;
-  if (y == 0) {  // group test: nothing left in this plane
-    w.put(0, 1);
-    bits -= used;
-    return;
-  }
-  w.put(1, 1);
-  uint32_t pos = n;
-  for (;;) {
-    const uint32_t t = ctz64(y);
-    const uint32_t p = pos + t;
-    if (p == (uint32_t)BS - 1) {  // a one in the last position is implied
-      w.put(0, t);
-      used += t;
-      n = BS;
-      break;
-    }
-    y = (y >> t) >> 1;
-    const uint64_t more = y != 0;
-    w.put((1 | (more << 1)) << t, t + 2);  // t zeros, the one, the next group test
-    used += t + 2;
-    pos = p + 1;
-    if (!more) {
-      n = pos;
-      break;
-    }
-  }
-  bits -= used;
-}
-
-// decode_plane when at least 2*BS+1 bits of budget remain.
-template <int BS, class R>
-GZ_HD uint64_t decode_plane_fast(uint32_t& n, uint32_t& bits, R& r) {
-  if (n == (uint32_t)BS) {
-    bits -= BS;
-    return r.read(BS);
-  }
-  uint64_t x = r.read(n);
-  uint32_t used = n + 1;
-  uint64_t w = r.peek64();
-  r.skip(1);
-  if (w & 1) {
-    uint32_t pos = n;
-    for (;;) {
-      w = r.peek64();
-      const uint32_t t = ctz64(w);
-      if (pos + t >= (uint32_t)BS - 1) {  // zeros up to the implied last one
-        const uint32_t c = BS - 1 - pos;
-        r.skip(c);
-        used += c;
-        x |= 1ull << (BS - 1);
-        n = BS;
-        break;
-      }
-      const uint32_t p = pos + t;
-      x |= 1ull << p;
-      const uint32_t more = (uint32_t)(w >> (t + 1)) & 1u;
-      r.skip(t + 2);
-      used += t + 2;
-      pos = p + 1;
-      if (!more) {
-        n = pos;
-        break;
-      }
-    }
-  }
-  bits -= used;
-  return x;
-}
-
-// Inverse of encode_plane, matching decode_ints (Z/src/template/
-// decode.c:73-105) bit for bit, including its rule that a run cut off by
-// the budget still deposits a one at the current position.
+// General one-plane decoder, matching decode_ints bit for bit including
+// its rule that a run cut off by the budget still deposits a one at the
+// current position (Z/src/template/decode.c:94-98).
 template <int BS, class R>
 GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
   uint32_t m = n < bits ? n : bits;
@@ -462,17 +399,98 @@ GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
   return x;
 }
 
-// one plane, on the unclipped path while the budget cannot run out in it
-template <int BS, class W>
-GZ_HD void code_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
-  if (bits >= 2 * BS + 1)
-    encode_plane_fast<BS>(x, n, bits, w);
-  else
-    encode_plane<BS>(x, n, bits, w);
+// Rank spread of the ones of z: the one of rank j moves from bit q to bit
+// q + j.  Closed form for up to three ones, a loop beyond.
+GZ_HD uint64_t rank_spread(uint64_t z) {
+  const uint64_t l0 = z & (0 - z);
+  const uint64_t z1 = z ^ l0;
+  const uint64_t l1 = z1 & (0 - z1);
+  uint64_t z2 = z1 ^ l1;
+  const uint64_t l2 = z2 & (0 - z2);
+  uint64_t S = l0 | (l1 << 1) | (l2 << 2);
+  z2 ^= l2;
+  for (uint32_t j = 3; z2; j++) {
+    const uint64_t low = z2 & (0 - z2);
+    S |= low << j;
+    z2 ^= low;
+  }
+  return S;
 }
-template <int BS, class R>
-GZ_HD uint64_t uncode_plane(uint32_t& n, uint32_t& bits, R& r) {
-  return bits >= 2 * BS + 1 ? decode_plane_fast<BS>(n, bits, r) : decode_plane<BS>(n, bits, r);
+
+// Code planes k, k-1, ... down to k_low while budget remains; plane(k)
+// yields plane k.  Returns the index of the next plane.  The loop body has
+// no data-dependent branch except the rare general path (a one implied by
+// the last position, or a code longer than 64 bits), so the 32 threads of
+// a warp (32 blocks) stay converged plane after plane.  A budget that ends
+// inside a plane's code just truncates it, as the bit-serial coder does.
+template <int BS, class W, class PlaneFn>
+GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, PlaneFn&& plane) {
+  for (; k >= k_low && bits; k--) {
+    const uint64_t x = plane(k);
+    const bool full = n == (uint32_t)BS;            // all significant: plane verbatim
+    const uint32_t sh = full ? 0 : n;
+    const uint64_t xh = full ? 0 : x >> sh;         // ones above the frontier
+    const bool any = xh != 0;
+    const uint32_t hb = 63 - clz64(xh | 1);         // top one, relative to the frontier
+    const uint32_t m = (uint32_t)popcount64(xh);
+    const uint32_t top = n + hb;
+    const uint32_t glen = top + m + 2;              // code length when any
+    if (any && (top >= (uint32_t)BS - 1 || glen > 64)) {
+      encode_plane<BS>(x, n, bits, w);
+      continue;
+    }
+    const uint64_t S = rank_spread(xh);
+    const uint64_t grp = any ? (1 | (S << 1) | ((S - (1ull << ((hb + m - 1) & 63))) << 2)) : 0;
+    uint64_t code = full ? x : (x & ((1ull << sh) - 1)) | (grp << sh);
+    uint32_t len = full ? (uint32_t)BS : any ? glen : n + 1;
+    n = any ? top + 1 : n;
+    const bool cut = len > bits;  // the budget ends inside this plane's code
+    code = cut ? code & ((1ull << (bits & 63)) - 1) : code;
+    len = cut ? bits : len;
+    w.put(code, len);
+    bits -= len;
+  }
+  return k;
+}
+
+// Decode planes k, ... down to k_low while budget remains, handing each to
+// store(k, x).  Returns the index of the next plane.  A plane is decoded
+// from one 64-bit window when its code lies inside the window and the
+// budget and no one is implied by the last position; otherwise (the last
+// plane of a block, and rarely others) the general routine re-reads it.
+template <int BS, class R, class StoreFn>
+GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
+  for (; k >= k_low && bits; k--) {
+    const uint64_t w = r.peek64();
+    const bool full = n == (uint32_t)BS;
+    const uint32_t sh = full ? 0 : n;
+    const uint64_t head = full ? w & lowmask64(BS) : w & ((1ull << sh) - 1);
+    const bool test = !full && ((w >> sh) & 1);
+    uint64_t g = (w >> sh) >> 1, x = head;
+    uint32_t used = full ? (uint32_t)BS : n + 1, pos = n;
+    bool ok = used <= bits;
+    bool more = test;
+    while (more && ok) {  // runs once per one of the plane
+      const uint32_t t = ctz64(g);
+      ok = pos + t < (uint32_t)BS - 1 && used + t + 2 <= 64 && used + t + 2 <= bits;
+      if (ok) {
+        x |= 1ull << (pos + t);
+        more = (g >> (t + 1)) & 1;
+        g = (g >> (t + 1)) >> 1;
+        used += t + 2;
+        pos += t + 1;
+      }
+    }
+    if (ok) {
+      r.skip(used);
+      bits -= used;
+      n = test ? pos : n;
+      store(k, x);
+    } else {
+      store(k, decode_plane<BS>(n, bits, r));  // nothing consumed yet: start over
+    }
+  }
+  return k;
 }
 
 // --------------------------------------------------------- float <-> bits
@@ -628,23 +646,22 @@ GZ_HD void dequantize(const int32_t* q, uint32_t* raw, int n, int emax) {
   for (int i = 0; i < n; i++) raw[i] = f32_bits(i32_scaled(q[i], s));
 }
 
-// f64: round-to-nearest-even int64 -> double done in integer arithmetic and
-// the power-of-two scale folded into the exponent, wherever the result is a
-// normal number for every q (-960 <= emax <= 1022); otherwise the FP64 unit.
+// f64: wherever the result is a normal number for every nonzero q
+// (-960 <= emax <= 1022), the round-to-nearest int64 -> double conversion
+// runs on the conversion unit (it shares the FP64 pipe, which is otherwise
+// idle here) and the power-of-two scale is an integer add to the exponent
+// field; outside that range the full IEEE multiply is used.
 GZ_HD void dequantize(const int64_t* q, uint64_t* raw, int n, int emax) {
   if (emax >= -960 && emax <= 1022) {
+    const uint64_t scale = (uint64_t)(int64_t)(emax - 62) << 52;
 #pragma unroll
     for (int i = 0; i < n; i++) {
-      uint64_t sign = (uint64_t)q[i] & 0x8000000000000000ull;
-      uint64_t a = sign ? 0 - (uint64_t)q[i] : (uint64_t)q[i];
-      uint32_t lz = clz64(a);
-      uint64_t norm = a << (lz & 63);
-      uint64_t mant = norm >> 11;
-      uint32_t rb = (uint32_t)norm & 0x7ffu;
-      uint64_t up = (rb > 0x400u || (rb == 0x400u && (mant & 1))) ? 1 : 0;
-      uint64_t biased = (uint64_t)(int64_t)(emax - (int)lz + 1024);
-      uint64_t b = ((biased - 1) << 52) + mant + up;
-      raw[i] = a ? (b | sign) : 0;
+#if defined(__CUDA_ARCH__)
+      const uint64_t d = f64_bits(__ll2double_rn(q[i]));
+#else
+      const uint64_t d = f64_bits((double)q[i]);
+#endif
+      raw[i] = q[i] ? d + scale : 0;
     }
   } else {
     const double s = pow2d(emax - 62);
@@ -708,15 +725,12 @@ GZ_HD void front_end(const typename FT<T>::UInt* raw, int emax, typename FT<T>::
 // Encode one block of raw IEEE bit patterns (gathered and padded) into
 // exactly maxbits bits (Z/src/template/encode.c:154-234).
 //
-// 4^3 double blocks are coded one 32-bit slice (32 planes) at a time.  The
-// bottom slice is needed only when the top 32 planes do not use up the
-// budget: with SPILL it is parked in plane-store slots 32..63, otherwise it
-// is recomputed from the input (`regather(raw)` gathers the block again),
-// which keeps the store at 32 slots for the lower rates where the bottom
-// slice is seldom reached.
-template <int D, typename T, bool SPILL, class W, class PS, class Regather>
+// 4^3 double blocks are coded one 32-bit slice (32 planes) at a time; the
+// bottom slice waits in plane-store slots 32..63 while the top one is coded,
+// so only half of the block's coefficients stay in registers.
+template <int D, typename T, class W, class PS>
 GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps,
-                        const Ctx& c, Regather&& regather) {
+                        const Ctx& c) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   constexpr int BS = 1 << (2 * D);
@@ -751,38 +765,26 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
   uint32_t n = 0;
   int k = P - 1;
   if constexpr (BS == 64 && P == 64) {
-    if constexpr (SPILL) {
 #pragma unroll
-      for (int i = 0; i < 32; i++)
-        ps.put(32 + i, (uint64_t)(uint32_t)u[2 * i] | ((uint64_t)u[2 * i + 1] << 32));
-    }
+    for (int i = 0; i < 32; i++)
+      ps.put(32 + i, (uint64_t)(uint32_t)u[2 * i] | ((uint64_t)u[2 * i + 1] << 32));
     planes_to_store<1>(u, ps);
-#pragma unroll 1
-    for (; k >= 32 && k >= kmin && bits; k--) code_plane<BS>(ps.get(k - 32), n, bits, w);
+    k = code_planes<BS>(k, kmin > 32 ? kmin : 32, n, bits, w,
+                        [&](int kk) { return ps.get(kk - 32); });
     if (k >= kmin && bits) {
       uint32_t lo[64];
-      if constexpr (SPILL) {
 #pragma unroll
-        for (int i = 0; i < 32; i++) {
-          const uint64_t v = ps.get(32 + i);
-          lo[2 * i] = (uint32_t)v;
-          lo[2 * i + 1] = (uint32_t)(v >> 32);
-        }
-      } else {
-        UInt raw2[BS], u2[BS];
-        regather(raw2);
-        front_end<D, T>(raw2, emax, u2, c);
-#pragma unroll
-        for (int i = 0; i < BS; i++) lo[i] = (uint32_t)u2[i];
+      for (int i = 0; i < 32; i++) {
+        const uint64_t v = ps.get(32 + i);
+        lo[2 * i] = (uint32_t)v;
+        lo[2 * i + 1] = (uint32_t)(v >> 32);
       }
       planes_to_store<0>(lo, ps);
-#pragma unroll 1
-      for (; k >= kmin && bits; k--) code_plane<BS>(ps.get(k), n, bits, w);
+      code_planes<BS>(k, kmin, n, bits, w, [&](int kk) { return ps.get(kk); });
     }
   } else if constexpr (BS == 64) {
     planes_to_store<0>(u, ps);
-#pragma unroll 1
-    for (; k >= kmin && bits; k--) code_plane<BS>(ps.get(k), n, bits, w);
+    code_planes<BS>(k, kmin, n, bits, w, [&](int kk) { return ps.get(kk); });
   } else {
     PL pl;
 #pragma unroll
@@ -792,12 +794,11 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
     }
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, pl.tw[i]);
-#pragma unroll 1
-    for (; k >= kmin && bits; k--) {
-      const int G = k >> 5, kk = k & 31, r = kk % PL::N, g = kk / PL::N;
+    code_planes<BS>(k, kmin, n, bits, w, [&](int kp) {
+      const int G = kp >> 5, kk = kp & 31, r = kk % PL::N, g = kk / PL::N;
       const uint32_t word = (uint32_t)ps.get(G * BS + r);
-      code_plane<BS>((word >> (g * PL::N)) & ((1u << PL::N) - 1), n, bits, w);
-    }
+      return (uint64_t)((word >> (g * PL::N)) & ((1u << PL::N) - 1));
+    });
   }
   w.zeros(bits);
 }
@@ -839,30 +840,26 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& p
       // top-half planes into the store, folded into the coefficients before
       // the bottom half reuses the store
       const int top = k;
-#pragma unroll 1
-      for (; k >= 32 && k >= kmin && bits; k--) ps.put(k - 32, uncode_plane<BS>(n, bits, r));
+      k = uncode_planes<BS>(k, kmin > 32 ? kmin : 32, n, bits, r,
+                            [&](int kk, uint64_t x) { ps.put(kk - 32, x); });
       store_to_coeffs<1>(ps, 0, k - 32, top - 32, u);
       if (k >= kmin && bits) {
         const int top0 = k;
-#pragma unroll 1
-        for (; k >= kmin && bits; k--) ps.put(k, uncode_plane<BS>(n, bits, r));
+        k = uncode_planes<BS>(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
         store_to_coeffs<0>(ps, 0, k, top0, u);
       }
     } else {
       const int top = k;
-#pragma unroll 1
-      for (; k >= kmin && bits; k--) ps.put(k, uncode_plane<BS>(n, bits, r));
+      k = uncode_planes<BS>(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
       store_to_coeffs<0>(ps, 0, k, top, u);
     }
   } else {
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, 0);
-#pragma unroll 1
-    for (; k >= kmin && bits; k--) {
-      const int G = k >> 5, kk = k & 31, rr = kk % PL::N, g = kk / PL::N;
-      const uint64_t x = uncode_plane<BS>(n, bits, r);
+    uncode_planes<BS>(k, kmin, n, bits, r, [&](int kp, uint64_t x) {
+      const int G = kp >> 5, kk = kp & 31, rr = kk % PL::N, g = kk / PL::N;
       ps.put(G * BS + rr, ps.get(G * BS + rr) | (x << (g * PL::N)));
-    }
+    });
     PL pl;
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) pl.tw[i] = (uint32_t)ps.get(i);

@@ -23,10 +23,6 @@ namespace gzfp {
 constexpr int kThreads = 128;            // threads (= blocks) per CTA
 constexpr int kStride = kThreads + 1;    // staged word buffer row pitch (words)
 constexpr uint32_t kMaxStagedWords = 64; // staged decode up to 4096-bit blocks
-// 4^3 double blocks of more than this many bits park their bottom 32-bit
-// slice in shared memory instead of recomputing it when it is reached
-constexpr uint32_t kSpillBits = 1100;
-
 // dynamic shared memory of a CTA: the plane store (32 or 64 slots of 8
 // bytes per thread) and, for staged decode, the word buffer
 inline size_t smem_bytes(int slots, bool staged, uint32_t words_per_block) {
@@ -99,7 +95,14 @@ struct MinBlocks {
   static constexpr int value = (D == 3 && sizeof(T) == 8) ? 3 : 4;
 };
 
-template <int D, typename T, bool SPILL>
+// plane-store slots per thread: 64 for 4^3 double blocks (two 32-plane
+// halves' worth), 32 otherwise
+template <int D, typename T>
+constexpr int store_slots() {
+  return (D == 3 && sizeof(T) == 8) ? 64 : 32;
+}
+
+template <int D, typename T>
 __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
     encode_kernel(const T* __restrict__ in, Geom g, uint32_t maxbits, uint64_t* __restrict__ out,
                   uint64_t nwords, Ctx c) {
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
   SmemPlanes ps{smem + threadIdx.x};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b < g.nblocks)
-    encode_one<D, T, SPILL>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps, c);
+    encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps, c);
 }
 
 template <int D, typename T, bool STAGED>
@@ -141,9 +144,8 @@ cudaError_t launch_encode_t(const T* in, const Geom& g, uint32_t maxbits, uint64
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   const Ctx c{1u, 0xffffffffu};
-  const bool spill = D == 3 && sizeof(T) == 8 && maxbits > kSpillBits;
-  const size_t sm = smem_bytes(spill ? 64 : 32, false, 0);
-  auto k = spill ? encode_kernel<D, T, true> : encode_kernel<D, T, false>;
+  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0);
+  auto k = encode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   k<<<grid, kThreads, sm, s>>>(in, g, maxbits, out, nwords, c);

@@ -25,9 +25,7 @@ struct HostWords {
 bool geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
   if (!nx || (nz && !ny)) return false;
   dims = nz ? 3 : ny ? 2 : 1;
-  g.nx = nx; g.ny = ny ? ny : 1; g.nz = nz ? nz : 1;
-  g.bx = (g.nx + 3) / 4; g.by = (g.ny + 3) / 4; g.bz = (g.nz + 3) / 4;
-  g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  g = gzfp::make_geom_blocks(nx, ny ? ny : 1, nz ? nz : 1);
   g.vec = (nx % 4 == 0);  // memcpy rows on the host: only the index math matters
   return true;
 }
@@ -43,13 +41,8 @@ void enc(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out,
   HostWords w{out, nullptr, words};
   gzfp::LocalPlanes ps;
   const gzfp::Ctx c{1u, 0xffffffffu};
-  // both lower-slice strategies of the 4^3 double coder must agree
-  for (uint64_t b = 0; b < g.nblocks; b++) {
-    if (b & 1)
-      gzfp::encode_one<D, T, true>((const T*)data, g, b, maxbits, w, ps, c);
-    else
-      gzfp::encode_one<D, T, false>((const T*)data, g, b, maxbits, w, ps, c);
-  }
+  for (uint64_t b = 0; b < g.nblocks; b++)
+    gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w, ps, c);
 }
 
 template <int D, typename T>
