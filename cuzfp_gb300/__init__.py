@@ -312,9 +312,153 @@ def version() -> int:
     return int(_lib.gzfp_version())
 
 
+# ------------------------------------------------------------------ batches
+
+class BatchItem(ctypes.Structure):
+    """gzfp_batch_item (include/gzfp.h)."""
+    _fields_ = [("type", _I), ("nx", _U), ("ny", _U), ("nz", _U), ("maxbits", _U),
+                ("field", _VP), ("stream", _VP), ("stream_capacity", _SZ)]
+
+
+class BatchConfig(ctypes.Structure):
+    """gzfp_batch_config: threads per CTA, resident CTAs per SM, blocks per
+    thread per claimed chunk, claim-ahead flag."""
+    _fields_ = [("threads", _I), ("ctas_per_sm", _I), ("blocks_per_thread", _I),
+                ("claim_ahead", _I)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+_lib.gzfp_batch_default_config.restype = None
+_lib.gzfp_batch_default_config.argtypes = [ctypes.POINTER(BatchConfig)]
+_lib.gzfp_batch_last_error.restype = ctypes.c_char_p
+for _fn in (_lib.gzfp_batch_compress, _lib.gzfp_batch_decompress):
+    _fn.restype = _I
+    _fn.argtypes = [ctypes.POINTER(BatchItem), _I, ctypes.POINTER(BatchConfig), _VP]
+_lib.gzfp_batch_plan_create.restype = _I
+_lib.gzfp_batch_plan_create.argtypes = [ctypes.POINTER(BatchItem), _I, _I,
+                                        ctypes.POINTER(BatchConfig), ctypes.POINTER(_VP)]
+_lib.gzfp_batch_plan_launch.restype = _I
+_lib.gzfp_batch_plan_launch.argtypes = [_VP, _VP]
+_lib.gzfp_batch_plan_destroy.restype = None
+_lib.gzfp_batch_plan_destroy.argtypes = [_VP]
+_lib.gzfp_batch_autotune.restype = _I
+_lib.gzfp_batch_autotune.argtypes = [ctypes.POINTER(BatchItem), _I, _I, _I,
+                                     ctypes.POINTER(BatchConfig), ctypes.POINTER(ctypes.c_float),
+                                     _VP]
+
+
+class BatchError(GzfpError):
+    def __init__(self, status: int, what: str):
+        RuntimeError.__init__(self, f"{what}: {_lib.gzfp_status_string(status).decode()} "
+                                    f"({_lib.gzfp_batch_last_error().decode()})")
+        self.status = status
+
+
+def _bcheck(status: int, what: str) -> None:
+    if status != GZFP_OK:
+        raise BatchError(status, what)
+
+
+def default_batch_config() -> BatchConfig:
+    c = BatchConfig()
+    _lib.gzfp_batch_default_config(ctypes.byref(c))
+    return c
+
+
+def batch_items(fields, streams, rates):
+    """ctypes array of gzfp_batch_item for CUDA tensors `fields` (float32 /
+    float64, 1-3 dims), stream word tensors `streams` and per-array rates."""
+    items = (BatchItem * len(fields))()
+    for i, (f, w, r) in enumerate(zip(fields, streams, rates)):
+        t = _type_of(f.dtype)
+        nx, ny, nz = _dims_of(f.shape)
+        items[i] = BatchItem(int(t), nx, ny, nz,
+                             _lib.gzfp_rate_to_maxbits(int(t), len(f.shape), float(r)),
+                             f.data_ptr(), w.data_ptr(), w.numel() * w.element_size())
+    return items
+
+
+def batch_stream_buffers(fields, rates):
+    """Word tensors sized for each array's fixed-rate stream."""
+    import torch
+    out = []
+    for f, r in zip(fields, rates):
+        t = _type_of(f.dtype)
+        nx, ny, nz = _dims_of(f.shape)
+        mb = _lib.gzfp_rate_to_maxbits(int(t), len(f.shape), float(r))
+        out.append(torch.empty(stream_size(t, nx, ny, nz, mb) // 8, dtype=torch.int64,
+                               device=f.device))
+    return out
+
+
+def compress_batch(fields, rates, streams=None, config: Optional[BatchConfig] = None,
+                   cuda_stream: Any = None):
+    """Compress many CUDA arrays with one persistent kernel; returns the
+    stream word tensors (one per array)."""
+    if streams is None:
+        streams = batch_stream_buffers(fields, rates)
+    items = batch_items(fields, streams, rates)
+    _bcheck(_lib.gzfp_batch_compress(items, len(items), ctypes.byref(config) if config else None,
+                                     _cuda_stream_handle(cuda_stream)), "compress_batch")
+    return streams
+
+
+def decompress_batch(streams, fields, rates, config: Optional[BatchConfig] = None,
+                     cuda_stream: Any = None):
+    """Decompress many streams into the CUDA tensors `fields` (shape and
+    dtype give each array's geometry)."""
+    items = batch_items(fields, streams, rates)
+    _bcheck(_lib.gzfp_batch_decompress(items, len(items),
+                                       ctypes.byref(config) if config else None,
+                                       _cuda_stream_handle(cuda_stream)), "decompress_batch")
+    return fields
+
+
+class BatchPlan:
+    """A batch captured in a CUDA graph; launch() replays it."""
+
+    def __init__(self, fields, streams, rates, decompress: bool = False,
+                 config: Optional[BatchConfig] = None):
+        self._items = batch_items(fields, streams, rates)
+        self._keep = (list(fields), list(streams))
+        h = _VP()
+        _bcheck(_lib.gzfp_batch_plan_create(self._items, len(self._items), int(decompress),
+                                            ctypes.byref(config) if config else None,
+                                            ctypes.byref(h)), "BatchPlan")
+        self._h = h
+
+    def launch(self, cuda_stream: Any = None) -> None:
+        _bcheck(_lib.gzfp_batch_plan_launch(self._h, _cuda_stream_handle(cuda_stream)),
+                "BatchPlan.launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.gzfp_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def autotune_batch(fields, streams, rates, decompress: bool = False, repeats: int = 3,
+                   cuda_stream: Any = None):
+    """Time every launch shape on this batch; returns (BatchConfig, ms)."""
+    items = batch_items(fields, streams, rates)
+    best = BatchConfig()
+    ms = ctypes.c_float(0)
+    _bcheck(_lib.gzfp_batch_autotune(items, len(items), int(decompress), int(repeats),
+                                     ctypes.byref(best), ctypes.byref(ms),
+                                     _cuda_stream_handle(cuda_stream)), "autotune_batch")
+    return best, float(ms.value)
+
+
 __all__ = [
     "GzfpError", "zfp_type", "zfp_stream", "zfp_field", "zfp_stream_open", "zfp_field_1d",
     "zfp_field_2d", "zfp_field_3d", "zfp_field_dimensionality", "zfp_type_size",
     "stream_set_rate", "zfp_stream_maximum_size", "stream_size", "compress", "decompress",
-    "compress_tensor", "decompress_tensor", "version", "LIB_PATH",
+    "compress_tensor", "decompress_tensor", "version", "LIB_PATH", "BatchItem", "BatchConfig",
+    "default_batch_config", "compress_batch", "decompress_batch", "BatchPlan", "autotune_batch",
+    "batch_stream_buffers",
 ]

@@ -1,0 +1,350 @@
+// gzfp_batch.cu -- host side of the batched path (include/gzfp.h, "batch").
+//
+// Builds the device work list of a batch (array descriptors and the
+// chunk -> array table), launches the persistent kernel, captures the whole
+// batch in a CUDA graph ("plans") and tunes the launch shape.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "gzfp.h"
+#include "gzfp_batch_launch.h"
+
+namespace gzfp {
+
+// Fill chunk_item[first_chunk .. first_chunk + chunks) of every array.
+__global__ void batch_chunk_table(const BatchDesc* __restrict__ descs, int count,
+                                  uint32_t* chunk_item, uint64_t nchunks) {
+  const int i = blockIdx.y;
+  if (i >= count) return;
+  const uint64_t lo = descs[i].first_chunk;
+  const uint64_t hi = i + 1 < count ? descs[i + 1].first_chunk : nchunks;
+  for (uint64_t cidx = lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; cidx < hi;
+       cidx += (uint64_t)gridDim.x * blockDim.x)
+    chunk_item[cidx] = (uint32_t)i;
+}
+
+}  // namespace gzfp
+
+namespace {
+
+thread_local char g_batch_error[256];
+
+int bfail(int status, const char* msg) {
+  snprintf(g_batch_error, sizeof g_batch_error, "%s", msg);
+  return status;
+}
+int bcuda(cudaError_t e, const char* what) {
+  snprintf(g_batch_error, sizeof g_batch_error, "%s: %s", what, cudaGetErrorString(e));
+  return GZFP_ERR_CUDA;
+}
+
+constexpr int kMaxBatchItems = 65535;
+
+bool valid_config(const gzfp_batch_config& c) {
+  return (c.threads == 64 || c.threads == 128 || c.threads == 256) && c.ctas_per_sm >= 1 &&
+         c.ctas_per_sm <= 16 && (c.blocks_per_thread == 1 || c.blocks_per_thread == 2 ||
+                                 c.blocks_per_thread == 4);
+}
+
+int occupancy(int threads, bool decode) {
+  switch (threads) {
+    case 64: return gzfp::batch_occupancy_64(decode);
+    case 128: return gzfp::batch_occupancy_128(decode);
+    default: return gzfp::batch_occupancy_256(decode);
+  }
+}
+
+// Host-side description of a batch: descriptors, chunk count, and the
+// streams that neighbouring blocks share words of (zeroed before launch).
+struct Prepared {
+  std::vector<gzfp::BatchDesc> descs;
+  uint64_t nchunks = 0;
+  std::vector<std::pair<void*, size_t>> zero;  // encode only
+};
+
+int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
+            Prepared& p) {
+  if (!items || count < 0 || count > kMaxBatchItems) return bfail(GZFP_ERR_ARG, "bad item list");
+  const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
+  p.descs.resize(count);
+  p.nchunks = 0;
+  p.zero.clear();
+  for (int i = 0; i < count; i++) {
+    const gzfp_batch_item& it = items[i];
+    if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
+      return bfail(GZFP_ERR_UNSUPPORTED, "batch items must be float or double");
+    if (it.nx == 0 || (it.nz != 0 && it.ny == 0)) return bfail(GZFP_ERR_ARG, "bad dimensions");
+    if (!it.field || !it.stream) return bfail(GZFP_ERR_ARG, "null pointer");
+    const unsigned ebits = it.type == GZFP_TYPE_FLOAT ? 8 : 11;
+    if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
+      return bfail(GZFP_ERR_ARG, "bits per block out of range");
+    const int dims = it.nz ? 3 : it.ny ? 2 : 1;
+    gzfp::BatchDesc& d = p.descs[i];
+    d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+    if (d.g.nblocks >= (1ull << 32)) return bfail(GZFP_ERR_ARG, "too many blocks");
+    const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
+    d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+    d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
+    if (it.stream_capacity < d.nwords * 8)
+      return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
+    d.maxbits = it.maxbits;
+    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
+    d.in = decode ? it.stream : it.field;
+    d.out = decode ? it.field : it.stream;
+    d.first_chunk = p.nchunks;
+    p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+    if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
+  }
+  return GZFP_OK;
+}
+
+// Device work list of one batch: descriptors, chunk table and the claim
+// counter, plus a pinned host copy of the descriptors.
+struct WorkList {
+  gzfp::BatchDesc* descs = nullptr;
+  gzfp::BatchDesc* host = nullptr;  // pinned
+  size_t desc_cap = 0;
+  uint32_t* chunk_item = nullptr;
+  size_t chunk_cap = 0;
+  unsigned long long* counter = nullptr;
+
+  cudaError_t reserve(size_t ndesc, size_t nchunks) {
+    cudaError_t e = cudaSuccess;
+    if (!counter && (e = cudaMalloc(&counter, sizeof(unsigned long long)))) return e;
+    if (ndesc > desc_cap) {
+      cudaFree(descs);
+      cudaFreeHost(host);
+      descs = nullptr;
+      host = nullptr;
+      desc_cap = 0;
+      if ((e = cudaMalloc(&descs, ndesc * sizeof(gzfp::BatchDesc)))) return e;
+      if ((e = cudaMallocHost(&host, ndesc * sizeof(gzfp::BatchDesc)))) return e;
+      desc_cap = ndesc;
+    }
+    if (nchunks > chunk_cap) {
+      cudaFree(chunk_item);
+      chunk_item = nullptr;
+      chunk_cap = 0;
+      if ((e = cudaMalloc(&chunk_item, nchunks * sizeof(uint32_t)))) return e;
+      chunk_cap = nchunks;
+    }
+    return e;
+  }
+  void release() {
+    cudaFree(descs);
+    cudaFreeHost(host);
+    cudaFree(chunk_item);
+    cudaFree(counter);
+    descs = nullptr;
+    host = nullptr;
+    chunk_item = nullptr;
+    counter = nullptr;
+    desc_cap = chunk_cap = 0;
+  }
+};
+
+// Queue everything one batch needs on stream s: zeroing of shared-word
+// streams, descriptor upload, chunk table, counter reset, persistent kernel.
+cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_batch_config& cfg,
+                    cudaStream_t s) {
+  cudaError_t e;
+  const int count = (int)p.descs.size();
+  if (count == 0 || p.nchunks == 0) return cudaSuccess;
+  for (const auto& z : p.zero)
+    if ((e = cudaMemsetAsync(z.first, 0, z.second, s))) return e;
+  if ((e = cudaMemcpyAsync(wl.descs, wl.host, count * sizeof(gzfp::BatchDesc),
+                           cudaMemcpyHostToDevice, s)))
+    return e;
+  const dim3 tgrid(64, (unsigned)count);
+  gzfp::batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.nchunks);
+  if ((e = cudaGetLastError())) return e;
+  if ((e = cudaMemsetAsync(wl.counter, 0, sizeof(unsigned long long), s))) return e;
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev))) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
+  int per_sm = std::min(cfg.ctas_per_sm, std::max(1, occupancy(cfg.threads, decode)));
+  const int grid = sms * per_sm;
+  const bool ahead = cfg.claim_ahead != 0;
+  switch (cfg.threads) {
+    case 64:
+      return gzfp::launch_batch_64(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
+                                   wl.chunk_item, p.nchunks, wl.counter, s);
+    case 128:
+      return gzfp::launch_batch_128(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
+                                    wl.chunk_item, p.nchunks, wl.counter, s);
+    default:
+      return gzfp::launch_batch_256(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
+                                    wl.chunk_item, p.nchunks, wl.counter, s);
+  }
+}
+
+struct DeviceWork {
+  std::mutex mu;
+  WorkList wl;
+};
+constexpr int kMaxDevices = 64;
+DeviceWork g_work[kMaxDevices];
+
+int run_batch(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg_in,
+              void* cuda_stream, bool decode) {
+  g_batch_error[0] = 0;
+  gzfp_batch_config cfg;
+  gzfp_batch_default_config(&cfg);
+  if (cfg_in) cfg = *cfg_in;
+  if (!valid_config(cfg)) return bfail(GZFP_ERR_ARG, "bad batch configuration");
+  Prepared p;
+  int st = prepare(items, count, decode, cfg, p);
+  if (st) return st;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return bcuda(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return bfail(GZFP_ERR_CUDA, "device index out of range");
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  DeviceWork& dw = g_work[dev];
+  std::lock_guard<std::mutex> lock(dw.mu);
+  if ((e = dw.wl.reserve(p.descs.size(), p.nchunks))) return bcuda(e, "batch work list allocation");
+  // the pinned descriptor copy is reused by the next call: wait until the
+  // previous upload from it has finished
+  if ((e = cudaStreamSynchronize(s))) return bcuda(e, "cudaStreamSynchronize");
+  memcpy(dw.wl.host, p.descs.data(), p.descs.size() * sizeof(gzfp::BatchDesc));
+  if ((e = enqueue(p, dw.wl, decode, cfg, s))) return bcuda(e, "batch launch");
+  return GZFP_OK;
+}
+
+}  // namespace
+
+struct gzfp_batch_plan {
+  WorkList wl;
+  Prepared p;
+  bool decode = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+};
+
+extern "C" {
+
+const char* gzfp_batch_last_error(void) { return g_batch_error; }
+
+void gzfp_batch_default_config(gzfp_batch_config* cfg) {
+  if (!cfg) return;
+  cfg->threads = 128;
+  cfg->ctas_per_sm = 16;  // as many as fit
+  cfg->blocks_per_thread = 1;
+  cfg->claim_ahead = 1;
+}
+
+int gzfp_batch_compress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
+                        void* cuda_stream) {
+  return run_batch(items, count, cfg, cuda_stream, false);
+}
+
+int gzfp_batch_decompress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
+                          void* cuda_stream) {
+  return run_batch(items, count, cfg, cuda_stream, true);
+}
+
+int gzfp_batch_plan_create(const gzfp_batch_item* items, int count, int decompress,
+                           const gzfp_batch_config* cfg_in, gzfp_batch_plan** out) {
+  g_batch_error[0] = 0;
+  if (!out) return bfail(GZFP_ERR_ARG, "null plan pointer");
+  *out = nullptr;
+  gzfp_batch_config cfg;
+  gzfp_batch_default_config(&cfg);
+  if (cfg_in) cfg = *cfg_in;
+  if (!valid_config(cfg)) return bfail(GZFP_ERR_ARG, "bad batch configuration");
+  gzfp_batch_plan* plan = new gzfp_batch_plan();
+  plan->decode = decompress != 0;
+  int st = prepare(items, count, plan->decode, cfg, plan->p);
+  cudaError_t e = cudaSuccess;
+  cudaStream_t s = nullptr;
+  if (!st && (e = cudaGetDevice(&plan->device))) st = bcuda(e, "cudaGetDevice");
+  if (!st && (e = plan->wl.reserve(plan->p.descs.size(), plan->p.nchunks)))
+    st = bcuda(e, "plan work list allocation");
+  if (!st) memcpy(plan->wl.host, plan->p.descs.data(), plan->p.descs.size() * sizeof(gzfp::BatchDesc));
+  if (!st && (e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking))) st = bcuda(e, "cudaStreamCreate");
+  if (!st && (e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)))
+    st = bcuda(e, "cudaStreamBeginCapture");
+  if (!st) {
+    cudaError_t el = enqueue(plan->p, plan->wl, plan->decode, cfg, s);
+    cudaError_t ec = cudaStreamEndCapture(s, &plan->graph);
+    if (el) st = bcuda(el, "plan capture");
+    else if (ec) st = bcuda(ec, "cudaStreamEndCapture");
+  }
+  if (!st && (e = cudaGraphInstantiate(&plan->exec, plan->graph, 0)))
+    st = bcuda(e, "cudaGraphInstantiate");
+  if (s) cudaStreamDestroy(s);
+  if (st) {
+    gzfp_batch_plan_destroy(plan);
+    return st;
+  }
+  *out = plan;
+  return GZFP_OK;
+}
+
+int gzfp_batch_plan_launch(gzfp_batch_plan* plan, void* cuda_stream) {
+  g_batch_error[0] = 0;
+  if (!plan || !plan->exec) return bfail(GZFP_ERR_ARG, "null plan");
+  cudaError_t e = cudaGraphLaunch(plan->exec, (cudaStream_t)cuda_stream);
+  return e ? bcuda(e, "cudaGraphLaunch") : GZFP_OK;
+}
+
+void gzfp_batch_plan_destroy(gzfp_batch_plan* plan) {
+  if (!plan) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  plan->wl.release();
+  delete plan;
+}
+
+int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress, int repeats,
+                        gzfp_batch_config* best, float* best_ms, void* cuda_stream) {
+  g_batch_error[0] = 0;
+  if (!best) return bfail(GZFP_ERR_ARG, "null result pointer");
+  if (repeats < 1) repeats = 1;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e;
+  if ((e = cudaEventCreate(&a)) || (e = cudaEventCreate(&b))) return bcuda(e, "cudaEventCreate");
+  float top = -1;
+  int st = GZFP_OK;
+  const int threads[] = {64, 128, 256};
+  const int bpts[] = {1, 2, 4};
+  // every candidate is timed as it is meant to run: a graph replay
+  for (int nt : threads) {
+    const int occ = std::max(1, occupancy(nt, decompress != 0));
+    for (int per_sm = 1; per_sm <= occ && !st; per_sm++) {
+      for (int bpt : bpts) {
+        for (int ahead = 0; ahead < 2 && !st; ahead++) {
+          const gzfp_batch_config cfg{nt, per_sm, bpt, ahead};
+          gzfp_batch_plan* plan = nullptr;
+          st = gzfp_batch_plan_create(items, count, decompress, &cfg, &plan);
+          if (!st) st = gzfp_batch_plan_launch(plan, s);  // untimed
+          if (!st && (e = cudaEventRecord(a, s))) st = bcuda(e, "cudaEventRecord");
+          for (int r = 0; r < repeats && !st; r++) st = gzfp_batch_plan_launch(plan, s);
+          if (!st && ((e = cudaEventRecord(b, s)) || (e = cudaEventSynchronize(b))))
+            st = bcuda(e, "timing");
+          float ms = 0;
+          if (!st) cudaEventElapsedTime(&ms, a, b);
+          gzfp_batch_plan_destroy(plan);
+          if (st) break;
+          ms /= repeats;
+          if (top < 0 || ms < top) {
+            top = ms;
+            *best = cfg;
+          }
+        }
+      }
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!st && best_ms) *best_ms = top;
+  return st;
+}
+
+}  // extern "C"

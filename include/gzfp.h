@@ -88,6 +88,61 @@ int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned
 int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
                          const void* stream, size_t bytes, void* data, void* cuda_stream);
 
+/* ------------------------------------------------------------ batches ---
+   Many arrays -- each with its own shape, scalar type, dimensionality and
+   bits per block -- coded by one persistent kernel over a device-side work
+   list of (array, chunk of blocks) items.  Every array's stream is the one
+   gzfp_compress_bits would write.  Device pointers only; calls are
+   asynchronous on `cuda_stream`.  No counterpart in cuZFP, which codes one
+   array per call (src/cuZFP/cuZFP.cu:174-269). */
+
+typedef struct {
+  int type;               /* GZFP_TYPE_FLOAT or GZFP_TYPE_DOUBLE */
+  unsigned nx, ny, nz;    /* as gzfp_compress: ny = 0 for 1D, nz = 0 for 2D */
+  unsigned maxbits;       /* bits per block (gzfp_rate_to_maxbits) */
+  void* field;            /* device array: input of compress, output of decompress */
+  void* stream;           /* device words: output of compress, input of decompress */
+  size_t stream_capacity; /* bytes at `stream` */
+} gzfp_batch_item;
+
+/* Launch shape of the persistent kernel: threads per CTA (64, 128, 256),
+   resident CTAs per SM (capped at what fits), blocks per thread per claimed
+   chunk (1, 2, 4) and whether the next chunk is claimed while the current
+   one is coded (claim_ahead). */
+typedef struct {
+  int threads;
+  int ctas_per_sm;
+  int blocks_per_thread;
+  int claim_ahead;
+} gzfp_batch_config;
+
+void gzfp_batch_default_config(gzfp_batch_config* cfg);
+
+/* Detail of the last batch-path failure on the calling thread. */
+const char* gzfp_batch_last_error(void);
+
+/* One batch, built and launched now (cfg may be NULL for the default).  The
+   library's per-device work list is reused by the next call, which waits
+   for this one's upload to finish. */
+int gzfp_batch_compress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
+                        void* cuda_stream);
+int gzfp_batch_decompress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
+                          void* cuda_stream);
+
+/* A batch prepared once and captured in a CUDA graph (work list upload,
+   zeroing, claim counter reset, persistent kernel); each launch replays it
+   on the same buffers. */
+typedef struct gzfp_batch_plan gzfp_batch_plan;
+int gzfp_batch_plan_create(const gzfp_batch_item* items, int count, int decompress,
+                           const gzfp_batch_config* cfg, gzfp_batch_plan** plan);
+int gzfp_batch_plan_launch(gzfp_batch_plan* plan, void* cuda_stream);
+void gzfp_batch_plan_destroy(gzfp_batch_plan* plan);
+
+/* Time every launch shape on this batch (graph replays, `repeats` each)
+   and return the fastest in *best and its time in *best_ms. */
+int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress, int repeats,
+                        gzfp_batch_config* best, float* best_ms, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
