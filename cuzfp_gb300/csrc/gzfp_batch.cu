@@ -217,6 +217,10 @@ int run_batch(const gzfp_batch_item* items, int count, const gzfp_batch_config* 
 
 }  // namespace
 
+void gzfp::batch_set_error(const char* msg) {
+  snprintf(g_batch_error, sizeof g_batch_error, "%s", msg);
+}
+
 struct gzfp_batch_plan {
   WorkList wl;
   Prepared p;

@@ -25,4 +25,7 @@ int batch_occupancy_64(bool decode);
 int batch_occupancy_128(bool decode);
 int batch_occupancy_256(bool decode);
 
+// Record the detail that gzfp_batch_last_error returns on this thread.
+void batch_set_error(const char* msg);
+
 }  // namespace gzfp

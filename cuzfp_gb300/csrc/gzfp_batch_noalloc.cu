@@ -1,0 +1,170 @@
+// gzfp_batch_noalloc.cu -- gzfp_batch_run_noalloc (include/gzfp.h): the
+// batched persistent codec with its work list in a fixed, file-scope device
+// array instead of memory allocated per call.
+//
+// The kernels are the batch path's own (gzfp_batch.cuh); only where their
+// scratch lives differs.  Scratch layout, one copy per device (a __device__
+// array is instantiated in every context that loads the module):
+//   [0, 256)                      claim counter (zeroed before every launch)
+//   [256, 256 + descs)            array descriptors, uploaded every call
+//   [.., + 4 * kNoAllocMaxChunks) chunk -> array table, built on the device
+// Nothing here calls cudaMalloc, cudaMallocHost, cudaFree or an allocating
+// library, and no host heap is touched: descriptors are built in a static
+// host buffer and uploaded with a pageable cudaMemcpyAsync, which the CUDA
+// runtime stages through its own buffers and which returns only once the
+// host buffer may be reused.
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "gzfp.h"
+#include "gzfp_batch_launch.h"
+
+namespace {
+
+constexpr int kMaxItems = GZFP_NOALLOC_MAX_ITEMS;
+constexpr uint64_t kMaxChunks = GZFP_NOALLOC_MAX_CHUNKS;
+constexpr size_t kDescOffset = 256;
+constexpr size_t kDescBytes = (size_t)kMaxItems * sizeof(gzfp::BatchDesc);
+constexpr size_t kTableOffset = (kDescOffset + kDescBytes + 255) / 256 * 256;
+constexpr size_t kScratchBytes = kTableOffset + kMaxChunks * sizeof(uint32_t);
+static_assert(sizeof(gzfp::BatchDesc) % 8 == 0, "descriptor alignment");
+
+__device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices];  // per device, set once
+std::mutex g_mu;                    // guards g_scratch_addr and g_host
+gzfp::BatchDesc g_host[kMaxItems];  // descriptors of the call in flight on the host
+
+// failures are reported through gzfp_batch_last_error
+int nfail(int status, const char* msg) {
+  gzfp::batch_set_error(msg);
+  return status;
+}
+
+int ncuda(cudaError_t e, const char* what) {
+  char msg[256];
+  snprintf(msg, sizeof msg, "%s: %s", what, cudaGetErrorString(e));
+  return nfail(GZFP_ERR_CUDA, msg);
+}
+
+}  // namespace
+
+namespace gzfp {
+__global__ void batch_chunk_table(const BatchDesc* __restrict__ descs, int count,
+                                  uint32_t* chunk_item, uint64_t nchunks);
+}
+
+extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompress,
+                                      const gzfp_batch_config* cfg_in, void* cuda_stream) {
+  gzfp::batch_set_error("");
+  gzfp_batch_config cfg;
+  gzfp_batch_default_config(&cfg);
+  if (cfg_in) cfg = *cfg_in;
+  if (!(cfg.threads == 64 || cfg.threads == 128 || cfg.threads == 256) || cfg.ctas_per_sm < 1 ||
+      cfg.ctas_per_sm > 16 ||
+      !(cfg.blocks_per_thread == 1 || cfg.blocks_per_thread == 2 || cfg.blocks_per_thread == 4))
+    return nfail(GZFP_ERR_ARG, "bad batch configuration");
+  if (!items || count < 0) return nfail(GZFP_ERR_ARG, "bad item list");
+  if (count > kMaxItems) {
+    char msg[160];
+    snprintf(msg, sizeof msg, "batch of %d arrays exceeds the no-alloc scratch limit of %d arrays",
+             count, kMaxItems);
+    return nfail(GZFP_ERR_CAPACITY, msg);
+  }
+  if (count == 0) return GZFP_OK;
+  const bool decode = decompress != 0;
+  const cudaStream_t s = (cudaStream_t)cuda_stream;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return ncuda(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return nfail(GZFP_ERR_CUDA, "device index out of range");
+
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    if ((e = cudaGetSymbolAddress(&p, g_scratch)))
+      return ncuda(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    g_scratch_addr[dev] = p;
+  }
+  unsigned char* base = (unsigned char*)g_scratch_addr[dev];
+  unsigned long long* counter = (unsigned long long*)base;
+  gzfp::BatchDesc* descs = (gzfp::BatchDesc*)(base + kDescOffset);
+  uint32_t* chunk_item = (uint32_t*)(base + kTableOffset);
+
+  // descriptors: the same validation and layout as the allocating batch path
+  const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
+  uint64_t nchunks = 0;
+  for (int i = 0; i < count; i++) {
+    const gzfp_batch_item& it = items[i];
+    if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
+      return nfail(GZFP_ERR_UNSUPPORTED, "batch items must be float or double");
+    if (it.nx == 0 || (it.nz != 0 && it.ny == 0)) return nfail(GZFP_ERR_ARG, "bad dimensions");
+    if (!it.field || !it.stream) return nfail(GZFP_ERR_ARG, "null pointer");
+    const unsigned ebits = it.type == GZFP_TYPE_FLOAT ? 8 : 11;
+    if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
+      return nfail(GZFP_ERR_ARG, "bits per block out of range");
+    const int dims = it.nz ? 3 : it.ny ? 2 : 1;
+    gzfp::BatchDesc& d = g_host[i];
+    d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+    if (d.g.nblocks >= (1ull << 32)) return nfail(GZFP_ERR_ARG, "too many blocks");
+    const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
+    d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+    d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
+    if (it.stream_capacity < d.nwords * 8)
+      return nfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
+    d.maxbits = it.maxbits;
+    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
+    d.in = decode ? it.stream : it.field;
+    d.out = decode ? it.field : it.stream;
+    d.first_chunk = nchunks;
+    nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+  }
+  if (nchunks > kMaxChunks) {
+    char msg[160];
+    snprintf(msg, sizeof msg, "batch needs %llu chunks of %llu blocks; the no-alloc scratch holds %llu",
+             (unsigned long long)nchunks, (unsigned long long)chunk_blocks,
+             (unsigned long long)kMaxChunks);
+    return nfail(GZFP_ERR_CAPACITY, msg);
+  }
+
+  // streams whose blocks share edge words are assembled with atomic ORs and
+  // must start at zero, as must the claim counter
+  if (!decode)
+    for (int i = 0; i < count; i++)
+      if (items[i].maxbits % 64 &&
+          (e = cudaMemsetAsync(items[i].stream, 0, (size_t)(g_host[i].nwords * 8), s)))
+        return ncuda(e, "cudaMemsetAsync(stream)");
+  if ((e = cudaMemcpyAsync(descs, g_host, count * sizeof(gzfp::BatchDesc), cudaMemcpyHostToDevice,
+                           s)))
+    return ncuda(e, "cudaMemcpyAsync(descriptors)");
+  gzfp::batch_chunk_table<<<dim3(64, (unsigned)count), 256, 0, s>>>(descs, count, chunk_item,
+                                                                    nchunks);
+  if ((e = cudaGetLastError())) return ncuda(e, "chunk table launch");
+  if ((e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s)))
+    return ncuda(e, "cudaMemsetAsync(counter)");
+
+  int sms = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+    return ncuda(e, "cudaDeviceGetAttribute");
+  int occ = cfg.threads == 64    ? gzfp::batch_occupancy_64(decode)
+            : cfg.threads == 128 ? gzfp::batch_occupancy_128(decode)
+                                 : gzfp::batch_occupancy_256(decode);
+  const int grid = sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : (occ > 1 ? occ : 1));
+  const bool ahead = cfg.claim_ahead != 0;
+  const int bpt = cfg.blocks_per_thread;
+  switch (cfg.threads) {
+    case 64:
+      e = gzfp::launch_batch_64(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
+      break;
+    case 128:
+      e = gzfp::launch_batch_128(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
+      break;
+    default:
+      e = gzfp::launch_batch_256(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
+      break;
+  }
+  return e ? ncuda(e, "batch kernel launch") : GZFP_OK;
+}

@@ -143,6 +143,40 @@ void gzfp_batch_plan_destroy(gzfp_batch_plan* plan);
 int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress, int repeats,
                         gzfp_batch_config* best, float* best_ms, void* cuda_stream);
 
+/* ---------------------------------------------------- no-alloc batches ---
+   gzfp_batch_compress / gzfp_batch_decompress (decompress = 0 / 1) with no
+   memory allocated by the call: the work list (claim counter, array
+   descriptors, chunk table) lives in a fixed device array compiled into the
+   library, about 2.1 MiB per device.  No counterpart in cuZFP, which
+   cudaMallocs and frees on every host-pointer call (src/cuZFP/cuZFP.cu:107-170).
+
+   For callers that must not allocate: code running inside a device-memory
+   allocator or its out-of-memory handler (an allocation there re-enters the
+   allocator), programs whose caching allocator has already reserved nearly
+   all device memory, and latency-bound loops that cannot afford cudaFree's
+   device-wide synchronisation or a failed cudaMalloc in the middle of a step.
+
+   Limits: at most GZFP_NOALLOC_MAX_ITEMS arrays and GZFP_NOALLOC_MAX_CHUNKS
+   chunks of threads * blocks_per_thread zfp blocks (2^19 chunks of 128
+   blocks = 2^26 blocks at the default shape); larger batches are rejected
+   with GZFP_ERR_CAPACITY and a message naming the limit, before any GPU work.
+
+   Set-up: the first call on each device, with that device current, looks up
+   the array's device address (cudaGetSymbolAddress); with lazy module loading
+   this is also when the driver loads the module, so make the first call
+   before any stream capture.  No graph-capture support is claimed.
+
+   The call waits on the host for earlier work on `cuda_stream` (the
+   descriptor upload is a pageable copy) and then queues its work
+   asynchronously.  All calls on one device share the one work list:
+   calls whose work overlaps on the device -- from different streams or
+   threads without ordering between them -- race and give wrong streams.
+   Calls in sequence on one stream are safe. */
+#define GZFP_NOALLOC_MAX_ITEMS 1024
+#define GZFP_NOALLOC_MAX_CHUNKS (1u << 19)
+int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompress,
+                           const gzfp_batch_config* cfg, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
