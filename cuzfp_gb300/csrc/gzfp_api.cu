@@ -59,14 +59,33 @@ bool is_device_pointer(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Device buffers used to stage host arrays and streams, one set per device,
-// grown on demand and kept for the life of the process.
-struct Workspace {
-  std::mutex mu;
+// Host-staged calls are cut into slabs of whole block layers along the
+// slowest axis (z in 3D, y in 2D, x in 1D).  A slab's values are one
+// contiguous run of the array and its blocks one contiguous run of the
+// stream; the slab height is chosen so that every slab boundary falls on a
+// 64-bit word, so each slab is coded as an independent array and its stream
+// is exactly the matching word range of the whole stream.  Slabs rotate over
+// kSlots device buffers, each with its own CUDA stream: the upload of one
+// slab, the kernel of the previous one and the download of the one before
+// that overlap, so the call runs at the speed of the host link rather than
+// the sum of copies and kernels.
+constexpr int kSlots = 3;
+constexpr uint64_t kSlabTarget = 32ull << 20;  // field bytes per slab
+
+struct Slot {
   void* field = nullptr;
   size_t field_cap = 0;
   void* stream = nullptr;
   size_t stream_cap = 0;
+  cudaStream_t cs = nullptr;
+};
+
+// Staging state of one device, created on first use and kept for the life
+// of the process.
+struct Workspace {
+  std::mutex mu;
+  Slot slot[kSlots];
+  cudaEvent_t start = nullptr;
 };
 constexpr int kMaxDevices = 64;
 Workspace g_ws[kMaxDevices];
@@ -79,6 +98,72 @@ cudaError_t reserve(void*& p, size_t& cap, size_t need) {
   cudaError_t e = cudaMalloc(&p, need);
   if (e == cudaSuccess) cap = need;
   return e;
+}
+
+cudaError_t init_workspace(Workspace& ws) {
+  cudaError_t e = cudaSuccess;
+  if (!ws.start && (e = cudaEventCreateWithFlags(&ws.start, cudaEventDisableTiming))) return e;
+  for (Slot& sl : ws.slot)
+    if (!sl.cs && (e = cudaStreamCreateWithFlags(&sl.cs, cudaStreamNonBlocking))) return e;
+  return e;
+}
+
+// Slab decomposition of an array: `layers` block layers of `layer_blocks`
+// blocks and 4 planes of `plane_values` values each (the last layer may
+// hold fewer than 4 of the axis' `extent` planes), `per_slab` layers a slab.
+struct Slabs {
+  int dims;
+  unsigned nx, ny;
+  uint64_t extent, layers, layer_blocks, plane_values, per_slab, count;
+};
+
+Slabs plan_slabs(const gzfp::Geom& g, int dims, unsigned maxbits, size_t scalar) {
+  Slabs p;
+  p.dims = dims;
+  p.nx = g.nx;
+  p.ny = g.ny;
+  if (dims == 3) {
+    p.extent = g.nz, p.layers = g.bz, p.layer_blocks = (uint64_t)g.bx * g.by;
+    p.plane_values = (uint64_t)g.nx * g.ny;
+  } else if (dims == 2) {
+    p.extent = g.ny, p.layers = g.by, p.layer_blocks = g.bx, p.plane_values = g.nx;
+  } else {
+    p.extent = g.nx, p.layers = g.bx, p.layer_blocks = 1, p.plane_values = 1;
+  }
+  // slab boundaries on whole words: per_slab * layer_blocks * maxbits % 64 == 0
+  const uint64_t bits = p.layer_blocks * maxbits;
+  int tz = 0;
+  while (tz < 6 && !((bits >> tz) & 1)) tz++;
+  const uint64_t quantum = 64ull >> tz;
+  const uint64_t layer_bytes = 4 * p.plane_values * scalar;
+  uint64_t per = kSlabTarget / layer_bytes / quantum * quantum;
+  if (per < quantum) per = quantum;
+  if (per >= p.layers) per = p.layers;
+  p.per_slab = per;
+  p.count = (p.layers + per - 1) / per;
+  return p;
+}
+
+// Slab j: first plane, plane count, first block, block count, and the
+// array geometry it is coded as.
+struct Slab {
+  uint64_t plane0, planes, block0, blocks;
+  gzfp::Geom g;
+};
+
+Slab slab_at(const Slabs& p, uint64_t j) {
+  Slab s;
+  const uint64_t l0 = j * p.per_slab;
+  const uint64_t l1 = l0 + p.per_slab < p.layers ? l0 + p.per_slab : p.layers;
+  s.plane0 = 4 * l0;
+  s.planes = (4 * l1 < p.extent ? 4 * l1 : p.extent) - s.plane0;
+  s.block0 = l0 * p.layer_blocks;
+  s.blocks = (l1 - l0) * p.layer_blocks;
+  const unsigned n = (unsigned)s.planes;
+  s.g = p.dims == 3   ? gzfp::make_geom_blocks(p.nx, p.ny, n)
+        : p.dims == 2 ? gzfp::make_geom_blocks(p.nx, n, 1)
+                      : gzfp::make_geom_blocks(n, 1, 1);
+  return s;
 }
 
 int check_common(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
@@ -147,6 +232,107 @@ size_t gzfp_maximum_size(int type, unsigned nx, unsigned ny, unsigned nz, unsign
   return (size_t)(((148 + g.nblocks * b + 63) & ~63ull) / 8);
 }
 
+}  // extern "C"
+
+namespace {
+
+cudaError_t encode_launch(int type, int dims, const void* in, const gzfp::Geom& g,
+                          unsigned maxbits, uint64_t* out, uint64_t nwords, cudaStream_t s) {
+  if (type == GZFP_TYPE_FLOAT)
+    return gzfp::launch_encode_f32(dims, (const float*)in, g, maxbits, out, nwords, s);
+  return gzfp::launch_encode_f64(dims, (const double*)in, g, maxbits, out, nwords, s);
+}
+
+cudaError_t decode_launch(int type, int dims, const uint64_t* in, uint64_t nwords,
+                          const gzfp::Geom& g, unsigned maxbits, void* out, cudaStream_t s) {
+  if (type == GZFP_TYPE_FLOAT)
+    return gzfp::launch_decode_f32(dims, in, nwords, g, maxbits, (float*)out, s);
+  return gzfp::launch_decode_f64(dims, in, nwords, g, maxbits, (double*)out, s);
+}
+
+// One host-staged call: slabs through the workspace's slots (see Slabs).
+// `field` / `words` are the caller's pointers; dev_field / dev_words say
+// which of them are device memory.  Returns after the last slab has landed.
+int staged(bool decode, int type, int dims, const gzfp::Geom& g, unsigned maxbits, void* field,
+           bool dev_field, uint64_t* words, bool dev_words, cudaStream_t s) {
+  const size_t scalar = type == GZFP_TYPE_FLOAT ? sizeof(float) : sizeof(double);
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (device < 0 || device >= kMaxDevices) return fail(GZFP_ERR_CUDA, "device index out of range");
+  Workspace& ws = g_ws[device];
+  std::lock_guard<std::mutex> lock(ws.mu);
+  if ((e = init_workspace(ws))) return cuda_fail(e, "staging streams");
+  const Slabs p = plan_slabs(g, dims, maxbits, scalar);
+  const uint64_t slab_values = 4 * p.per_slab * p.plane_values;
+  const uint64_t slab_words = (p.per_slab * p.layer_blocks * maxbits + 63) / 64;
+  for (int k = 0; k < kSlots && (uint64_t)k < p.count; k++) {
+    Slot& sl = ws.slot[k];
+    if (!dev_field && (e = reserve(sl.field, sl.field_cap, (size_t)(slab_values * scalar))))
+      return cuda_fail(e, "cudaMalloc(field staging)");
+    if (!dev_words && (e = reserve(sl.stream, sl.stream_cap, (size_t)(slab_words * 8))))
+      return cuda_fail(e, "cudaMalloc(stream staging)");
+  }
+  // work the caller queued on `s` (say, the kernel that filled a device
+  // field) comes first
+  if ((e = cudaEventRecord(ws.start, s))) return cuda_fail(e, "cudaEventRecord");
+  for (int k = 0; k < kSlots; k++)
+    if ((e = cudaStreamWaitEvent(ws.slot[k].cs, ws.start, 0)))
+      return cuda_fail(e, "cudaStreamWaitEvent");
+  int st = GZFP_OK;
+  for (uint64_t j = 0; j < p.count && !st; j++) {
+    Slot& sl = ws.slot[j % kSlots];
+    const cudaStream_t cs = sl.cs;
+    const Slab b = slab_at(p, j);
+    const size_t fbytes = (size_t)(b.planes * p.plane_values * scalar);
+    char* hf = (char*)field + b.plane0 * p.plane_values * scalar;  // this slab of the field
+    const uint64_t w0 = b.block0 * maxbits / 64;                   // word-aligned by plan_slabs
+    const uint64_t nw = (b.blocks * maxbits + 63) / 64;
+    uint64_t* hw = words + w0;
+    void* df = dev_field ? (void*)hf : sl.field;
+    uint64_t* dw = dev_words ? hw : (uint64_t*)sl.stream;
+    gzfp::Geom gs = b.g;
+    gs.vec = rows_vectorizable(df, p.nx, type);
+    if (!decode) {
+      if (!dev_field && (e = cudaMemcpyAsync(df, hf, fbytes, cudaMemcpyHostToDevice, cs))) {
+        st = cuda_fail(e, "cudaMemcpyAsync(field H2D)");
+        break;
+      }
+      if (maxbits % 64 && (e = cudaMemsetAsync(dw, 0, (size_t)(nw * 8), cs))) {
+        st = cuda_fail(e, "cudaMemsetAsync(stream)");  // blocks share edge words
+        break;
+      }
+      if ((e = encode_launch(type, dims, df, gs, maxbits, dw, nw, cs))) {
+        st = cuda_fail(e, "encode kernel launch");
+        break;
+      }
+      if (!dev_words && (e = cudaMemcpyAsync(hw, dw, (size_t)(nw * 8), cudaMemcpyDeviceToHost, cs)))
+        st = cuda_fail(e, "cudaMemcpyAsync(stream D2H)");
+    } else {
+      if (!dev_words && (e = cudaMemcpyAsync(dw, hw, (size_t)(nw * 8), cudaMemcpyHostToDevice, cs))) {
+        st = cuda_fail(e, "cudaMemcpyAsync(stream H2D)");
+        break;
+      }
+      if ((e = decode_launch(type, dims, dw, nw, gs, maxbits, df, cs))) {
+        st = cuda_fail(e, "decode kernel launch");
+        break;
+      }
+      if (!dev_field && (e = cudaMemcpyAsync(hf, df, fbytes, cudaMemcpyDeviceToHost, cs)))
+        st = cuda_fail(e, "cudaMemcpyAsync(field D2H)");
+    }
+  }
+  // nothing of this call stays in flight, on success or not
+  for (int k = 0; k < kSlots; k++) {
+    cudaError_t es = cudaStreamSynchronize(ws.slot[k].cs);
+    if (es && !st) st = cuda_fail(es, "cudaStreamSynchronize");
+  }
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
 int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
                        const void* data, void* stream, size_t capacity, size_t* out_bytes,
                        void* cuda_stream) {
@@ -162,48 +348,19 @@ int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned
   if (out_bytes) *out_bytes = bytes;
   if (g.nblocks == 0) return GZFP_OK;
   cudaStream_t s = (cudaStream_t)cuda_stream;
-  const size_t field_bytes =
-      (size_t)g.nx * g.ny * g.nz * (type == GZFP_TYPE_FLOAT ? sizeof(float) : sizeof(double));
-
   const bool dev_data = is_device_pointer(data);
   const bool dev_stream = is_device_pointer(stream);
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (device < 0 || device >= kMaxDevices) return fail(GZFP_ERR_CUDA, "device index out of range");
-  Workspace& ws = g_ws[device];
-  std::unique_lock<std::mutex> lock(ws.mu, std::defer_lock);
-  if (!dev_data || !dev_stream) lock.lock();
-
-  const void* d_data = data;
-  uint64_t* d_stream = (uint64_t*)stream;
-  if (!dev_data) {
-    if ((e = reserve(ws.field, ws.field_cap, field_bytes))) return cuda_fail(e, "cudaMalloc(field workspace)");
-    if ((e = cudaMemcpyAsync(ws.field, data, field_bytes, cudaMemcpyHostToDevice, s)))
-      return cuda_fail(e, "cudaMemcpyAsync(field H2D)");
-    d_data = ws.field;
-  }
-  if (!dev_stream) {
-    if ((e = reserve(ws.stream, ws.stream_cap, bytes))) return cuda_fail(e, "cudaMalloc(stream workspace)");
-    d_stream = (uint64_t*)ws.stream;
-  }
+  if (!dev_data || !dev_stream)
+    return staged(false, type, dims, g, maxbits, (void*)data, dev_data, (uint64_t*)stream,
+                  dev_stream, s);
+  cudaError_t e;
   if (maxbits % 64 != 0) {
     // blocks share boundary words, which the kernel ORs into a zeroed stream
-    if ((e = cudaMemsetAsync(d_stream, 0, bytes, s))) return cuda_fail(e, "cudaMemsetAsync(stream)");
+    if ((e = cudaMemsetAsync(stream, 0, bytes, s))) return cuda_fail(e, "cudaMemsetAsync(stream)");
   }
-  g.vec = rows_vectorizable(d_data, nx, type);
-  if (type == GZFP_TYPE_FLOAT)
-    e = gzfp::launch_encode_f32(dims, (const float*)d_data, g, maxbits, d_stream, nwords, s);
-  else
-    e = gzfp::launch_encode_f64(dims, (const double*)d_data, g, maxbits, d_stream, nwords, s);
-  if (e) return cuda_fail(e, "encode kernel launch");
-  if (!dev_stream) {
-    if ((e = cudaMemcpyAsync(stream, d_stream, bytes, cudaMemcpyDeviceToHost, s)))
-      return cuda_fail(e, "cudaMemcpyAsync(stream D2H)");
-  }
-  if (!dev_data || !dev_stream) {
-    if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "cudaStreamSynchronize");
-  }
+  g.vec = rows_vectorizable(data, nx, type);
+  if ((e = encode_launch(type, dims, data, g, maxbits, (uint64_t*)stream, nwords, s)))
+    return cuda_fail(e, "encode kernel launch");
   return GZFP_OK;
 }
 
@@ -220,44 +377,13 @@ int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsign
   if (bytes < need) return fail(GZFP_ERR_ARG, "stream shorter than the compressed size");
   if (g.nblocks == 0) return GZFP_OK;
   cudaStream_t s = (cudaStream_t)cuda_stream;
-  const size_t field_bytes =
-      (size_t)g.nx * g.ny * g.nz * (type == GZFP_TYPE_FLOAT ? sizeof(float) : sizeof(double));
-
   const bool dev_data = is_device_pointer(data);
   const bool dev_stream = is_device_pointer(stream);
-  int device = 0;
-  cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (device < 0 || device >= kMaxDevices) return fail(GZFP_ERR_CUDA, "device index out of range");
-  Workspace& ws = g_ws[device];
-  std::unique_lock<std::mutex> lock(ws.mu, std::defer_lock);
-  if (!dev_data || !dev_stream) lock.lock();
-
-  const uint64_t* d_stream = (const uint64_t*)stream;
-  void* d_data = data;
-  if (!dev_stream) {
-    if ((e = reserve(ws.stream, ws.stream_cap, need))) return cuda_fail(e, "cudaMalloc(stream workspace)");
-    if ((e = cudaMemcpyAsync(ws.stream, stream, need, cudaMemcpyHostToDevice, s)))
-      return cuda_fail(e, "cudaMemcpyAsync(stream H2D)");
-    d_stream = (const uint64_t*)ws.stream;
-  }
-  if (!dev_data) {
-    if ((e = reserve(ws.field, ws.field_cap, field_bytes))) return cuda_fail(e, "cudaMalloc(field workspace)");
-    d_data = ws.field;
-  }
-  g.vec = rows_vectorizable(d_data, nx, type);
-  if (type == GZFP_TYPE_FLOAT)
-    e = gzfp::launch_decode_f32(dims, d_stream, nwords, g, maxbits, (float*)d_data, s);
-  else
-    e = gzfp::launch_decode_f64(dims, d_stream, nwords, g, maxbits, (double*)d_data, s);
+  if (!dev_data || !dev_stream)
+    return staged(true, type, dims, g, maxbits, data, dev_data, (uint64_t*)stream, dev_stream, s);
+  g.vec = rows_vectorizable(data, nx, type);
+  cudaError_t e = decode_launch(type, dims, (const uint64_t*)stream, nwords, g, maxbits, data, s);
   if (e) return cuda_fail(e, "decode kernel launch");
-  if (!dev_data) {
-    if ((e = cudaMemcpyAsync(data, d_data, field_bytes, cudaMemcpyDeviceToHost, s)))
-      return cuda_fail(e, "cudaMemcpyAsync(field D2H)");
-  }
-  if (!dev_data || !dev_stream) {
-    if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "cudaStreamSynchronize");
-  }
   return GZFP_OK;
 }
 

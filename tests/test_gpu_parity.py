@@ -142,6 +142,61 @@ def test_mixed_pointers(gz, orc, cuda):
     assert same_bits(dev_out.cpu().numpy(), orc.decompress(s_ref, a.shape, a.dtype, rate))
 
 
+@pytest.mark.parametrize("shape,dtype,rate", [
+    ((203, 257, 301), np.float32, 7.3),   # 467-bit blocks: slabs of 16 block layers
+    ((2999, 3001), np.float64, 4.0),      # word-sized blocks, ragged last slab
+    (((1 << 24) + 3,), np.float32, 12.0),  # 48-bit blocks, 4 blocks per 3 words
+])
+def test_staged_slabs(gz, cuda, shape, dtype, rate):
+    """Host buffers larger than one staging slab: the slab pipeline gives the
+    stream and array of the all-device call (which the oracle pins), for
+    pinned and pageable host memory and for mixed pointers."""
+    import torch
+    rng = np.random.default_rng(17)
+    a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).astype(dtype).reshape(shape)
+    x = torch.from_numpy(a).to(cuda)
+    w_dev = gz.compress_tensor(x, rate)
+    y_dev = gz.decompress_tensor(w_dev, shape, x.dtype, rate)
+    torch.cuda.synchronize()
+    w_ref = w_dev.cpu()
+    y_ref = y_dev.cpu().numpy()
+    t = gz.zfp_type.float if dtype == np.float32 else gz.zfp_type.double
+    dims = gz._dims_of(shape)
+
+    def field(data):
+        return gz.zfp_field(type=t, nx=dims[0], ny=dims[1], nz=dims[2], data=data)
+
+    for pinned in (True, False):
+        src = torch.from_numpy(a)
+        buf = torch.zeros_like(w_ref)
+        out = torch.zeros(shape, dtype=x.dtype)
+        if pinned:
+            src, buf, out = src.pin_memory(), buf.pin_memory(), out.pin_memory()
+        zfp = gz.zfp_stream(stream=buf)
+        gz.stream_set_rate(zfp, rate, t, len(shape))
+        assert gz.compress(zfp, field(src)) == buf.numel() * 8
+        assert torch.equal(buf, w_ref), pinned
+        gz.decompress(zfp, field(out))
+        assert same_bits(out.numpy(), y_ref), pinned
+    # device array <-> host stream, host stream -> device array
+    buf = torch.zeros_like(w_ref).pin_memory()
+    zfp = gz.zfp_stream(stream=buf)
+    gz.stream_set_rate(zfp, rate, t, len(shape))
+    gz.compress(zfp, field(x))
+    assert torch.equal(buf, w_ref)
+    y = torch.zeros_like(x)
+    gz.decompress(zfp, field(y))
+    torch.cuda.synchronize()
+    assert same_bits(y.cpu().numpy(), y_ref)
+    # host array -> device stream
+    w = torch.zeros_like(w_dev)
+    zfp = gz.zfp_stream(stream=w)
+    gz.stream_set_rate(zfp, rate, t, len(shape))
+    gz.compress(zfp, field(torch.from_numpy(a).pin_memory()))
+    torch.cuda.synchronize()
+    assert torch.equal(w, w_dev)
+
+
 def test_user_stream_async(gz, orc, cuda):
     """Device buffers on a caller's stream: the call is asynchronous and the
     result is complete once that stream is synchronised."""
