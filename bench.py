@@ -51,10 +51,16 @@ def parse():
     p.add_argument("--edge", type=int, default=512,
                    help="cube edge of the field (smaller cases for profiling)")
     p.add_argument("--rate", type=float, default=16.0)
-    p.add_argument("--workload", default="plain3d", choices=["plain3d", "batched"],
+    p.add_argument("--workload", default="plain3d", choices=["plain3d", "batched", "serving"],
                    help="plain3d: the 1 GiB 3D float64 field (default); batched: 512 mixed "
-                        "3D arrays in one persistent launch vs 512 plain launches")
+                        "3D arrays in one persistent launch vs 512 plain launches; serving: "
+                        "Poisson request arrivals through the request server")
     p.add_argument("--arrays", type=int, default=512, help="batched workload: array count")
+    p.add_argument("--requests", type=int, default=20000, help="serving workload: requests")
+    p.add_argument("--inflight", type=int, default=3, help="serving workload: batches in flight")
+    p.add_argument("--max-batch", type=int, default=256, help="serving workload: requests per batch")
+    p.add_argument("--load", type=float, default=0.7,
+                   help="serving workload: arrival rate as a fraction of plain-path capacity")
     args = p.parse_args()
     global SHAPE, RATE, WORKLOAD
     SHAPE = (args.edge,) * 3
@@ -330,6 +336,163 @@ def run_batched(args, rank, world, local):
     print(json.dumps(res), flush=True)
 
 
+# ------------------------------------------------------------ serving loop
+
+def serving_requests(n: int, seed: int = 0):
+    """(op, edge, dtype, rate) of the request mix: cubic arrays with edge
+    log-uniform in 32..384, float32 / float64 50/50, rate from {8, 16, 32},
+    compress / decompress 50/50."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    edges = np.rint(np.exp(rng.uniform(np.log(32), np.log(384), n))).astype(int)
+    f32 = rng.random(n) < 0.5
+    rates = rng.choice([8.0, 16.0, 32.0], n)
+    comp = rng.random(n) < 0.5
+    return [(0 if comp[i] else 1, int(edges[i]), "float32" if f32[i] else "float64",
+             float(rates[i])) for i in range(n)]
+
+
+def run_serving(args, rank, world, local):
+    """Poisson arrivals at 70% of the plain path's capacity through the
+    request server, against serial plain calls on the same requests."""
+    import numpy as np
+    import torch
+
+    import cuzfp_gb300 as gz
+    from cuzfp_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    n = args.requests
+    specs = serving_requests(n, seed=rank)
+    dts = {"float32": torch.float32, "float64": torch.float64}
+    # resident inputs: one 384^3 field per dtype (a request of edge e reads
+    # its first e^3 values as an e^3 cube) and, for decompression, the stream
+    # of every (edge, dtype, rate) that a decompress request names
+    pool = {k: synth.sinusoids_device((384, 384, 384), 16, 32, seed=rank, dtype=v, device=dev)
+            for k, v in dts.items()}
+
+    def field(e, dt):
+        return pool[dt].view(-1)[: e ** 3].view(e, e, e)
+
+    streams = {}
+    for op, e, dt, r in specs:
+        if op == 1 and (e, dt, r) not in streams:
+            streams[(e, dt, r)] = gz.compress_tensor(field(e, dt), r)
+    torch.cuda.synchronize()
+    lib = gz._lib
+    maxf = 384 ** 3 * 8
+    scratch = torch.empty(maxf // 8, dtype=torch.int64, device=dev)
+    nbytes = np.array([e ** 3 * (4 if dt == "float32" else 8) for _, e, dt, _ in specs], float)
+
+    def plain_args(i):
+        op, e, dt, r = specs[i]
+        t = int(gz._type_of(dts[dt]))
+        mb = lib.gzfp_rate_to_maxbits(t, 3, r)
+        sb = gz.stream_size(gz._type_of(dts[dt]), e, e, e, mb)
+        if op == 0:
+            return lib.gzfp_compress_bits, (t, e, e, e, mb, field(e, dt).data_ptr(),
+                                            scratch.data_ptr(), maxf, None, stream.cuda_stream)
+        return lib.gzfp_decompress_bits, (t, e, e, e, mb, streams[(e, dt, r)].data_ptr(), sb,
+                                          scratch.data_ptr(), stream.cuda_stream)
+
+    # serial plain calls: each request's device time = its service time
+    calls = [plain_args(i) for i in range(n)]
+    for fn, a in calls[:50]:
+        fn(*a)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * n)]
+    torch.cuda.synchronize()
+    for i, (fn, a) in enumerate(calls):
+        ev[2 * i].record(stream)
+        if fn(*a) != 0:
+            raise RuntimeError(lib.gzfp_last_error().decode())
+        ev[2 * i + 1].record(stream)
+    torch.cuda.synchronize()
+    service = np.array([ev[2 * i].elapsed_time(ev[2 * i + 1]) * 1e-3 for i in range(n)])
+    plain_gbs = nbytes.sum() / service.sum() / 1e9
+    capacity = n / service.sum()  # requests/s, device time only
+    lam = args.load * capacity
+    rng = np.random.default_rng(1000 + rank)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+    # the plain path under the same arrivals: one FIFO server
+    fin, lat_plain = 0.0, np.empty(n)
+    for i in range(n):
+        fin = max(arrivals[i], fin) + service[i]
+        lat_plain[i] = fin - arrivals[i]
+
+    # sampled requests are checked bit for bit against their plain result
+    sample = list(range(0, n, 97))
+    check, expect = {}, {}
+    for i in sample:
+        op, e, dt, r = specs[i]
+        if op == 0:
+            ref = gz.compress_tensor(field(e, dt), r)
+        else:
+            ref = gz.decompress_tensor(streams[(e, dt, r)], (e, e, e), dts[dt], r)
+        expect[i] = ref
+        check[i] = torch.empty_like(ref)
+    torch.cuda.synchronize()
+
+    def requests(arr):
+        out = []
+        for i, (op, e, dt, r) in enumerate(specs):
+            cp = check.get(i)
+            if op == 0:
+                out.append(gz.serve_request(0, field(e, dt), r, float(arr[i]), copy_to=cp))
+            else:
+                out.append(gz.serve_request(1, streams[(e, dt, r)], r, float(arr[i]),
+                                            shape=(e, e, e), dtype=dts[dt], copy_to=cp))
+        return out
+
+    cfg = gz.default_serve_config()
+    cfg.budget_bytes = 40 << 30
+    cfg.max_inflight = args.inflight
+    cfg.max_batch = args.max_batch
+    with ClockSampler(local) as clk:
+        res, stats = gz.serve(requests(arrivals), cfg)
+    lat = np.array([r.completed - arrivals[i] for i, r in enumerate(res)])
+    ok = all(r.status == 0 for r in res)
+    # saturation: every request queued at time zero
+    sres, sstats = gz.serve(requests(np.zeros(n)), cfg)
+    torch.cuda.synchronize()
+
+    def same(a, b):
+        if a.dtype in (torch.float32, torch.float64):
+            it = torch.int32 if a.dtype == torch.float32 else torch.int64
+            return torch.equal(a.view(it), b.view(it))
+        return torch.equal(a, b)
+
+    bit_identical = ok and all(same(expect[i], check[i]) for i in sample)
+    if rank != 0:
+        return
+    p50, p99 = np.percentile(lat, 50), np.percentile(lat, 99)
+    res_line = {
+        "metric": f"serving p99 latency at {round(100 * args.load)}% of plain-path capacity",
+        "value": round(p99 * 1e3, 4), "unit": "ms", "n_gpus": world, "steps": 1,
+        "warmup": 50, "ms_per_step": round(stats.wall * 1e3, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"serving_{n}_requests_cubic_32to384_poisson{round(100 * args.load)}",
+                   "requests": n, "budget_gb": 40, "arrival_rate_per_s": round(lam, 2),
+                   "uncompressed_bytes": float(nbytes.sum()),
+                   "l2": "inputs larger than L2 (a 384^3 field per dtype, ~2 GB of streams "
+                         "per second of arrivals)",
+                   "server": {"max_batch": cfg.max_batch, "max_inflight": cfg.max_inflight}},
+        "latency_ms": {"p50": round(p50 * 1e3, 4), "p99": round(p99 * 1e3, 4),
+                       "mean": round(float(lat.mean()) * 1e3, 4)},
+        "plain_serial_latency_ms": {"p50": round(np.percentile(lat_plain, 50) * 1e3, 4),
+                                    "p99": round(np.percentile(lat_plain, 99) * 1e3, 4)},
+        "served_gbs": round(nbytes.sum() / stats.wall / 1e9, 2),
+        "saturated_gbs": round(nbytes.sum() / sstats.wall / 1e9, 2),
+        "plain_serial_gbs": round(plain_gbs, 2),
+        "saturated_vs_plain": round(nbytes.sum() / sstats.wall / 1e9 / plain_gbs, 3),
+        "stats": stats.as_dict(), "saturated_stats": sstats.as_dict(),
+        "bit_identical_sample": bool(bit_identical), "checked": len(sample),
+        "gpu_launches": int(stats.kernels), "clocks": clk.summary(),
+    }
+    print(json.dumps(res_line), flush=True)
+
+
 # --------------------------------------------------------------- GPU side
 
 def main():
@@ -344,6 +507,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, rank, world, local)
+        return
+    if args.workload == "serving":
+        run_serving(args, rank, world, local)
         return
     import numpy as np
     import torch

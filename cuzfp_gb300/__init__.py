@@ -454,11 +454,84 @@ def autotune_batch(fields, streams, rates, decompress: bool = False, repeats: in
     return best, float(ms.value)
 
 
+# ------------------------------------------------------------------ serving
+
+GZFP_SERVE_COMPRESS = 0
+GZFP_SERVE_DECOMPRESS = 1
+
+
+class ServeRequest(ctypes.Structure):
+    """gzfp_serve_request (include/gzfp.h)."""
+    _fields_ = [("op", _I), ("type", _I), ("nx", _U), ("ny", _U), ("nz", _U), ("maxbits", _U),
+                ("input", _VP), ("copy_to", _VP), ("arrival", ctypes.c_double)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("admitted", ctypes.c_double), ("completed", ctypes.c_double),
+                ("output_bytes", _SZ), ("batch", _I), ("status", _I)]
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", _SZ), ("max_batch", _I), ("max_inflight", _I),
+                ("compress_cfg", BatchConfig), ("decompress_cfg", BatchConfig)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("wall", ctypes.c_double), ("batches", _I), ("mean_batch", ctypes.c_double),
+                ("peak_bytes", _SZ), ("busy", ctypes.c_double), ("kernels", _I)]
+
+    def as_dict(self) -> dict:
+        return {f: (float(getattr(self, f)) if t is ctypes.c_double else int(getattr(self, f)))
+                for f, t in self._fields_}
+
+
+_lib.gzfp_serve_default_config.restype = None
+_lib.gzfp_serve_default_config.argtypes = [ctypes.POINTER(ServeConfig)]
+_lib.gzfp_serve_run.restype = _I
+_lib.gzfp_serve_run.argtypes = [ctypes.POINTER(ServeRequest), _I, ctypes.POINTER(ServeConfig),
+                                ctypes.POINTER(ServeResult), ctypes.POINTER(ServeStats)]
+
+
+def default_serve_config() -> ServeConfig:
+    c = ServeConfig()
+    _lib.gzfp_serve_default_config(ctypes.byref(c))
+    return c
+
+
+def serve_request(op: int, x, rate: float, arrival: float, shape=None, dtype=None,
+                  copy_to=None) -> ServeRequest:
+    """A request on the resident CUDA tensor ``x``: the field to compress
+    (op GZFP_SERVE_COMPRESS) or the stream words to decompress into an array
+    of ``shape`` / ``dtype``."""
+    if op == GZFP_SERVE_COMPRESS:
+        shape, dtype = x.shape, x.dtype
+    t = _type_of(dtype)
+    nx, ny, nz = _dims_of(shape)
+    mb = _lib.gzfp_rate_to_maxbits(int(t), len(shape), float(rate))
+    req = ServeRequest(op, int(t), nx, ny, nz, mb, x.data_ptr(),
+                       copy_to.data_ptr() if copy_to is not None else None, float(arrival))
+    req._keep = (x, copy_to)  # the request holds raw pointers: keep the tensors alive
+    return req
+
+
+def serve(requests, config: Optional[ServeConfig] = None):
+    """Run the request server over ``requests`` (a sequence of ServeRequest);
+    returns (list of ServeResult, ServeStats)."""
+    reqs = (ServeRequest * len(requests))(*requests)
+    res = (ServeResult * len(requests))()
+    stats = ServeStats()
+    _bcheck(_lib.gzfp_serve_run(reqs, len(requests), ctypes.byref(config) if config else None,
+                                res, ctypes.byref(stats)), "serve")
+    return list(res), stats
+
+
 __all__ = [
     "GzfpError", "zfp_type", "zfp_stream", "zfp_field", "zfp_stream_open", "zfp_field_1d",
     "zfp_field_2d", "zfp_field_3d", "zfp_field_dimensionality", "zfp_type_size",
     "stream_set_rate", "zfp_stream_maximum_size", "stream_size", "compress", "decompress",
     "compress_tensor", "decompress_tensor", "version", "LIB_PATH", "BatchItem", "BatchConfig",
     "default_batch_config", "compress_batch", "decompress_batch", "BatchPlan", "autotune_batch",
-    "batch_stream_buffers",
+    "batch_stream_buffers", "ServeRequest", "ServeResult", "ServeConfig", "ServeStats",
+    "default_serve_config", "serve_request", "serve", "GZFP_SERVE_COMPRESS",
+    "GZFP_SERVE_DECOMPRESS",
 ]

@@ -11,7 +11,7 @@
 #include <vector>
 
 #include "gzfp.h"
-#include "gzfp_batch_launch.h"
+#include "gzfp_batch_host.h"
 
 namespace gzfp {
 
@@ -44,6 +44,11 @@ int bcuda(cudaError_t e, const char* what) {
 
 constexpr int kMaxBatchItems = 65535;
 
+}  // namespace
+
+namespace gzfp {
+namespace bhost {
+
 bool valid_config(const gzfp_batch_config& c) {
   return (c.threads == 64 || c.threads == 128 || c.threads == 256) && c.ctas_per_sm >= 1 &&
          c.ctas_per_sm <= 16 && (c.blocks_per_thread == 1 || c.blocks_per_thread == 2 ||
@@ -52,19 +57,11 @@ bool valid_config(const gzfp_batch_config& c) {
 
 int occupancy(int threads, bool decode) {
   switch (threads) {
-    case 64: return gzfp::batch_occupancy_64(decode);
-    case 128: return gzfp::batch_occupancy_128(decode);
-    default: return gzfp::batch_occupancy_256(decode);
+    case 64: return batch_occupancy_64(decode);
+    case 128: return batch_occupancy_128(decode);
+    default: return batch_occupancy_256(decode);
   }
 }
-
-// Host-side description of a batch: descriptors, chunk count, and the
-// streams that neighbouring blocks share words of (zeroed before launch).
-struct Prepared {
-  std::vector<gzfp::BatchDesc> descs;
-  uint64_t nchunks = 0;
-  std::vector<std::pair<void*, size_t>> zero;  // encode only
-};
 
 int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
             Prepared& p) {
@@ -83,8 +80,8 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
     if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
       return bfail(GZFP_ERR_ARG, "bits per block out of range");
     const int dims = it.nz ? 3 : it.ny ? 2 : 1;
-    gzfp::BatchDesc& d = p.descs[i];
-    d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+    BatchDesc& d = p.descs[i];
+    d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
     if (d.g.nblocks >= (1ull << 32)) return bfail(GZFP_ERR_ARG, "too many blocks");
     const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
     d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
@@ -92,7 +89,7 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
     if (it.stream_capacity < d.nwords * 8)
       return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
     d.maxbits = it.maxbits;
-    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
+    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? kKindDouble : 0u);
     d.in = decode ? it.stream : it.field;
     d.out = decode ? it.field : it.stream;
     d.first_chunk = p.nchunks;
@@ -102,50 +99,43 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
   return GZFP_OK;
 }
 
-// Device work list of one batch: descriptors, chunk table and the claim
-// counter, plus a pinned host copy of the descriptors.
-struct WorkList {
-  gzfp::BatchDesc* descs = nullptr;
-  gzfp::BatchDesc* host = nullptr;  // pinned
-  size_t desc_cap = 0;
-  uint32_t* chunk_item = nullptr;
-  size_t chunk_cap = 0;
-  unsigned long long* counter = nullptr;
-
-  cudaError_t reserve(size_t ndesc, size_t nchunks) {
-    cudaError_t e = cudaSuccess;
-    if (!counter && (e = cudaMalloc(&counter, sizeof(unsigned long long)))) return e;
-    if (ndesc > desc_cap) {
-      cudaFree(descs);
-      cudaFreeHost(host);
-      descs = nullptr;
-      host = nullptr;
-      desc_cap = 0;
-      if ((e = cudaMalloc(&descs, ndesc * sizeof(gzfp::BatchDesc)))) return e;
-      if ((e = cudaMallocHost(&host, ndesc * sizeof(gzfp::BatchDesc)))) return e;
-      desc_cap = ndesc;
-    }
-    if (nchunks > chunk_cap) {
-      cudaFree(chunk_item);
-      chunk_item = nullptr;
-      chunk_cap = 0;
-      if ((e = cudaMalloc(&chunk_item, nchunks * sizeof(uint32_t)))) return e;
-      chunk_cap = nchunks;
-    }
-    return e;
-  }
-  void release() {
+cudaError_t WorkList::reserve(size_t ndesc, size_t nchunks) {
+  cudaError_t e = cudaSuccess;
+  if (!counter && (e = cudaMalloc(&counter, sizeof(unsigned long long)))) return e;
+  if (!done && (e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming))) return e;
+  if (ndesc > desc_cap) {
     cudaFree(descs);
     cudaFreeHost(host);
-    cudaFree(chunk_item);
-    cudaFree(counter);
     descs = nullptr;
     host = nullptr;
-    chunk_item = nullptr;
-    counter = nullptr;
-    desc_cap = chunk_cap = 0;
+    desc_cap = 0;
+    if ((e = cudaMalloc(&descs, ndesc * sizeof(BatchDesc)))) return e;
+    if ((e = cudaMallocHost(&host, ndesc * sizeof(BatchDesc)))) return e;
+    desc_cap = ndesc;
   }
-};
+  if (nchunks > chunk_cap) {
+    cudaFree(chunk_item);
+    chunk_item = nullptr;
+    chunk_cap = 0;
+    if ((e = cudaMalloc(&chunk_item, nchunks * sizeof(uint32_t)))) return e;
+    chunk_cap = nchunks;
+  }
+  return e;
+}
+
+void WorkList::release() {
+  cudaFree(descs);
+  cudaFreeHost(host);
+  cudaFree(chunk_item);
+  cudaFree(counter);
+  if (done) cudaEventDestroy(done);
+  descs = nullptr;
+  host = nullptr;
+  chunk_item = nullptr;
+  counter = nullptr;
+  done = nullptr;
+  desc_cap = chunk_cap = 0;
+}
 
 // Queue everything one batch needs on stream s: zeroing of shared-word
 // streams, descriptor upload, chunk table, counter reset, persistent kernel.
@@ -153,14 +143,14 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
                     cudaStream_t s) {
   cudaError_t e;
   const int count = (int)p.descs.size();
-  if (count == 0 || p.nchunks == 0) return cudaSuccess;
+  if (count == 0 || p.nchunks == 0) return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
   for (const auto& z : p.zero)
     if ((e = cudaMemsetAsync(z.first, 0, z.second, s))) return e;
-  if ((e = cudaMemcpyAsync(wl.descs, wl.host, count * sizeof(gzfp::BatchDesc),
+  if ((e = cudaMemcpyAsync(wl.descs, wl.host, count * sizeof(BatchDesc),
                            cudaMemcpyHostToDevice, s)))
     return e;
   const dim3 tgrid(64, (unsigned)count);
-  gzfp::batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.nchunks);
+  batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.nchunks);
   if ((e = cudaGetLastError())) return e;
   if ((e = cudaMemsetAsync(wl.counter, 0, sizeof(unsigned long long), s))) return e;
   int dev = 0, sms = 0;
@@ -171,16 +161,31 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
   const bool ahead = cfg.claim_ahead != 0;
   switch (cfg.threads) {
     case 64:
-      return gzfp::launch_batch_64(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
-                                   wl.chunk_item, p.nchunks, wl.counter, s);
+      e = launch_batch_64(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
+                          p.nchunks, wl.counter, s);
+      break;
     case 128:
-      return gzfp::launch_batch_128(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
-                                    wl.chunk_item, p.nchunks, wl.counter, s);
+      e = launch_batch_128(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
+                           p.nchunks, wl.counter, s);
+      break;
     default:
-      return gzfp::launch_batch_256(decode, grid, cfg.blocks_per_thread, ahead, wl.descs,
-                                    wl.chunk_item, p.nchunks, wl.counter, s);
+      e = launch_batch_256(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
+                           p.nchunks, wl.counter, s);
+      break;
   }
+  if (e) return e;
+  return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
 }
+
+}  // namespace bhost
+}  // namespace gzfp
+
+namespace {
+
+using gzfp::bhost::occupancy;
+using gzfp::bhost::Prepared;
+using gzfp::bhost::valid_config;
+using gzfp::bhost::WorkList;
 
 struct DeviceWork {
   std::mutex mu;
@@ -206,10 +211,11 @@ int run_batch(const gzfp_batch_item* items, int count, const gzfp_batch_config* 
   cudaStream_t s = (cudaStream_t)cuda_stream;
   DeviceWork& dw = g_work[dev];
   std::lock_guard<std::mutex> lock(dw.mu);
+  // the work list is this device's only one: wait until the previous batch,
+  // on whatever stream it ran, has finished with it
+  if (dw.wl.done && (e = cudaEventSynchronize(dw.wl.done)))
+    return bcuda(e, "cudaEventSynchronize(previous batch)");
   if ((e = dw.wl.reserve(p.descs.size(), p.nchunks))) return bcuda(e, "batch work list allocation");
-  // the pinned descriptor copy is reused by the next call: wait until the
-  // previous upload from it has finished
-  if ((e = cudaStreamSynchronize(s))) return bcuda(e, "cudaStreamSynchronize");
   memcpy(dw.wl.host, p.descs.data(), p.descs.size() * sizeof(gzfp::BatchDesc));
   if ((e = enqueue(p, dw.wl, decode, cfg, s))) return bcuda(e, "batch launch");
   return GZFP_OK;

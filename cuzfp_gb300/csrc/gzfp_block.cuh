@@ -684,19 +684,20 @@ GZ_HD void planes_to_store(const UInt* u, PS& ps) {
 
 // Inverse of planes_to_store: slots base + kk for kk in (lo, hi] hold planes
 // 32G + kk, the others are zero; OR the slice into the coefficients.
+// The low and high 32 bits of the planes (coefficients 0..31 and 32..63)
+// are transposed one after the other, which keeps 32 words live, not 64.
 template <int G, typename UInt, class PS>
 GZ_HD void store_to_coeffs(const PS& ps, int base, int lo, int hi, UInt* u) {
-  uint32_t t[64];
 #pragma unroll
-  for (int kk = 0; kk < 32; kk++) {
-    const uint64_t x = (kk > lo && kk <= hi) ? ps.get(base + kk) : 0;
-    t[kk] = (uint32_t)x;
-    t[32 + kk] = (uint32_t)(x >> 32);
+  for (int h = 0; h < 2; h++) {
+    uint32_t t[32];
+#pragma unroll
+    for (int kk = 0; kk < 32; kk++)
+      t[kk] = (kk > lo && kk <= hi) ? (uint32_t)(ps.get(base + kk) >> (32 * h)) : 0u;
+    transpose_tiles<32>(t);
+#pragma unroll
+    for (int i = 0; i < 32; i++) u[32 * h + i] |= (UInt)((uint64_t)t[i] << (32 * G));
   }
-  transpose_tiles<32>(t);
-  transpose_tiles<32>(t + 32);
-#pragma unroll
-  for (int i = 0; i < 64; i++) u[i] |= (UInt)((uint64_t)t[i] << (32 * G));
 }
 
 // ------------------------------------------------------------- block codec

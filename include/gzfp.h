@@ -122,8 +122,9 @@ void gzfp_batch_default_config(gzfp_batch_config* cfg);
 const char* gzfp_batch_last_error(void);
 
 /* One batch, built and launched now (cfg may be NULL for the default).  The
-   library's per-device work list is reused by the next call, which waits
-   for this one's upload to finish. */
+   library keeps one work list per device: a call first waits on the host
+   until the previous call's kernel, on whatever stream, has finished with
+   it, then queues its own work and returns. */
 int gzfp_batch_compress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
                         void* cuda_stream);
 int gzfp_batch_decompress(const gzfp_batch_item* items, int count, const gzfp_batch_config* cfg,
@@ -176,6 +177,66 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
 #define GZFP_NOALLOC_MAX_CHUNKS (1u << 19)
 int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompress,
                            const gzfp_batch_config* cfg, void* cuda_stream);
+
+/* ------------------------------------------------------------ serving ---
+   A request server.  Compress and decompress requests of mixed shape,
+   scalar type and rate arrive over time.  A request is admitted once the
+   server's device-memory budget can hold its output.  Admitted requests are
+   coded together by the batched persistent kernel, and up to `max_inflight`
+   batches run on the device at once, each on its own stream: a request
+   that arrives while earlier batches run joins the next batch without
+   waiting for them (continuous batching).  Inputs stay resident in device
+   memory; outputs live in a device arena of `budget_bytes`, allocated once
+   per run, and are released when their batch completes (optionally after
+   a copy to a caller buffer).  No counterpart in cuZFP, whose calls are
+   synchronous and one array at a time (src/cuZFP/cuZFP.cu:174-269). */
+
+#define GZFP_SERVE_COMPRESS 0
+#define GZFP_SERVE_DECOMPRESS 1
+
+typedef struct {
+  int op;                /* GZFP_SERVE_COMPRESS or GZFP_SERVE_DECOMPRESS */
+  int type;              /* GZFP_TYPE_FLOAT or GZFP_TYPE_DOUBLE */
+  unsigned nx, ny, nz;   /* as gzfp_compress */
+  unsigned maxbits;      /* bits per block */
+  const void* input;     /* device: the field (compress) or stream words (decompress) */
+  void* copy_to;         /* device buffer that receives the output, or NULL */
+  double arrival;        /* seconds after the start of the run */
+} gzfp_serve_request;
+
+typedef struct {
+  double admitted;       /* seconds after the start: output memory granted, batch launched */
+  double completed;      /* seconds after the start: the request's batch finished */
+  size_t output_bytes;
+  int batch;             /* index of the batch that ran it (-1 if never run) */
+  int status;            /* GZFP_OK, or GZFP_ERR_CAPACITY for an output larger than the budget */
+} gzfp_serve_result;
+
+typedef struct {
+  size_t budget_bytes;   /* device arena for request outputs */
+  int max_batch;         /* requests per batch (1..65535) */
+  int max_inflight;      /* batches on the device at once (1..8) */
+  gzfp_batch_config compress_cfg;   /* launch shapes (see gzfp_batch_autotune) */
+  gzfp_batch_config decompress_cfg;
+} gzfp_serve_config;
+
+typedef struct {
+  double wall;           /* seconds from the start to the last completion */
+  int batches;
+  double mean_batch;     /* requests per batch */
+  size_t peak_bytes;     /* largest arena use */
+  double busy;           /* fraction of the run with at least one batch on the device */
+  int kernels;           /* kernels launched (chunk tables and persistent batch kernels) */
+} gzfp_serve_stats;
+
+void gzfp_serve_default_config(gzfp_serve_config* cfg);
+
+/* Serve `count` requests (any order; each is released at its arrival time
+   on the host clock) and fill results[i] for reqs[i].  Returns after every
+   request has completed.  The calling thread polls; the current device
+   runs everything.  Failure details: gzfp_batch_last_error. */
+int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_config* cfg,
+                   gzfp_serve_result* results, gzfp_serve_stats* stats);
 
 #ifdef __cplusplus
 }

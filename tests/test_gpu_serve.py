@@ -1,0 +1,109 @@
+"""Request server (gzfp_serve_run): every request's output is the same bits
+whether it runs alone (a plain gzfp call) or in the server's mix of
+batches; admission respects the device-memory budget; continuous batching
+actually forms multi-request batches and overlaps them."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(gz, cuda, rng, count, max_edge, gap):
+    """Mixed compress / decompress requests with resident inputs and a
+    copy_to buffer each; returns (requests, expected outputs, copy buffers)."""
+    import torch
+    reqs, expect, outs = [], [], []
+    t = 0.0
+    for i in range(count):
+        dims = int(rng.integers(1, 4))
+        if dims == 1:
+            shape = (int(rng.integers(1, max_edge ** 3)),)
+        elif dims == 2:
+            shape = tuple(int(v) for v in rng.integers(1, max_edge * 5, 2))
+        else:
+            shape = tuple(int(v) for v in rng.integers(1, max_edge, 3))
+        dt = torch.float32 if rng.random() < 0.5 else torch.float64
+        rate = float(rng.choice([4, 8, 12.5, 16, 32]))
+        x = torch.from_numpy(np.cumsum(rng.standard_normal(int(np.prod(shape))))
+                             .reshape(shape)).to(dt).to(cuda)
+        w = gz.compress_tensor(x, rate)  # alone
+        t += float(rng.exponential(gap))
+        if rng.random() < 0.5:
+            out = torch.full_like(w, -1)
+            reqs.append(gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, rate, t, copy_to=out))
+            expect.append(w)
+        else:
+            y = gz.decompress_tensor(w, shape, dt, rate)  # alone
+            out = torch.full_like(y, float("nan"))
+            reqs.append(gz.serve_request(gz.GZFP_SERVE_DECOMPRESS, w, rate, t, shape=shape,
+                                         dtype=dt, copy_to=out))
+            expect.append(y)
+        outs.append(out)
+    torch.cuda.synchronize()
+    return reqs, expect, outs
+
+
+def _same(a, b):
+    import torch
+    if a.dtype == torch.float64:
+        return torch.equal(a.view(torch.int64), b.view(torch.int64))
+    if a.dtype == torch.float32:
+        return torch.equal(a.view(torch.int32), b.view(torch.int32))
+    return torch.equal(a, b)
+
+
+def test_serve_alone_equals_mix(gz, cuda):
+    import torch
+    rng = np.random.default_rng(101)
+    reqs, expect, outs = _requests(gz, cuda, rng, 240, 48, 20e-6)
+    cfg = gz.default_serve_config()
+    cfg.budget_bytes = 1 << 30
+    cfg.max_inflight = 3
+    res, stats = gz.serve(reqs, cfg)
+    torch.cuda.synchronize()
+    for i, (r, e, o) in enumerate(zip(res, expect, outs)):
+        assert r.status == 0, i
+        assert r.completed >= r.admitted >= reqs[i].arrival - 1e-9, i
+        assert _same(e, o), (i, reqs[i].op, reqs[i].nx, reqs[i].ny, reqs[i].nz, reqs[i].maxbits)
+    assert stats.batches < len(reqs) and stats.mean_batch > 1.0  # requests shared batches
+    assert 0 < stats.peak_bytes <= cfg.budget_bytes
+
+
+def test_serve_budget_and_fifo(gz, cuda):
+    """A budget far below the offered outputs: requests wait for memory,
+    results stay identical, the arena never exceeds the budget, and a request
+    that can never fit is refused without stalling the rest."""
+    import torch
+    rng = np.random.default_rng(102)
+    reqs, expect, outs = _requests(gz, cuda, rng, 120, 40, 0.0)  # all at once
+    big = torch.zeros((160, 160, 160), dtype=torch.float64, device=cuda)  # 32 MiB output
+    reqs.insert(60, gz.serve_request(gz.GZFP_SERVE_COMPRESS, big, 64.0, 0.0))
+    cfg = gz.default_serve_config()
+    cfg.budget_bytes = 2 << 20
+    cfg.max_batch = 8
+    cfg.max_inflight = 2
+    res, stats = gz.serve(reqs, cfg)
+    torch.cuda.synchronize()
+    assert res[60].status == gz.GZFP_ERR_CAPACITY
+    rest = [r for i, r in enumerate(res) if i != 60]
+    assert all(r.status == 0 for r in rest)
+    for e, o in zip(expect, outs):
+        assert _same(e, o)
+    assert stats.peak_bytes <= cfg.budget_bytes
+    assert stats.batches >= len(rest) / cfg.max_batch
+    # FIFO: admission times follow arrival order (all arrivals are equal here,
+    # so request order)
+    adm = [r.admitted for r in rest]
+    assert all(a <= b for a, b in zip(adm, adm[1:]))
+
+
+def test_serve_bad_config(gz, cuda):
+    import torch
+    x = torch.zeros((8, 8, 8), dtype=torch.float32, device=cuda)
+    req = gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, 8.0, 0.0)
+    cfg = gz.default_serve_config()
+    cfg.max_inflight = 0
+    with pytest.raises(gz.GzfpError):
+        gz.serve([req], cfg)
