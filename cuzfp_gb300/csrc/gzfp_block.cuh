@@ -366,14 +366,12 @@ GZ_HD void encode_plane(uint64_t x, uint32_t& n, uint32_t& bits, W& w) {
   }
 }
 
-// General one-plane decoder, matching decode_ints bit for bit including
-// its rule that a run cut off by the budget still deposits a one at the
-// current position (Z/src/template/decode.c:94-98).
+// Group tests of one plane, from the reader's position (the first test bit)
+// on, with x holding the plane's verbatim bits: the bit-serial loop of
+// decode_ints (Z/src/template/decode.c:88-99), including its rule that a
+// run cut off by the budget still deposits a one at the current position.
 template <int BS, class R>
-GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
-  uint32_t m = n < bits ? n : bits;
-  uint64_t x = r.read(m);
-  bits -= m;
+GZ_HD uint64_t decode_group(uint64_t x, uint32_t& n, uint32_t& bits, R& r) {
   while (n < (uint32_t)BS && bits) {
     uint64_t w = r.peek64();
     bits--;
@@ -399,6 +397,15 @@ GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
   return x;
 }
 
+// General one-plane decoder: the verbatim bits, then the group tests.
+template <int BS, class R>
+GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
+  uint32_t m = n < bits ? n : bits;
+  uint64_t x = r.read(m);
+  bits -= m;
+  return decode_group<BS>(x, n, bits, r);
+}
+
 // Rank spread of the ones of z: the one of rank j moves from bit q to bit
 // q + j.  Closed form for up to three ones, a loop beyond.
 GZ_HD uint64_t rank_spread(uint64_t z) {
@@ -418,11 +425,13 @@ GZ_HD uint64_t rank_spread(uint64_t z) {
 }
 
 // Code planes k, k-1, ... down to k_low while budget remains; plane(k)
-// yields plane k.  Returns the index of the next plane.  The loop body has
-// no data-dependent branch except the rare general path (a one implied by
-// the last position, or a code longer than 64 bits), so the 32 threads of
-// a warp (32 blocks) stay converged plane after plane.  A budget that ends
-// inside a plane's code just truncates it, as the bit-serial coder does.
+// yields plane k.  Returns the index of the next plane.  A plane's code is
+// written as two pieces -- its n verbatim bits, then its group tests (at
+// most 64 bits) -- so the loop body has no data-dependent branch except the
+// rare general path (a one implied by the last position, or group tests
+// longer than 64 bits), and the 32 threads of a warp (32 blocks) stay
+// converged plane after plane.  A budget that ends inside a plane just
+// truncates its code, as the bit-serial coder does.
 template <int BS, class W, class PlaneFn>
 GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, PlaneFn&& plane) {
   for (; k >= k_low && bits; k--) {
@@ -434,41 +443,53 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
     const uint32_t hb = 63 - clz64(xh | 1);         // top one, relative to the frontier
     const uint32_t m = (uint32_t)popcount64(xh);
     const uint32_t top = n + hb;
-    const uint32_t glen = top + m + 2;              // code length when any
-    if (any && (top >= (uint32_t)BS - 1 || glen > 64)) {
+    if (any && (top >= (uint32_t)BS - 1 || hb + m > 62)) {
       encode_plane<BS>(x, n, bits, w);
       continue;
     }
     const uint64_t S = rank_spread(xh);
     const uint64_t grp = any ? (1 | (S << 1) | ((S - (1ull << ((hb + m - 1) & 63))) << 2)) : 0;
-    uint64_t code = full ? x : (x & ((1ull << sh) - 1)) | (grp << sh);
-    uint32_t len = full ? (uint32_t)BS : any ? glen : n + 1;
+    const uint32_t hlen = full ? (uint32_t)BS : n;
+    const uint64_t head = full ? x : x & ((1ull << sh) - 1);
+    const uint32_t glen = full ? 0 : any ? hb + m + 2 : 1;
     n = any ? top + 1 : n;
-    const bool cut = len > bits;  // the budget ends inside this plane's code
-    code = cut ? code & ((1ull << (bits & 63)) - 1) : code;
-    len = cut ? bits : len;
-    w.put(code, len);
-    bits -= len;
+    uint32_t l = hlen < bits ? hlen : bits;
+    w.put(head & lowmask64(l), l);
+    bits -= l;
+    l = glen < bits ? glen : bits;
+    w.put(grp & lowmask64(l), l);
+    bits -= l;
   }
   return k;
 }
 
 // Decode planes k, ... down to k_low while budget remains, handing each to
-// store(k, x).  Returns the index of the next plane.  A plane is decoded
-// from one 64-bit window when its code lies inside the window and the
-// budget and no one is implied by the last position; otherwise (the last
-// plane of a block, and rarely others) the general routine re-reads it.
+// store(k, x).  Returns the index of the next plane.  The verbatim bits are
+// read first; the group tests are then decoded from a fresh 64-bit window
+// when they lie inside it and the budget, with no one implied by the last
+// position.  Otherwise (the plane the budget ends in, and rarely others)
+// the general routine decodes the group tests.
 template <int BS, class R, class StoreFn>
 GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
   for (; k >= k_low && bits; k--) {
-    const uint64_t w = r.peek64();
     const bool full = n == (uint32_t)BS;
-    const uint32_t sh = full ? 0 : n;
-    const uint64_t head = full ? w & lowmask64(BS) : w & ((1ull << sh) - 1);
-    const bool test = !full && ((w >> sh) & 1);
-    uint64_t g = (w >> sh) >> 1, x = head;
-    uint32_t used = full ? (uint32_t)BS : n + 1, pos = n;
-    bool ok = used <= bits;
+    const uint32_t hlen = full ? (uint32_t)BS : n;
+    if (hlen > bits) {  // the budget ends inside the verbatim bits
+      store(k, decode_plane<BS>(n, bits, r));
+      continue;
+    }
+    uint64_t x = r.peek64() & lowmask64(hlen);
+    r.skip(hlen);
+    bits -= hlen;
+    if (full || !bits) {
+      store(k, x);
+      continue;
+    }
+    const uint64_t w = r.peek64();
+    const bool test = w & 1;
+    uint64_t g = w >> 1;
+    uint32_t used = 1, pos = n;
+    bool ok = true;
     bool more = test;
     while (more && ok) {  // runs once per one of the plane
       const uint32_t t = ctz64(g);
@@ -487,7 +508,7 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
       n = test ? pos : n;
       store(k, x);
     } else {
-      store(k, decode_plane<BS>(n, bits, r));  // nothing consumed yet: start over
+      store(k, decode_group<BS>(x, n, bits, r));  // group tests not consumed yet
     }
   }
   return k;

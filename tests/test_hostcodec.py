@@ -65,3 +65,19 @@ def test_golden(hostcodec, orc):
         assert np.array_equal(hc_compress(hostcodec, orc, a, c["rate"]), c["stream"]), c["name"]
         h = hc_decompress(hostcodec, orc, c["stream"], a.shape, a.dtype, c["rate"])
         assert np.array_equal(h.view(np.uint8), c["output"].view(np.uint8)), c["name"]
+
+
+def test_full_planes_on_noise(hostcodec, orc):
+    """White noise makes every coefficient significant within a few planes,
+    so blocks code many 64-bit verbatim planes, some starting exactly on a
+    word boundary of the stream."""
+    rng = np.random.default_rng(5)
+    for shape, dt in (((40, 40, 40), np.float64), ((36, 44, 40), np.float32),
+                      ((200, 204), np.float64), ((40000,), np.float64)):
+        a = rng.standard_normal(shape).astype(dt)
+        for rate in (24, 32, 41.5, 64):
+            s = orc.compress(a, rate)
+            assert np.array_equal(hc_compress(hostcodec, orc, a, rate), s), (shape, dt, rate)
+            d = orc.decompress(s, a.shape, a.dtype, rate)
+            h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
+            assert np.array_equal(d.view(np.uint8), h.view(np.uint8)), (shape, dt, rate)
