@@ -113,8 +113,11 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
     encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps, c);
 }
 
-template <int D, typename T, bool STAGED>
-__global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
+// MINB: resident CTAs per SM the register budget is sized for.  The decoder
+// is latency-bound on its plane chain, so a fourth CTA is worth a tighter
+// register budget whenever shared memory allows one (dec_min_blocks).
+template <int D, typename T, bool STAGED, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
     decode_kernel(const uint64_t* __restrict__ in, uint64_t nwords, Geom g, uint32_t maxbits,
                   T* __restrict__ out, Ctx c) {
   extern __shared__ uint64_t smem[];
@@ -152,6 +155,10 @@ cudaError_t launch_encode_t(const T* in, const Geom& g, uint32_t maxbits, uint64
   return cudaGetLastError();
 }
 
+// Shared memory of a staged decode CTA that still lets 4 CTAs share an SM
+// (228 KB per SM, 1 KB reserved per CTA).
+constexpr size_t kSmemFor4 = 56 * 1024;
+
 template <int D, typename T>
 cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, uint32_t maxbits,
                             T* out, cudaStream_t s) {
@@ -160,7 +167,10 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
   const Ctx c{1u, 0xffffffffu};
   const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords;
   const size_t sm = smem_bytes(32, staged, maxbits >> 6);
-  auto k = staged ? decode_kernel<D, T, true> : decode_kernel<D, T, false>;
+  constexpr int MB = MinBlocks<D, T>::value;
+  auto k = !staged ? decode_kernel<D, T, false, MB>
+           : (MB < 4 && sm <= kSmemFor4) ? decode_kernel<D, T, true, 4>
+                                         : decode_kernel<D, T, true, MB>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   k<<<grid, kThreads, sm, s>>>(in, nwords, g, maxbits, out, c);
