@@ -16,8 +16,11 @@ codec, which cuZFP's test driver treats as ground truth):
   in zfp_structs.h:64-69); the two agree for every integer 3D rate.
 * Partial edge blocks are padded by zfp's pad_block rule.
 * Errors raise ``GzfpError`` instead of being printed.
-* Strided fields (non-zero sx/sy/sz), which cuZFP silently ignores, and
-  integer fields are rejected with ``GzfpError``.
+* Strided fields (non-zero sx/sy/sz), which cuZFP silently ignores, are
+  rejected with ``GzfpError``.
+* Integer fields (int32 / int64) are coded as zfp 0.5.0's integer block
+  codec does (no exponent, whole budget); a rate that gives 0 bits per
+  block is rejected.
 """
 from __future__ import annotations
 
@@ -275,6 +278,10 @@ def _type_of(dtype) -> zfp_type:
         return zfp_type.float
     if name.endswith("float64"):
         return zfp_type.double
+    if name.endswith("int32") and not name.endswith("uint32"):
+        return zfp_type.int32
+    if name.endswith("int64") and not name.endswith("uint64"):
+        return zfp_type.int64
     raise GzfpError(GZFP_ERR_UNSUPPORTED, f"dtype {name}")
 
 

@@ -32,7 +32,19 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 constexpr unsigned kMaxBitsLimit = 1u << 20;
 
-int ebits_of(int type) { return type == GZFP_TYPE_FLOAT ? 8 : 11; }
+bool known_type(int type) {
+  return type == GZFP_TYPE_FLOAT || type == GZFP_TYPE_DOUBLE || type == GZFP_TYPE_INT32 ||
+         type == GZFP_TYPE_INT64;
+}
+
+// exponent bits of a block header: none for integer fields
+int ebits_of(int type) {
+  return type == GZFP_TYPE_FLOAT ? 8 : type == GZFP_TYPE_DOUBLE ? 11 : 0;
+}
+
+size_t scalar_size(int type) {
+  return type == GZFP_TYPE_FLOAT || type == GZFP_TYPE_INT32 ? 4 : 8;
+}
 
 // Field geometry; ny = 0 selects 1D, nz = 0 selects 2D (zfp_field_1d/2d/3d).
 bool make_geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
@@ -43,9 +55,9 @@ bool make_geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) 
 }
 
 // Rows of full blocks move as one vector when every row start is aligned:
-// 16 bytes for float, 32 for double.
+// 16 bytes for 4-byte values, 32 for 8-byte values.
 uint32_t rows_vectorizable(const void* p, unsigned nx, int type) {
-  const uintptr_t a = type == GZFP_TYPE_FLOAT ? 16 : 32;
+  const uintptr_t a = 4 * scalar_size(type);
   return (nx % 4 == 0 && (uintptr_t)p % a == 0) ? 1u : 0u;
 }
 
@@ -168,10 +180,7 @@ Slab slab_at(const Slabs& p, uint64_t j) {
 
 int check_common(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
                  gzfp::Geom& g, int& dims) {
-  if (type == GZFP_TYPE_INT32 || type == GZFP_TYPE_INT64)
-    return fail(GZFP_ERR_UNSUPPORTED, "integer fields are not supported by this path");
-  if (type != GZFP_TYPE_FLOAT && type != GZFP_TYPE_DOUBLE)
-    return fail(GZFP_ERR_ARG, "unknown scalar type");
+  if (!known_type(type)) return fail(GZFP_ERR_ARG, "unknown scalar type");
   if (!make_geom(nx, ny, nz, g, dims))
     return fail(GZFP_ERR_ARG, "bad dimensions (nx must be > 0; nz > 0 needs ny > 0; under 2^32 blocks)");
   if (maxbits < (unsigned)ebits_of(type) + 1 || maxbits > kMaxBitsLimit)
@@ -203,27 +212,27 @@ const char* gzfp_status_string(int status) {
 const char* gzfp_last_error(void) { return g_last_error; }
 
 unsigned gzfp_rate_to_maxbits(int type, unsigned dims, double rate) {
-  if ((type != GZFP_TYPE_FLOAT && type != GZFP_TYPE_DOUBLE) || dims < 1 || dims > 3) return 0;
+  if (!known_type(type) || dims < 1 || dims > 3) return 0;
   if (!(rate >= 0) || rate > 1e6) return 0;
   unsigned n = 1u << (2 * dims);
   unsigned bits = (unsigned)floor(n * rate + 0.5);
-  unsigned lo = 1u + (unsigned)ebits_of(type);
+  // zfp raises float and double blocks to 1 + exponent bits and leaves
+  // integer blocks alone (Z/src/zfp.c:409-419); 0 bits is not a stream
+  unsigned lo = ebits_of(type) ? 1u + (unsigned)ebits_of(type) : 0u;
   return bits < lo ? lo : bits;
 }
 
 size_t gzfp_stream_size(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits) {
   gzfp::Geom g;
   int dims;
-  if ((type != GZFP_TYPE_FLOAT && type != GZFP_TYPE_DOUBLE) || !make_geom(nx, ny, nz, g, dims))
-    return 0;
+  if (!known_type(type) || !make_geom(nx, ny, nz, g, dims)) return 0;
   return (size_t)(stream_words(g, maxbits) * 8);
 }
 
 size_t gzfp_maximum_size(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits) {
   gzfp::Geom g;
   int dims;
-  if ((type != GZFP_TYPE_FLOAT && type != GZFP_TYPE_DOUBLE) || !make_geom(nx, ny, nz, g, dims))
-    return 0;
+  if (!known_type(type) || !make_geom(nx, ny, nz, g, dims)) return 0;
   // zfp_stream_maximum_size: min(maxbits, bits of a block coded in full),
   // raised to minbits -- which equals maxbits in fixed-rate mode -- plus the
   // 148 header bits, rounded up to a 64-bit word
@@ -238,16 +247,30 @@ namespace {
 
 cudaError_t encode_launch(int type, int dims, const void* in, const gzfp::Geom& g,
                           unsigned maxbits, uint64_t* out, uint64_t nwords, cudaStream_t s) {
-  if (type == GZFP_TYPE_FLOAT)
-    return gzfp::launch_encode_f32(dims, (const float*)in, g, maxbits, out, nwords, s);
-  return gzfp::launch_encode_f64(dims, (const double*)in, g, maxbits, out, nwords, s);
+  switch (type) {
+    case GZFP_TYPE_FLOAT:
+      return gzfp::launch_encode_f32(dims, (const float*)in, g, maxbits, out, nwords, s);
+    case GZFP_TYPE_DOUBLE:
+      return gzfp::launch_encode_f64(dims, (const double*)in, g, maxbits, out, nwords, s);
+    case GZFP_TYPE_INT32:
+      return gzfp::launch_encode_i32(dims, (const int32_t*)in, g, maxbits, out, nwords, s);
+    default:
+      return gzfp::launch_encode_i64(dims, (const int64_t*)in, g, maxbits, out, nwords, s);
+  }
 }
 
 cudaError_t decode_launch(int type, int dims, const uint64_t* in, uint64_t nwords,
                           const gzfp::Geom& g, unsigned maxbits, void* out, cudaStream_t s) {
-  if (type == GZFP_TYPE_FLOAT)
-    return gzfp::launch_decode_f32(dims, in, nwords, g, maxbits, (float*)out, s);
-  return gzfp::launch_decode_f64(dims, in, nwords, g, maxbits, (double*)out, s);
+  switch (type) {
+    case GZFP_TYPE_FLOAT:
+      return gzfp::launch_decode_f32(dims, in, nwords, g, maxbits, (float*)out, s);
+    case GZFP_TYPE_DOUBLE:
+      return gzfp::launch_decode_f64(dims, in, nwords, g, maxbits, (double*)out, s);
+    case GZFP_TYPE_INT32:
+      return gzfp::launch_decode_i32(dims, in, nwords, g, maxbits, (int32_t*)out, s);
+    default:
+      return gzfp::launch_decode_i64(dims, in, nwords, g, maxbits, (int64_t*)out, s);
+  }
 }
 
 // One host-staged call: slabs through the workspace's slots (see Slabs).
@@ -255,7 +278,7 @@ cudaError_t decode_launch(int type, int dims, const uint64_t* in, uint64_t nword
 // which of them are device memory.  Returns after the last slab has landed.
 int staged(bool decode, int type, int dims, const gzfp::Geom& g, unsigned maxbits, void* field,
            bool dev_field, uint64_t* words, bool dev_words, cudaStream_t s) {
-  const size_t scalar = type == GZFP_TYPE_FLOAT ? sizeof(float) : sizeof(double);
+  const size_t scalar = scalar_size(type);
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -393,8 +416,6 @@ int gzfp_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate, 
   gzfp::Geom g;
   int dims;
   if (!make_geom(nx, ny, nz, g, dims)) return fail(GZFP_ERR_ARG, "bad dimensions");
-  if (type == GZFP_TYPE_INT32 || type == GZFP_TYPE_INT64)
-    return fail(GZFP_ERR_UNSUPPORTED, "integer fields are not supported by this path");
   unsigned maxbits = gzfp_rate_to_maxbits(type, (unsigned)dims, rate);
   if (!maxbits) return fail(GZFP_ERR_ARG, "bad type or rate");
   return gzfp_compress_bits(type, nx, ny, nz, maxbits, data, stream, capacity, out_bytes,
@@ -407,8 +428,6 @@ int gzfp_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate
   gzfp::Geom g;
   int dims;
   if (!make_geom(nx, ny, nz, g, dims)) return fail(GZFP_ERR_ARG, "bad dimensions");
-  if (type == GZFP_TYPE_INT32 || type == GZFP_TYPE_INT64)
-    return fail(GZFP_ERR_UNSUPPORTED, "integer fields are not supported by this path");
   unsigned maxbits = gzfp_rate_to_maxbits(type, (unsigned)dims, rate);
   if (!maxbits) return fail(GZFP_ERR_ARG, "bad type or rate");
   return gzfp_decompress_bits(type, nx, ny, nz, maxbits, stream, bytes, data, cuda_stream);

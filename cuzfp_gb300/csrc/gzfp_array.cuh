@@ -128,6 +128,12 @@ GZ_HD void store_row(double* p, const uint64_t* r) {
 #endif
 }
 
+// Integer fields move exactly like the floating-point type of the same size.
+GZ_HD void load_row(const int32_t* p, uint32_t* r) { load_row((const float*)p, r); }
+GZ_HD void load_row(const int64_t* p, uint64_t* r) { load_row((const double*)p, r); }
+GZ_HD void store_row(int32_t* p, const uint32_t* r) { store_row((float*)p, r); }
+GZ_HD void store_row(int64_t* p, const uint64_t* r) { store_row((double*)p, r); }
+
 // Gather block (ix, iy, iz) as raw IEEE bits, padded at partial edges.
 template <int D, typename T>
 GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,

@@ -81,6 +81,7 @@ template <>
 struct FT<float> {
   typedef uint32_t UInt;
   typedef int32_t Int;
+  static constexpr bool INT = false;  // integer field: no exponent, no cast
   static constexpr int P = 32;       // integer precision
   static constexpr int EBITS = 8;    // exponent bits (Z/src/traitsf.h)
   static constexpr int EBIAS = 127;  // (1 << (EBITS - 1)) - 1
@@ -93,11 +94,34 @@ template <>
 struct FT<double> {
   typedef uint64_t UInt;
   typedef int64_t Int;
+  static constexpr bool INT = false;
   static constexpr int P = 64;
   static constexpr int EBITS = 11;  // Z/src/traitsd.h
   static constexpr int EBIAS = 1023;
   static constexpr int MANT = 52;
   static constexpr int EMAXF = 1023;
+  static constexpr uint64_t NB = 0xaaaaaaaaaaaaaaaaull;
+};
+
+// Integer fields (zfp_type_int32 / int64): the values are the block's
+// integers; zfp codes them with no exponent and no cast, over the whole
+// budget, with maxprec 64 so every plane is eligible
+// (Z/src/template/encode.c:154-185, decode.c:107-135).
+template <>
+struct FT<int32_t> {
+  typedef uint32_t UInt;
+  typedef int32_t Int;
+  static constexpr bool INT = true;
+  static constexpr int P = 32;
+  static constexpr uint32_t NB = 0xaaaaaaaau;
+};
+
+template <>
+struct FT<int64_t> {
+  typedef uint64_t UInt;
+  typedef int64_t Int;
+  static constexpr bool INT = true;
+  static constexpr int P = 64;
   static constexpr uint64_t NB = 0xaaaaaaaaaaaaaaaaull;
 };
 
@@ -744,6 +768,22 @@ GZ_HD void front_end(const typename FT<T>::UInt* raw, int emax, typename FT<T>::
   for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
 }
 
+// Front end of the encoder for an integer block: transform, order, map.
+template <int D, typename T>
+GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* u,
+                         const Ctx& c) {
+  typedef FT<T> F;
+  typedef typename F::UInt UInt;
+  typedef typename F::Int Int;
+  constexpr int BS = 1 << (2 * D);
+  Int q[BS];
+#pragma unroll
+  for (int i = 0; i < BS; i++) q[i] = (Int)raw[i];
+  fwd_xform<D>(q, c);
+#pragma unroll
+  for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
+}
+
 // Encode one block of raw IEEE bit patterns (gathered and padded) into
 // exactly maxbits bits (Z/src/template/encode.c:154-234).
 //
@@ -759,31 +799,36 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
   constexpr int P = F::P;
   typedef Planes<D, P> PL;
 
-  // largest exponent field and a nonzero test, from the IEEE bits
-  uint32_t maxh = 0, orl = 0;
-#pragma unroll
-  for (int i = 0; i < BS; i++) {
-    uint32_t h = (uint32_t)((uint64_t)raw[i] >> (P - 32)) & 0x7fffffffu;
-    maxh = h > maxh ? h : maxh;
-    if (P == 64) orl |= (uint32_t)raw[i];
-  }
-  if ((maxh | orl) == 0) {  // all zero: one 0 bit, zero padding
-    w.zeros(maxbits);
-    return;
-  }
-  const int maxE = (int)(maxh >> (F::MANT - (P - 32)));
-  const int emax = maxE - (F::EBIAS - 1);  // frexp exponent, >= 1 - EBIAS
-  int prec = emax - kMinExp + 2 * D + 2;
-  prec = prec < 0 ? 0 : prec > P ? P : prec;
-  const uint32_t e = (uint32_t)(emax + F::EBIAS);
-  w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
-
   UInt u[BS];
-  front_end<D, T>(raw, emax, u, c);
-
-  const uint32_t budget = maxbits - (F::EBITS + 1);
-  uint32_t bits = budget;
-  const int kmin = P - prec;
+  uint32_t bits;
+  int kmin;
+  if constexpr (F::INT) {
+    front_end_int<D, T>(raw, u, c);
+    bits = maxbits;
+    kmin = 0;
+  } else {
+    // largest exponent field and a nonzero test, from the IEEE bits
+    uint32_t maxh = 0, orl = 0;
+#pragma unroll
+    for (int i = 0; i < BS; i++) {
+      uint32_t h = (uint32_t)((uint64_t)raw[i] >> (P - 32)) & 0x7fffffffu;
+      maxh = h > maxh ? h : maxh;
+      if (P == 64) orl |= (uint32_t)raw[i];
+    }
+    if ((maxh | orl) == 0) {  // all zero: one 0 bit, zero padding
+      w.zeros(maxbits);
+      return;
+    }
+    const int maxE = (int)(maxh >> (F::MANT - (P - 32)));
+    const int emax = maxE - (F::EBIAS - 1);  // frexp exponent, >= 1 - EBIAS
+    int prec = emax - kMinExp + 2 * D + 2;
+    prec = prec < 0 ? 0 : prec > P ? P : prec;
+    const uint32_t e = (uint32_t)(emax + F::EBIAS);
+    w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
+    front_end<D, T>(raw, emax, u, c);
+    bits = maxbits - (F::EBITS + 1);
+    kmin = P - prec;
+  }
   uint32_t n = 0;
   int k = P - 1;
   if constexpr (BS == 64 && P == 64) {
@@ -837,18 +882,22 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& p
   constexpr int P = F::P;
   typedef Planes<D, P> PL;
 
-  uint64_t head = r.peek64();
-  if (!(head & 1)) {
+  int emax = 0, kmin = 0;
+  uint32_t bits = maxbits;
+  if constexpr (!F::INT) {
+    const uint64_t head = r.peek64();
+    if (!(head & 1)) {
 #pragma unroll
-    for (int i = 0; i < BS; i++) raw[i] = 0;
-    return;
+      for (int i = 0; i < BS; i++) raw[i] = 0;
+      return;
+    }
+    r.skip(F::EBITS + 1);
+    emax = (int)((head >> 1) & ((1u << F::EBITS) - 1)) - F::EBIAS;
+    int prec = emax - kMinExp + 2 * D + 2;
+    prec = prec < 0 ? 0 : prec > P ? P : prec;
+    kmin = P - prec;
+    bits = maxbits - (F::EBITS + 1);
   }
-  r.skip(F::EBITS + 1);
-  const int emax = (int)((head >> 1) & ((1u << F::EBITS) - 1)) - F::EBIAS;
-  int prec = emax - kMinExp + 2 * D + 2;
-  prec = prec < 0 ? 0 : prec > P ? P : prec;
-  const int kmin = P - prec;
-  uint32_t bits = maxbits - (F::EBITS + 1);
 
   uint32_t n = 0;
   int k = P - 1;
@@ -894,7 +943,12 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& p
 #pragma unroll
   for (int i = 0; i < BS; i++) q[Perm<D>::at(i)] = (Int)((u[i] ^ (UInt)F::NB) - (UInt)F::NB);
   inv_xform<D>(q, c);
-  dequantize(q, raw, BS, emax);
+  if constexpr (F::INT) {
+#pragma unroll
+    for (int i = 0; i < BS; i++) raw[i] = (UInt)q[i];
+  } else {
+    dequantize(q, raw, BS, emax);
+  }
 }
 
 // Plane store backed by a plain array (host builds and tests).

@@ -18,5 +18,13 @@ cudaError_t launch_decode_f32(int dims, const uint64_t* in, uint64_t nwords, con
                               uint32_t maxbits, float* out, cudaStream_t s);
 cudaError_t launch_decode_f64(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
                               uint32_t maxbits, double* out, cudaStream_t s);
+cudaError_t launch_encode_i32(int dims, const int32_t* in, const Geom& g, uint32_t maxbits,
+                              uint64_t* out, uint64_t nwords, cudaStream_t s);
+cudaError_t launch_encode_i64(int dims, const int64_t* in, const Geom& g, uint32_t maxbits,
+                              uint64_t* out, uint64_t nwords, cudaStream_t s);
+cudaError_t launch_decode_i32(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
+                              uint32_t maxbits, int32_t* out, cudaStream_t s);
+cudaError_t launch_decode_i64(int dims, const uint64_t* in, uint64_t nwords, const Geom& g,
+                              uint32_t maxbits, int64_t* out, cudaStream_t s);
 
 }  // namespace gzfp

@@ -50,10 +50,11 @@ const char* gzfp_status_string(int status);
 const char* gzfp_last_error(void);
 
 /* Bits per block for `rate` bits per value on a `dims`-dimensional field:
-   floor(4^dims * rate + 0.5), at least 1 + exponent bits.  Replaces
-   stream_set_rate (src/cuZFP/zfp_structs.h:46-76), computed as zfp 0.5.0's
+   floor(4^dims * rate + 0.5), raised to 1 + exponent bits for float and
+   double (integer blocks carry no exponent).  Replaces stream_set_rate
+   (src/cuZFP/zfp_structs.h:46-76), computed as zfp 0.5.0's
    zfp_stream_set_rate with wra = 0 (zfp-0.5.0/src/zfp.c:405-430).  Returns 0
-   for an unsupported type or dims outside 1..3. */
+   for an unknown type, dims outside 1..3, or an integer rate of 0 bits. */
 unsigned gzfp_rate_to_maxbits(int type, unsigned dims, double rate);
 
 /* Exact size in bytes of the compressed stream: ceil(blocks * maxbits / 64)
@@ -81,7 +82,14 @@ int gzfp_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate
 /* As gzfp_compress / gzfp_decompress, with the block size given directly in
    bits (zfp_stream.maxbits), as cuZFP's internal::encode / internal::decode
    take it (src/cuZFP/cuZFP.cu:26-105).  Any maxbits >= 1 + exponent bits
-   (9 for float, 12 for double) up to 1<<20 is accepted. */
+   (9 for float, 12 for double, 1 for int32 and int64) up to 1<<20 is
+   accepted.
+
+   Integer fields (GZFP_TYPE_INT32 / INT64, cuZFP.cu:196-205) are coded as
+   zfp 0.5.0's integer block codec codes them (zfp_encode_block_int32_<d>,
+   zfp-0.5.0/src/template/encode.c:154-185): no exponent, the whole budget,
+   all planes eligible.  zfp has no partial integer block API; partial edge
+   blocks use its pad rule, as for floating point. */
 int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
                        const void* data, void* stream, size_t capacity, size_t* out_bytes,
                        void* cuda_stream);

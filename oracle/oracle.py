@@ -23,7 +23,7 @@ REF_LIB = os.path.join(HERE, "_ref", "libzfpref.so")
 FIELDS_LIB = os.path.join(HERE, "_ref", "libzfpfields.so")
 REF_TREE = os.environ.get("GZFP_REFERENCE_ROOT", "/root/reference")
 
-FLOAT, DOUBLE = 3, 4
+INT32, INT64, FLOAT, DOUBLE = 1, 2, 3, 4  # zfp_type (Z/inc/zfp.h:107-113)
 
 _A = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_double]
 
@@ -83,6 +83,11 @@ def ref() -> ctypes.CDLL:
         lib.zref_maximum_size.argtypes = _A
         lib.zref_set_rate_bits.restype = ctypes.c_uint
         lib.zref_set_rate_bits.argtypes = [ctypes.c_int, ctypes.c_uint, ctypes.c_double]
+        lib.zref_compress_int.restype = ctypes.c_size_t
+        lib.zref_compress_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        lib.zref_decompress_int.restype = ctypes.c_int
+        lib.zref_decompress_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t,
+                                                 ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -93,7 +98,15 @@ def type_code(dtype) -> int:
         return FLOAT
     if dt == np.float64:
         return DOUBLE
+    if dt == np.int32:
+        return INT32
+    if dt == np.int64:
+        return INT64
     raise ValueError(f"unsupported dtype {dt}")
+
+
+def is_int(dtype) -> bool:
+    return np.dtype(dtype) in (np.dtype(np.int32), np.dtype(np.int64))
 
 
 def dims3(shape) -> tuple[int, int, int]:
@@ -131,10 +144,19 @@ def decompress(words: np.ndarray, shape, dtype, rate: float, nthreads: int = 1) 
 
 
 def ref_compress(a: np.ndarray, rate: float) -> np.ndarray:
-    """Stream produced by the reference's own zfp 0.5.0 build."""
+    """Stream produced by the reference's own zfp 0.5.0 build (integer
+    arrays: its per-block integer API, whole blocks only)."""
     a = np.ascontiguousarray(a)
     nx, ny, nz = dims3(a.shape)
     t = type_code(a.dtype)
+    if is_int(a.dtype):
+        n = stream_bytes(a.shape, a.dtype, rate)
+        buf = np.zeros(max(n // 8, 1), np.uint64)
+        got = ref().zref_compress_int(t, nx, ny, nz, float(rate), a.ctypes.data,
+                                      buf.ctypes.data, buf.nbytes)
+        if got != n:
+            raise RuntimeError("reference integer compress failed (sizes must be multiples of 4)")
+        return buf[: n // 8]
     cap = int(ref().zref_maximum_size(t, nx, ny, nz, float(rate)))
     buf = np.zeros(cap // 8 + 1, np.uint64)
     n = ref().zref_compress(t, nx, ny, nz, float(rate), a.ctypes.data, buf.ctypes.data, cap)
@@ -145,6 +167,11 @@ def ref_decompress(words: np.ndarray, shape, dtype, rate: float) -> np.ndarray:
     words = np.ascontiguousarray(words, dtype=np.uint64)
     out = np.zeros(tuple(shape), dtype)
     nx, ny, nz = dims3(shape)
+    if is_int(dtype):
+        if not ref().zref_decompress_int(type_code(dtype), nx, ny, nz, float(rate),
+                                         words.ctypes.data, words.nbytes, out.ctypes.data):
+            raise RuntimeError("reference integer decompress failed")
+        return out
     ref().zref_decompress(type_code(dtype), nx, ny, nz, float(rate), words.ctypes.data,
                           words.nbytes, out.ctypes.data)
     return out

@@ -67,3 +67,100 @@ unsigned zref_set_rate_bits(int type, unsigned dims, double rate) {
   zfp_stream_close(zfp);
   return b;
 }
+
+/* Integer arrays.  zfp 0.5.0's zfp_compress takes float and double fields
+ * only (Z/src/zfp.c:618-624); its integer codec is the per-block API
+ * zfp_encode_block_int32_<d> / zfp_encode_block_int64_<d> and the matching
+ * decoders (Z/inc/zfp.h:452-521), with the rate set by zfp_stream_set_rate
+ * as for floating point.  These drive that API over a contiguous array whose
+ * sizes are multiples of 4, block by block in zfp_compress's order (x
+ * fastest, then y, then z; Z/src/template/compress.c), and flush the stream
+ * to a 64-bit word as zfp_compress does (Z/src/zfp.c:627-629). */
+static void int_block_io(int type, int dims, unsigned nx, unsigned ny, unsigned nz,
+                         unsigned bx, unsigned by, unsigned bz, void* data, void* blk,
+                         int to_block) {
+  const size_t es = type == zfp_type_int32 ? 4 : 8;
+  unsigned x, y, z;
+  unsigned dz = dims == 3 ? 4 : 1, dy = dims >= 2 ? 4 : 1;
+  for (z = 0; z < dz; z++)
+    for (y = 0; y < dy; y++)
+      for (x = 0; x < 4; x++) {
+        size_t idx = (4 * bx + x) + (size_t)nx * ((4 * by + y) + (size_t)ny * (4 * bz + z));
+        char* a = (char*)data + idx * es;
+        char* b = (char*)blk + (x + 4 * y + 16 * z) * es;
+        size_t i;
+        for (i = 0; i < es; i++) {
+          if (to_block) b[i] = a[i];
+          else a[i] = b[i];
+        }
+      }
+}
+
+static void int_block_codec(zfp_stream* zfp, int type, int dims, void* blk, int encode) {
+  if (type == zfp_type_int32) {
+    int32* b = (int32*)blk;
+    if (encode) {
+      if (dims == 1) zfp_encode_block_int32_1(zfp, b);
+      else if (dims == 2) zfp_encode_block_int32_2(zfp, b);
+      else zfp_encode_block_int32_3(zfp, b);
+    } else {
+      if (dims == 1) zfp_decode_block_int32_1(zfp, b);
+      else if (dims == 2) zfp_decode_block_int32_2(zfp, b);
+      else zfp_decode_block_int32_3(zfp, b);
+    }
+  } else {
+    int64* b = (int64*)blk;
+    if (encode) {
+      if (dims == 1) zfp_encode_block_int64_1(zfp, b);
+      else if (dims == 2) zfp_encode_block_int64_2(zfp, b);
+      else zfp_encode_block_int64_3(zfp, b);
+    } else {
+      if (dims == 1) zfp_decode_block_int64_1(zfp, b);
+      else if (dims == 2) zfp_decode_block_int64_2(zfp, b);
+      else zfp_decode_block_int64_3(zfp, b);
+    }
+  }
+}
+
+static size_t int_array(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                        void* data, void* buffer, size_t capacity, int encode) {
+  const int dims = nz ? 3 : ny ? 2 : 1;
+  const unsigned NY = ny ? ny : 1, NZ = nz ? nz : 1;
+  if ((type != zfp_type_int32 && type != zfp_type_int64) || nx % 4 ||
+      (dims >= 2 && NY % 4) || (dims == 3 && NZ % 4))
+    return 0;
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_rate(zfp, rate, (zfp_type)type, (uint)dims, 0);
+  const size_t blocks = (size_t)(nx / 4) * (dims >= 2 ? NY / 4 : 1) * (dims == 3 ? NZ / 4 : 1);
+  const size_t bytes = (blocks * zfp->maxbits + 63) / 64 * 8;
+  if (bytes > capacity) {
+    zfp_stream_close(zfp);
+    return 0;
+  }
+  bitstream* s = stream_open(buffer, capacity);
+  zfp_stream_set_bit_stream(zfp, s);
+  zfp_stream_rewind(zfp);
+  int64 blk[64];
+  unsigned bx, by, bz;
+  for (bz = 0; bz < (dims == 3 ? NZ / 4 : 1); bz++)
+    for (by = 0; by < (dims >= 2 ? NY / 4 : 1); by++)
+      for (bx = 0; bx < nx / 4; bx++) {
+        if (encode) int_block_io(type, dims, nx, NY, NZ, bx, by, bz, data, blk, 1);
+        int_block_codec(zfp, type, dims, blk, encode);
+        if (!encode) int_block_io(type, dims, nx, NY, NZ, bx, by, bz, data, blk, 0);
+      }
+  if (encode) stream_flush(s);
+  stream_close(s);
+  zfp_stream_close(zfp);
+  return bytes;
+}
+
+size_t zref_compress_int(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                         const void* data, void* buffer, size_t capacity) {
+  return int_array(type, nx, ny, nz, rate, (void*)data, buffer, capacity, 1);
+}
+
+int zref_decompress_int(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                        const void* buffer, size_t bytes, void* out) {
+  return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0) != 0;
+}

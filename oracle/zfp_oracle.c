@@ -25,6 +25,14 @@
  *                                   Z/src/template/decompress.c
  *   bit stream (LSB-first u64)      Z/src/inline/bitstream.c:195-373
  *   stream_flush / returned size    Z/src/zfp.c:603-630
+ *   int32 / int64 blocks            Z/src/template/encode.c:154-185 (no
+ *                                   exponent, whole budget, maxprec 64),
+ *                                   decode.c:116-135; zfp 0.5.0 codes them
+ *                                   one block at a time
+ *                                   (zfp_encode_block_int32_<d>), so arrays
+ *                                   use the same block order and, for
+ *                                   partial blocks, the same pad rule as
+ *                                   the float path
  *
  * Parity is pinned two ways (see tests/test_oracle.py): against a build of
  * the reference's own zfp sources (oracle/_ref, built by oracle/Makefile in
@@ -50,8 +58,11 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define GZO_FLOAT 3  /* zfp_type_float  (Z/inc/zfp.h:107-113) */
+#define GZO_INT32 1  /* zfp_type_int32  (Z/inc/zfp.h:107-113) */
+#define GZO_INT64 2  /* zfp_type_int64 */
+#define GZO_FLOAT 3  /* zfp_type_float */
 #define GZO_DOUBLE 4 /* zfp_type_double */
+#define GZO_IS_INT(t) ((t) == GZO_INT32 || (t) == GZO_INT64)
 #define GZO_MIN_EXP (-1074)
 
 /* ---------------------------------------------------------------- bits --- */
@@ -218,15 +229,17 @@ typedef struct {
   int ebias;  /* 127 or 1023 */
 } params;
 
+/* zfp_stream_set_rate, wra = 0 (Z/src/zfp.c:405-430): floor(4^d rate + 0.5)
+   bits per block, raised to 1 + EBITS for float and double only */
 unsigned gzo_maxbits(int type, int dims, double rate) {
   unsigned n = 1u << (2 * dims);
   unsigned bits = (unsigned)floor(n * rate + 0.5);
-  unsigned lo = type == GZO_FLOAT ? 9u : 12u;
+  unsigned lo = type == GZO_FLOAT ? 9u : type == GZO_DOUBLE ? 12u : 0u;
   return bits < lo ? lo : bits;
 }
 
 static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
-  if (type != GZO_FLOAT && type != GZO_DOUBLE) return 0;
+  if (type != GZO_FLOAT && type != GZO_DOUBLE && !GZO_IS_INT(type)) return 0;
   if (nx == 0) return 0;
   p->dims = nz ? 3 : ny ? 2 : 1;
   if (nz && !ny) return 0;
@@ -234,11 +247,15 @@ static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, dou
   p->nx = nx; p->ny = ny ? ny : 1; p->nz = nz ? nz : 1;
   p->bx = (p->nx + 3) / 4; p->by = (p->ny + 3) / 4; p->bz = (p->nz + 3) / 4;
   p->maxbits = gzo_maxbits(type, p->dims, rate);
-  p->P = type == GZO_FLOAT ? 32 : 64;
-  p->ebits = type == GZO_FLOAT ? 8 : 11;
-  p->ebias = (1 << (p->ebits - 1)) - 1;
+  if (p->maxbits == 0) return 0;
+  p->P = type == GZO_FLOAT || type == GZO_INT32 ? 32 : 64;
+  /* integer blocks carry no exponent (Z/src/template/encode.c:176-185) */
+  p->ebits = type == GZO_FLOAT ? 8 : type == GZO_DOUBLE ? 11 : 0;
+  p->ebias = p->ebits ? (1 << (p->ebits - 1)) - 1 : 0;
   return 1;
 }
+
+static size_t scalar_bytes(const params* p) { return p->P == 32 ? 4 : 8; }
 
 size_t gzo_stream_bytes(int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
   params p;
@@ -299,9 +316,39 @@ static unsigned encode_planes(wbits* w, unsigned budget, int intprec, int kmin,
   return budget - bits;
 }
 
+/* integer block: decorrelating transform, order, embedded coding of the
+   whole budget with maxprec 64 (kmin 0), zero padding to maxbits
+   (encode_block for Int, Z/src/template/encode.c:154-171, called by
+   zfp_encode_block_int32_<d> / int64, :176-185) */
+static void encode_int_block(wbits* w, const params* p, const void* iblock) {
+  int size = 1 << (2 * p->dims);
+  int i;
+  uint64_t u[64];
+  const unsigned char* perm = perm_for(p->dims);
+  if (p->P == 32) {
+    int32_t q[64];
+    memcpy(q, iblock, (size_t)size * 4);
+    xform(q, p->dims, 0, 0);
+    for (i = 0; i < size; i++)
+      u[i] = (uint32_t)(((uint32_t)q[perm[i]] + 0xaaaaaaaau) ^ 0xaaaaaaaau);
+  } else {
+    int64_t q[64];
+    memcpy(q, iblock, (size_t)size * 8);
+    xform(q, p->dims, 1, 0);
+    for (i = 0; i < size; i++)
+      u[i] = ((uint64_t)q[perm[i]] + 0xaaaaaaaaaaaaaaaaull) ^ 0xaaaaaaaaaaaaaaaaull;
+  }
+  unsigned used = encode_planes(w, p->maxbits, p->P, 0, u, size);
+  w_zeros(w, p->maxbits - used);
+}
+
 static void encode_block(wbits* w, const params* p, const void* fblock) {
   int size = 1 << (2 * p->dims);
   int i;
+  if (GZO_IS_INT(p->type)) {
+    encode_int_block(w, p, fblock);
+    return;
+  }
   /* largest magnitude -> common exponent (frexp convention) */
   int emax;
   if (p->type == GZO_FLOAT) {
@@ -373,8 +420,8 @@ static void gather(const params* p, const void* data, unsigned bx, unsigned by, 
         size_t gz = p->dims == 3 ? 4 * bz + padmap(cz, z) : 0;
         size_t idx = gx + p->nx * (gy + (size_t)p->ny * gz);
         unsigned o = x + 4 * y + 16 * z;
-        if (p->type == GZO_FLOAT) ((float*)blk)[o] = ((const float*)data)[idx];
-        else ((double*)blk)[o] = ((const double*)data)[idx];
+        const size_t es = scalar_bytes(p);  /* memcpy: any scalar type, no aliasing */
+        memcpy((char*)blk + o * es, (const char*)data + idx * es, es);
       }
 }
 
@@ -406,9 +453,37 @@ static void decode_planes(rbits* r, unsigned budget, int intprec, int kmin, uint
   }
 }
 
+/* inverse of encode_int_block (zfp_decode_block_int32_<d> / int64) */
+static void decode_int_block(rbits* r, const params* p, void* iblock) {
+  int size = 1 << (2 * p->dims);
+  int i;
+  size_t start = r->bit;
+  uint64_t u[64];
+  decode_planes(r, p->maxbits, p->P, 0, u, size);
+  r->bit = start + p->maxbits;
+  const unsigned char* perm = perm_for(p->dims);
+  if (p->P == 32) {
+    int32_t q[64];
+    for (i = 0; i < size; i++)
+      q[perm[i]] = (int32_t)(((uint32_t)u[i] ^ 0xaaaaaaaau) - 0xaaaaaaaau);
+    xform(q, p->dims, 0, 1);
+    memcpy(iblock, q, (size_t)size * 4);
+  } else {
+    int64_t q[64];
+    for (i = 0; i < size; i++)
+      q[perm[i]] = (int64_t)((u[i] ^ 0xaaaaaaaaaaaaaaaaull) - 0xaaaaaaaaaaaaaaaaull);
+    xform(q, p->dims, 1, 1);
+    memcpy(iblock, q, (size_t)size * 8);
+  }
+}
+
 static void decode_block(rbits* r, const params* p, void* fblock) {
   int size = 1 << (2 * p->dims);
   int i;
+  if (GZO_IS_INT(p->type)) {
+    decode_int_block(r, p, fblock);
+    return;
+  }
   size_t start = r->bit;
   if (!r_get(r, 1)) {
     if (p->type == GZO_FLOAT) for (i = 0; i < size; i++) ((float*)fblock)[i] = 0;
@@ -454,8 +529,8 @@ static void scatter(const params* p, void* data, unsigned bx, unsigned by, unsig
       for (x = 0; x < cx; x++) {
         size_t idx = (4 * bx + x) + p->nx * ((4 * by + y) + (size_t)p->ny * (4 * bz + z));
         unsigned o = x + 4 * y + 16 * z;
-        if (p->type == GZO_FLOAT) ((float*)data)[idx] = ((const float*)blk)[o];
-        else ((double*)data)[idx] = ((const double*)blk)[o];
+        const size_t es = scalar_bytes(p);
+        memcpy((char*)data + idx * es, (const char*)blk + o * es, es);
       }
 }
 

@@ -80,3 +80,35 @@ def has_saturating_blocks(a: np.ndarray) -> bool:
     m = m.reshape(shp)
     m = m.max(axis=tuple(range(1, 2 * a.ndim, 2)))
     return bool(np.any((m > 0) & (m < lim)))
+
+
+def int_case(rng, max_edge=(300, 40, 14), whole_blocks=False, wide=False):
+    """A random int32 / int64 array and rate: smooth walks and white noise,
+    with magnitudes inside zfp's integer range (|v| < 2^(P-2)) unless
+    `wide`, which draws from the whole type range (the codec wraps)."""
+    dims = int(rng.integers(1, 4))
+    if whole_blocks:
+        shape = tuple(4 * int(rng.integers(1, max(2, max_edge[dims - 1] // 4))) for _ in range(dims))
+    else:
+        shape = tuple(int(rng.integers(1, max_edge[dims - 1] + 1)) for _ in range(dims))
+    dt = np.int32 if rng.random() < 0.5 else np.int64
+    bits = 32 if dt == np.int32 else 64
+    n = int(np.prod(shape))
+    kind = rng.integers(0, 3)
+    if wide:
+        info = np.iinfo(dt)
+        a = rng.integers(info.min, info.max, n, dtype=dt, endpoint=True)
+    elif kind == 0:  # white noise at a random scale
+        lim = 1 << int(rng.integers(1, bits - 2))
+        a = rng.integers(-lim, lim, n, dtype=np.int64)
+    elif kind == 1:  # random walk
+        step = 1 << int(rng.integers(0, bits // 2))
+        a = np.cumsum(rng.integers(-step, step + 1, n, dtype=np.int64))
+        a = np.clip(a, -(1 << (bits - 3)), (1 << (bits - 3)))
+    else:  # mostly zero with a few spikes
+        a = np.zeros(n, np.int64)
+        idx = rng.integers(0, n, max(1, n // 50))
+        a[idx] = rng.integers(-(1 << (bits - 3)), 1 << (bits - 3), idx.size)
+    a = np.asarray(a).astype(dt).reshape(shape)
+    rate = float(rng.choice([0.5, 1, 2.25, 4, 8, 12.5, 16, 24, 32, 48, 64]))
+    return a, rate

@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures from the reference's own zfp 0.5.0 build.
 
 Run in a checkout that has the reference tree (the build reads its zfp
-sources):  python tests/golden/make_golden.py
-Writes tests/golden/small_cases.npz and tests/golden/manifest.json.
+sources):  python tests/golden/make_golden.py [--ints]
+Writes tests/golden/small_cases.npz, tests/golden/manifest.json and
+tests/golden/int_cases.npz (only the last with --ints).
 """
 from __future__ import annotations
 
@@ -90,5 +91,34 @@ def main() -> None:
     print(f"{len([k for k in arrays if k.endswith('__rate')])} small cases, {len(specs)} manifest cases")
 
 
+def write_int_cases() -> None:
+    """Integer arrays of whole blocks, coded by the reference's per-block
+    integer API (zfp 0.5.0's zfp_compress takes no integer fields), stored in
+    full in tests/golden/int_cases.npz."""
+    if not orc.build_ref():
+        raise SystemExit("reference tree not found; cannot regenerate golden fixtures")
+    rng = np.random.default_rng(20261204)
+    arrays = {}
+    k = 0
+    while k < 24:
+        a, rate = cases.int_case(rng, max_edge=(256, 32, 12), whole_blocks=True)
+        if orc.stream_bytes(a.shape, a.dtype, rate) == 0:
+            continue
+        s = orc.ref_compress(a, rate)
+        d = orc.ref_decompress(s, a.shape, a.dtype, rate)
+        nm = f"int{k:02d}_{a.ndim}d_{a.dtype.name}"
+        arrays[nm + "__input"] = a
+        arrays[nm + "__stream"] = s
+        arrays[nm + "__output"] = d
+        arrays[nm + "__rate"] = np.array(rate)
+        k += 1
+    np.savez_compressed(os.path.join(OUT, "int_cases.npz"), **arrays)
+    print(f"{k} integer cases")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--ints"]:
+        write_int_cases()
+    else:
+        main()
+        write_int_cases()

@@ -45,8 +45,8 @@ def manifest() -> list[dict]:
         return json.load(f)["cases"]
 
 
-def small_cases() -> list[dict]:
-    z = np.load(os.path.join(GOLDEN, "small_cases.npz"))
+def small_cases(fname: str = "small_cases.npz") -> list[dict]:
+    z = np.load(os.path.join(GOLDEN, fname))
     names = sorted({k.rsplit("__", 1)[0] for k in z.files})
     out = []
     for nm in names:
@@ -56,5 +56,6 @@ def small_cases() -> list[dict]:
 
 
 def load_all() -> list[dict]:
-    """Full-array golden cases (the small ones)."""
-    return small_cases()
+    """Full-array golden cases: the small floating-point ones and the
+    integer ones (int_cases.npz)."""
+    return small_cases() + small_cases("int_cases.npz")

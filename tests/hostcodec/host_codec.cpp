@@ -30,11 +30,19 @@ bool geom(unsigned nx, unsigned ny, unsigned nz, gzfp::Geom& g, int& dims) {
   return true;
 }
 
+// types: 1 int32, 2 int64, 3 float, 4 double (zfp_type)
 unsigned maxbits_for(int type, int dims, double rate) {
   unsigned bits = (unsigned)floor((1 << (2 * dims)) * rate + 0.5);
-  unsigned lo = type == 3 ? 9u : 12u;
+  unsigned lo = type == 3 ? 9u : type == 4 ? 12u : 0u;
   return bits < lo ? lo : bits;
 }
+
+template <typename T>
+void enc_t(int dims, const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out,
+           uint64_t words);
+template <typename T>
+void dec_t(int dims, const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbits,
+           void* data);
 
 template <int D, typename T>
 void enc(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out, uint64_t words) {
@@ -54,26 +62,38 @@ void dec(const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbi
     gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w, ps, c);
 }
 
+template <typename T>
+void enc_t(int dims, const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out,
+           uint64_t words) {
+  if (dims == 1) enc<1, T>(data, g, maxbits, out, words);
+  if (dims == 2) enc<2, T>(data, g, maxbits, out, words);
+  if (dims == 3) enc<3, T>(data, g, maxbits, out, words);
+}
+
+template <typename T>
+void dec_t(int dims, const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbits,
+           void* data) {
+  if (dims == 1) dec<1, T>(in, words, g, maxbits, data);
+  if (dims == 2) dec<2, T>(in, words, g, maxbits, data);
+  if (dims == 3) dec<3, T>(in, words, g, maxbits, data);
+}
+
 }  // namespace
 
 extern "C" size_t hc_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
                               const void* data, uint64_t* out, size_t cap) {
   gzfp::Geom g;
   int dims;
-  if (!geom(nx, ny, nz, g, dims) || (type != 3 && type != 4)) return 0;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
   unsigned maxbits = maxbits_for(type, dims, rate);
+  if (!maxbits) return 0;
   uint64_t words = (g.nblocks * maxbits + 63) / 64;
   if (cap < words * 8) return 0;
   memset(out, 0, words * 8);
-  if (type == 3) {
-    if (dims == 1) enc<1, float>(data, g, maxbits, out, words);
-    if (dims == 2) enc<2, float>(data, g, maxbits, out, words);
-    if (dims == 3) enc<3, float>(data, g, maxbits, out, words);
-  } else {
-    if (dims == 1) enc<1, double>(data, g, maxbits, out, words);
-    if (dims == 2) enc<2, double>(data, g, maxbits, out, words);
-    if (dims == 3) enc<3, double>(data, g, maxbits, out, words);
-  }
+  if (type == 1) enc_t<int32_t>(dims, data, g, maxbits, out, words);
+  if (type == 2) enc_t<int64_t>(dims, data, g, maxbits, out, words);
+  if (type == 3) enc_t<float>(dims, data, g, maxbits, out, words);
+  if (type == 4) enc_t<double>(dims, data, g, maxbits, out, words);
   return words * 8;
 }
 
@@ -81,17 +101,13 @@ extern "C" int hc_decompress(int type, unsigned nx, unsigned ny, unsigned nz, do
                              const uint64_t* in, size_t bytes, void* data) {
   gzfp::Geom g;
   int dims;
-  if (!geom(nx, ny, nz, g, dims) || (type != 3 && type != 4)) return 0;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
   unsigned maxbits = maxbits_for(type, dims, rate);
+  if (!maxbits) return 0;
   uint64_t words = bytes / 8;
-  if (type == 3) {
-    if (dims == 1) dec<1, float>(in, words, g, maxbits, data);
-    if (dims == 2) dec<2, float>(in, words, g, maxbits, data);
-    if (dims == 3) dec<3, float>(in, words, g, maxbits, data);
-  } else {
-    if (dims == 1) dec<1, double>(in, words, g, maxbits, data);
-    if (dims == 2) dec<2, double>(in, words, g, maxbits, data);
-    if (dims == 3) dec<3, double>(in, words, g, maxbits, data);
-  }
+  if (type == 1) dec_t<int32_t>(dims, in, words, g, maxbits, data);
+  if (type == 2) dec_t<int64_t>(dims, in, words, g, maxbits, data);
+  if (type == 3) dec_t<float>(dims, in, words, g, maxbits, data);
+  if (type == 4) dec_t<double>(dims, in, words, g, maxbits, data);
   return 1;
 }

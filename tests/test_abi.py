@@ -45,7 +45,7 @@ def test_version_and_status_strings(gz):
 
 
 def test_rate_to_maxbits_matches_reference(gz, ref):
-    for t in (3, 4):
+    for t in (1, 2, 3, 4):
         for dims in (1, 2, 3):
             for rate in (0, 0.1, 0.5, 1, 2, 2.25, 3.3, 4, 7.99, 8, 12, 16, 17.7, 24, 32, 64):
                 assert gz._lib.gzfp_rate_to_maxbits(t, dims, rate) == \
@@ -53,7 +53,7 @@ def test_rate_to_maxbits_matches_reference(gz, ref):
 
 
 def test_maximum_size_matches_reference(gz, ref):
-    for t in (3, 4):
+    for t in (1, 2, 3, 4):
         for shape in ((1,), (17,), (5, 9), (64, 64), (3, 4, 5), (33, 17, 9)):
             nx, ny, nz = ref.dims3(shape)
             for rate in (1, 4, 8, 16, 32, 64, 100):
@@ -79,8 +79,9 @@ def _compress_status(gz, t, nx, ny, nz, rate, data=1, stream=1, cap=1 << 30):
 def test_argument_errors_without_device(gz):
     """Checks that fail before any CUDA call."""
     assert _compress_status(gz, 9, 4, 4, 4, 8.0) == gz.GZFP_ERR_ARG
-    assert _compress_status(gz, 1, 4, 4, 4, 8.0) == gz.GZFP_ERR_UNSUPPORTED
-    assert _compress_status(gz, 2, 4, 4, 4, 8.0) == gz.GZFP_ERR_UNSUPPORTED
+    assert _compress_status(gz, 0, 4, 4, 4, 8.0) == gz.GZFP_ERR_ARG   # zfp_type_none
+    assert _compress_status(gz, 1, 4, 4, 4, 0.0) == gz.GZFP_ERR_ARG   # int32: 0 bits per block
+    assert _compress_status(gz, 2, 4, 4, 4, 0.001) == gz.GZFP_ERR_ARG  # int64: rounds to 0 bits
     assert _compress_status(gz, 3, 0, 4, 4, 8.0) == gz.GZFP_ERR_ARG
     assert _compress_status(gz, 3, 4, 0, 4, 8.0) == gz.GZFP_ERR_ARG
     assert _compress_status(gz, 3, 4, 4, 4, -1.0) == gz.GZFP_ERR_ARG

@@ -24,7 +24,8 @@ def gpu_compress(gz, a: np.ndarray, rate: float, cuda) -> np.ndarray:
 def gpu_decompress(gz, words: np.ndarray, shape, dtype, rate: float, cuda) -> np.ndarray:
     import torch
     tw = torch.from_numpy(np.ascontiguousarray(words).view(np.int64)).to(cuda)
-    tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+           np.dtype(np.int32): torch.int32, np.dtype(np.int64): torch.int64}[np.dtype(dtype)]
     return gz.decompress_tensor(tw, shape, tdt, rate).cpu().numpy()
 
 
@@ -40,6 +41,40 @@ def test_random_cases(gz, orc, cuda):
         assert np.array_equal(gpu_compress(gz, a, rate, cuda), s), (a.shape, a.dtype, rate)
         assert same_bits(gpu_decompress(gz, s, a.shape, a.dtype, rate, cuda),
                          orc.decompress(s, a.shape, a.dtype, rate)), (a.shape, a.dtype, rate)
+
+
+def test_integer_fields(gz, orc, cuda):
+    """int32 / int64 fields (cuZFP's integer path): every dimensionality,
+    ragged shapes, whole-range values, against the oracle."""
+    rng = np.random.default_rng(4343)
+    for i in range(200):
+        a, rate = cases.int_case(rng, wide=(i % 8 == 7))
+        if orc.stream_bytes(a.shape, a.dtype, rate) == 0:
+            continue
+        s = orc.compress(a, rate)
+        assert np.array_equal(gpu_compress(gz, a, rate, cuda), s), (a.shape, a.dtype, rate)
+        assert same_bits(gpu_decompress(gz, s, a.shape, a.dtype, rate, cuda),
+                         orc.decompress(s, a.shape, a.dtype, rate)), (a.shape, a.dtype, rate)
+
+
+def test_integer_host_buffers(gz, orc):
+    """Host integer arrays through cuZFP's pointer rules and the Python
+    mirror of its structs."""
+    rng = np.random.default_rng(4444)
+    for dt, rate in ((np.int32, 32.0), (np.int64, 64.0)):
+        a = rng.integers(-1000, 1000, (37, 41, 23)).astype(dt)
+        t = gz.zfp_type.int32 if dt == np.int32 else gz.zfp_type.int64
+        zfp = gz.zfp_stream()
+        gz.stream_set_rate(zfp, rate, t, 3)
+        buf = np.zeros(gz.zfp_stream_maximum_size(zfp, gz.zfp_field_3d(None, t, 23, 41, 37)) // 8,
+                       np.uint64)
+        zfp.stream = buf
+        n = gz.compress(zfp, gz.zfp_field_3d(a, t, 23, 41, 37))
+        s = orc.compress(a, rate)
+        assert np.array_equal(buf[: n // 8], s)
+        out = np.zeros_like(a)
+        gz.decompress(zfp, gz.zfp_field_3d(out, t, 23, 41, 37))
+        assert np.array_equal(out, orc.decompress(s, a.shape, a.dtype, rate))
 
 
 def test_edge_cases(gz, orc, cuda):
@@ -223,7 +258,9 @@ def test_errors(gz, cuda):
         gz.compress_tensor(x, 16.0, out=small)
     assert e.value.status == gz.GZFP_ERR_CAPACITY
     with pytest.raises(gz.GzfpError):
-        gz.compress_tensor(torch.zeros(4, dtype=torch.int32, device=cuda), 8.0)
+        gz.compress_tensor(torch.zeros(4, dtype=torch.int16, device=cuda), 8.0)
+    with pytest.raises(gz.GzfpError):  # 0 bits per integer block
+        gz.compress_tensor(torch.zeros(4, dtype=torch.int32, device=cuda), 0.0)
     # the context stays usable after rejected calls
     w = gz.compress_tensor(x, 16.0)
     assert int(w.abs().sum()) == 0

@@ -81,3 +81,18 @@ def test_full_planes_on_noise(hostcodec, orc):
             d = orc.decompress(s, a.shape, a.dtype, rate)
             h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
             assert np.array_equal(d.view(np.uint8), h.view(np.uint8)), (shape, dt, rate)
+
+
+def test_integer_fields(hostcodec, orc):
+    """int32 / int64 arrays of every dimensionality, ragged shapes and rates,
+    including values across the whole type range (the lifting wraps)."""
+    rng = np.random.default_rng(23)
+    for i in range(300):
+        a, rate = cases.int_case(rng, wide=(i % 10 == 9))
+        if orc.stream_bytes(a.shape, a.dtype, rate) == 0:
+            continue  # a rate of 0 bits per block is not a stream
+        s = orc.compress(a, rate)
+        assert np.array_equal(hc_compress(hostcodec, orc, a, rate), s), (a.shape, a.dtype, rate)
+        d = orc.decompress(s, a.shape, a.dtype, rate)
+        h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
+        assert np.array_equal(d, h), (a.shape, a.dtype, rate)
