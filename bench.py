@@ -74,6 +74,17 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest of every rank's `value` (the slowest rank's time); the
+    value itself when there is one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -286,10 +297,7 @@ def run_batched(args, rank, world, local):
             b.record(stream)
         b.synchronize()
         ms = a.elapsed_time(b) / steps
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, world, dev)
         return ms
 
     with ClockSampler(local) as clk:
@@ -330,7 +338,8 @@ def run_batched(args, rank, world, local):
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round((2 * nbytes + 2 * sbytes) / (batch_ms * 1e-3) / 1e9 / peak, 4),
                      "traffic": None},
-        "gpu_launches": 2 * args.steps,
+        # per step and direction: the chunk-table kernel and the persistent kernel
+        "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(res), flush=True)
@@ -502,6 +511,15 @@ def main():
         import torch.distributed as dist
         backend = "nccl" if args.impl == "gzfp" else "gloo"
         dist.init_process_group(backend)
+    try:
+        run(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+def run(args, rank, world, local):
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -560,10 +578,7 @@ def main():
     total_ms = t_start.elapsed_time(t_end)
     enc_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
     dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, dev)
     ms_per_step = total_ms / args.steps
     value = 2 * nbytes * world / (ms_per_step * 1e-3) / 1e9
 
@@ -596,10 +611,7 @@ def main():
         b.record(stream)
         b.synchronize()
         e_ms = a.elapsed_time(b) / e_steps
-        if world > 1:
-            t = torch.tensor([e_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e_ms = float(t.item())
+        e_ms = max_over_ranks(e_ms, world, dev)
         e2e = {"value": round(2 * nbytes * world / (e_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
                "ms_per_step": round(e_ms, 3),
                "h2d_bytes_per_step": nbytes + sbytes, "d2h_bytes_per_step": sbytes + nbytes}
