@@ -30,13 +30,14 @@ import bench
 rank, world, _ = bench.dist_env()
 dist.init_process_group("gloo")
 got = bench.max_over_ranks(1.5 + rank, world, "cpu")
-print(json.dumps({"rank": rank, "max": got}), flush=True)
+with open(os.path.join(os.environ["OUT_DIR"], f"rank{rank}.json"), "w") as f:
+    json.dump({"rank": rank, "max": got}, f)
 dist.destroy_process_group()
 """
 
 
-def _launch(args, timeout=240):
-    env = dict(os.environ, BENCH_ROOT=ROOT, OMP_NUM_THREADS="1")
+def _launch(args, timeout=240, out_dir=""):
+    env = dict(os.environ, BENCH_ROOT=ROOT, OMP_NUM_THREADS="1", OUT_DIR=str(out_dir))
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port())] + args
     return subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=timeout)
@@ -45,10 +46,10 @@ def _launch(args, timeout=240):
 def test_max_over_ranks_gloo(tmp_path):
     worker = tmp_path / "worker.py"
     worker.write_text(_WORKER)
-    p = _launch([str(worker)])
+    p = _launch([str(worker)], out_dir=tmp_path)
     assert p.returncode == 0, p.stderr[-2000:]
-    lines = [json.loads(l) for l in p.stdout.splitlines() if l.startswith("{")]
-    assert sorted(l["rank"] for l in lines) == [0, 1]
+    lines = [json.loads((tmp_path / f"rank{r}.json").read_text()) for r in (0, 1)]
+    assert [l["rank"] for l in lines] == [0, 1]
     assert all(l["max"] == 2.5 for l in lines)  # both ranks see the slower one
 
 
