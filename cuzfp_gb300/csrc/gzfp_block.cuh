@@ -431,19 +431,17 @@ GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
 }
 
 // Rank spread of the ones of z: the one of rank j moves from bit q to bit
-// q + j.  Closed form for up to three ones, a loop beyond.
+// q + j.  With z_i = z without its i lowest ones, the spread is
+// z + z_1 + 2 z_2 + 4 z_3 + ... (the one of rank j is counted once in z and
+// 2^(i-1) times for each i = 1..j, 2^j times in all), so up to three ones
+// cost two clears and three adds; more ones loop.
 GZ_HD uint64_t rank_spread(uint64_t z) {
-  const uint64_t l0 = z & (0 - z);
-  const uint64_t z1 = z ^ l0;
-  const uint64_t l1 = z1 & (0 - z1);
-  uint64_t z2 = z1 ^ l1;
-  const uint64_t l2 = z2 & (0 - z2);
-  uint64_t S = l0 | (l1 << 1) | (l2 << 2);
-  z2 ^= l2;
-  for (uint32_t j = 3; z2; j++) {
-    const uint64_t low = z2 & (0 - z2);
-    S |= low << j;
-    z2 ^= low;
+  const uint64_t z1 = z & (z - 1);
+  uint64_t z2 = z1 & (z1 - 1);
+  uint64_t S = z + z1 + (z2 << 1);
+  for (uint32_t j = 2; z2; j++) {
+    z2 &= z2 - 1;
+    S += z2 << j;
   }
   return S;
 }
@@ -458,16 +456,19 @@ GZ_HD uint64_t rank_spread(uint64_t z) {
 // truncates its code, as the bit-serial coder does.
 template <int BS, class W, class PlaneFn>
 GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, PlaneFn&& plane) {
+  // The frontier after a plane is max(n, bit length of the plane), so the
+  // chain from one plane to the next is a single max; the rest of a plane's
+  // code depends on n but not on the previous plane's code.
   for (; k >= k_low && bits; k--) {
     const uint64_t x = plane(k);
+    const uint32_t bl = 64 - clz64(x);              // bit length of the plane
     const bool full = n == (uint32_t)BS;            // all significant: plane verbatim
+    const bool any = bl > n;                        // a one above the frontier
     const uint32_t sh = full ? 0 : n;
     const uint64_t xh = full ? 0 : x >> sh;         // ones above the frontier
-    const bool any = xh != 0;
-    const uint32_t hb = 63 - clz64(xh | 1);         // top one, relative to the frontier
+    const uint32_t hb = bl - 1 - n;                 // top one, relative to the frontier
     const uint32_t m = (uint32_t)popcount64(xh);
-    const uint32_t top = n + hb;
-    if (any && (top >= (uint32_t)BS - 1 || hb + m > 62)) {
+    if (any && (bl >= (uint32_t)BS || hb + m > 62)) {
       encode_plane<BS>(x, n, bits, w);
       continue;
     }
@@ -476,7 +477,7 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
     const uint32_t hlen = full ? (uint32_t)BS : n;
     const uint64_t head = full ? x : x & ((1ull << sh) - 1);
     const uint32_t glen = full ? 0 : any ? hb + m + 2 : 1;
-    n = any ? top + 1 : n;
+    n = any ? bl : n;
     uint32_t l = hlen < bits ? hlen : bits;
     w.put(head & lowmask64(l), l);
     bits -= l;
