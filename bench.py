@@ -338,8 +338,9 @@ def run_batched(args, rank, world, local):
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round((2 * nbytes + 2 * sbytes) / (batch_ms * 1e-3) / 1e9 / peak, 4),
                      "traffic": None},
-        # per step and direction: the chunk-table kernel and the persistent kernel
-        "gpu_launches": 4 * args.steps,
+        # per step and direction: the chunk-table kernel and one persistent
+        # kernel per kind (all arrays are 3D: one kind per scalar type)
+        "gpu_launches": 2 * (1 + len({dt for _, dt, _, _ in specs})) * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(res), flush=True)

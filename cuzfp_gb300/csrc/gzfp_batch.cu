@@ -55,12 +55,11 @@ bool valid_config(const gzfp_batch_config& c) {
                                  c.blocks_per_thread == 4);
 }
 
-int occupancy(int threads, bool decode) {
-  switch (threads) {
-    case 64: return batch_occupancy_64(decode);
-    case 128: return batch_occupancy_128(decode);
-    default: return batch_occupancy_256(decode);
-  }
+int occupancy(int threads, bool decode, uint32_t staged_w) {
+  // the largest over the kinds: a shape's CTAs per SM are capped per kind
+  int best = 0;
+  for (int k = 0; k < kBatchKinds; k++) best = std::max(best, batch_occupancy(threads, decode, k, staged_w));
+  return best;
 }
 
 int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
@@ -69,7 +68,9 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
   const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
   p.descs.resize(count);
   p.nchunks = 0;
+  p.staged_w = 0;
   p.zero.clear();
+  std::vector<int> kind_of(count);
   for (int i = 0; i < count; i++) {
     const gzfp_batch_item& it = items[i];
     if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
@@ -80,28 +81,43 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
     if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
       return bfail(GZFP_ERR_ARG, "bits per block out of range");
     const int dims = it.nz ? 3 : it.ny ? 2 : 1;
-    BatchDesc& d = p.descs[i];
-    d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-    if (d.g.nblocks >= (1ull << 32)) return bfail(GZFP_ERR_ARG, "too many blocks");
-    const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
-    d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
-    d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
-    if (it.stream_capacity < d.nwords * 8)
+    const Geom g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+    if (g.nblocks >= (1ull << 32)) return bfail(GZFP_ERR_ARG, "too many blocks");
+    const uint64_t nwords = (g.nblocks * it.maxbits + 63) / 64;
+    if (it.stream_capacity < nwords * 8)
       return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
-    d.maxbits = it.maxbits;
-    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? kKindDouble : 0u);
-    d.in = decode ? it.stream : it.field;
-    d.out = decode ? it.field : it.stream;
-    d.first_chunk = p.nchunks;
-    p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
-    if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
+    kind_of[i] = batch_kind_index((uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? kKindDouble : 0u));
+  }
+  // descriptors grouped by kind, so each kind's chunks form one range
+  int slot = 0;
+  for (int k = 0; k < kBatchKinds; k++) {
+    p.kind_lo[k] = p.nchunks;
+    for (int i = 0; i < count; i++) {
+      if (kind_of[i] != k) continue;
+      const gzfp_batch_item& it = items[i];
+      BatchDesc& d = p.descs[slot++];
+      d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+      const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
+      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+      d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
+      d.maxbits = it.maxbits;
+      d.kind = kBatchKind[k];
+      d.in = decode ? it.stream : it.field;
+      d.out = decode ? it.field : it.stream;
+      d.first_chunk = p.nchunks;
+      p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+      if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
+      if (decode && it.maxbits % 64 == 0 && it.maxbits / 64 <= kBatchMaxStagedWords)
+        p.staged_w = std::max(p.staged_w, it.maxbits / 64);
+    }
+    p.kind_hi[k] = p.nchunks;
   }
   return GZFP_OK;
 }
 
 cudaError_t WorkList::reserve(size_t ndesc, size_t nchunks) {
   cudaError_t e = cudaSuccess;
-  if (!counter && (e = cudaMalloc(&counter, sizeof(unsigned long long)))) return e;
+  if (!counter && (e = cudaMalloc(&counter, kBatchKinds * sizeof(unsigned long long)))) return e;
   if (!done && (e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming))) return e;
   if (ndesc > desc_cap) {
     cudaFree(descs);
@@ -152,26 +168,19 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
   const dim3 tgrid(64, (unsigned)count);
   batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.nchunks);
   if ((e = cudaGetLastError())) return e;
-  if ((e = cudaMemsetAsync(wl.counter, 0, sizeof(unsigned long long), s))) return e;
+  if ((e = cudaMemsetAsync(wl.counter, 0, kBatchKinds * sizeof(unsigned long long), s))) return e;
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev))) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
-  int per_sm = std::min(cfg.ctas_per_sm, std::max(1, occupancy(cfg.threads, decode)));
-  const int grid = sms * per_sm;
+  const uint32_t sw = decode ? p.staged_w : 0;
   const bool ahead = cfg.claim_ahead != 0;
-  switch (cfg.threads) {
-    case 64:
-      e = launch_batch_64(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
-                          p.nchunks, wl.counter, s);
-      break;
-    case 128:
-      e = launch_batch_128(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
-                           p.nchunks, wl.counter, s);
-      break;
-    default:
-      e = launch_batch_256(decode, grid, cfg.blocks_per_thread, ahead, wl.descs, wl.chunk_item,
-                           p.nchunks, wl.counter, s);
-      break;
+  // one persistent kernel per kind present, in sequence on the stream
+  for (int k = 0; k < kBatchKinds && !e; k++) {
+    if (p.kind_hi[k] == p.kind_lo[k]) continue;
+    const int occ = std::max(1, batch_occupancy(cfg.threads, decode, k, sw));
+    const int grid = sms * std::min(cfg.ctas_per_sm, occ);
+    e = launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, wl.descs,
+                     wl.chunk_item, p.kind_lo[k], p.kind_hi[k], wl.counter + k, s);
   }
   if (e) return e;
   return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
@@ -324,9 +333,14 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
   int st = GZFP_OK;
   const int threads[] = {64, 128, 256};
   const int bpts[] = {1, 2, 4};
+  uint32_t sw = 0;  // the decode staging depth the kernel will use for this batch
+  if (decompress && items)
+    for (int i = 0; i < count; i++)
+      if (items[i].maxbits % 64 == 0 && items[i].maxbits / 64 <= gzfp::kBatchMaxStagedWords)
+        sw = std::max(sw, items[i].maxbits / 64);
   // every candidate is timed as it is meant to run: a graph replay
   for (int nt : threads) {
-    const int occ = std::max(1, occupancy(nt, decompress != 0));
+    const int occ = std::max(1, occupancy(nt, decompress != 0, sw));
     for (int per_sm = 1; per_sm <= occ && !st; per_sm++) {
       for (int bpt : bpts) {
         for (int ahead = 0; ahead < 2 && !st; ahead++) {

@@ -1,13 +1,17 @@
-// gzfp_batch.cuh -- the batched persistent kernel: many arrays of uneven
-// shape, scalar type, dimensionality and rate coded by one launch.
+// gzfp_batch.cuh -- the batched persistent kernels: many arrays of uneven
+// shape, scalar type, dimensionality and rate coded by a few launches.
 //
-// Work list (device memory, built per batch): one descriptor per array and a
-// table mapping every chunk -- NT * BPT consecutive zfp blocks of one array
-// -- to its array.  A grid of resident CTAs claims chunks from a global
-// counter (atomicAdd), optionally one claim ahead so that the claim's
-// latency overlaps the current chunk, and codes each block of the chunk
-// with the plain path's per-thread code.  Every block's bits are the same
-// as a plain launch on that array would produce.
+// Work list (device memory, built per batch): one descriptor per array,
+// grouped by kind (dimensionality x scalar type), and a table mapping every
+// chunk -- NT * BPT consecutive zfp blocks of one array -- to its array.
+// The chunks of one kind form one contiguous range.  Each kind present in
+// the batch gets one persistent kernel specialised for it (so its register
+// budget is the plain kernel's, not the union of all kinds): a grid of
+// resident CTAs claims chunks of its range from the kind's counter
+// (atomicAdd), optionally one claim ahead so that the claim's latency
+// overlaps the current chunk, and codes each block with the plain path's
+// per-thread code.  Every block's bits are the same as a plain launch on
+// that array would produce.
 #pragma once
 
 #include "gzfp_kernels.cuh"
@@ -26,6 +30,14 @@ struct BatchDesc {
 };
 
 constexpr uint32_t kKindDouble = 8;
+constexpr int kBatchKinds = 6;  // 1D/2D/3D x float/double
+constexpr uint32_t kBatchKind[kBatchKinds] = {1, 2, 3, 9, 10, 11};
+
+inline int batch_kind_index(uint32_t kind) {
+  for (int i = 0; i < kBatchKinds; i++)
+    if (kBatchKind[i] == kind) return i;
+  return -1;
+}
 
 template <int NT>
 struct BatchPlanes {
@@ -34,87 +46,161 @@ struct BatchPlanes {
   __device__ __forceinline__ void put(int i, uint64_t v) { p[i * NT] = v; }
 };
 
-template <int NT, bool DECODE>
+// Blocks of whole 64-bit words, up to this many per block, are decoded from
+// a shared-memory copy of the warp's 32 slots made with coalesced loads (as
+// the plain decoder does); others read the stream directly.
+constexpr uint32_t kBatchMaxStagedWords = 32;
+
+template <int NT, bool DECODE, int D, typename T>
 __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, BatchPlanes<NT>& ps,
-                                            const Ctx& c) {
-  if (b >= d.g.nblocks) return;
+                                            uint64_t* sbuf, uint32_t staged_w, const Ctx& c) {
   if (DECODE) {
-    const DevWords words{nullptr, (const uint64_t*)d.in, d.nwords};
-    switch (d.kind) {
-      case 1: decode_one<1, float>((float*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      case 2: decode_one<2, float>((float*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      case 3: decode_one<3, float>((float*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      case 9: decode_one<1, double>((double*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      case 10: decode_one<2, double>((double*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      case 11: decode_one<3, double>((double*)d.out, d.g, b, d.maxbits, words, ps, c); break;
-      default: break;
+    const uint32_t W = d.maxbits >> 6;
+    if (d.maxbits % 64 == 0 && W <= staged_w) {  // the same for the whole warp (one item)
+      const uint32_t lane = threadIdx.x & 31;
+      const uint64_t b0 = b - lane;
+      if (b0 < d.g.nblocks) {
+        const uint64_t left = d.g.nblocks - b0;
+        warp_copy<false, NT + 1>(sbuf + (threadIdx.x & ~31u), (uint64_t*)d.in + b0 * W, W,
+                                 left < 32 ? (uint32_t)left : 32);
+      }
+      __syncwarp();
+      if (b < d.g.nblocks)
+        decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
+                         StagedWords<NT + 1>{sbuf + threadIdx.x, b * W, W}, ps, c);
+      __syncwarp();  // the next chunk's copy reuses the buffer
+      return;
     }
+    if (b >= d.g.nblocks) return;
+    decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
+                     DevWords{nullptr, (const uint64_t*)d.in, d.nwords}, ps, c);
   } else {
-    const DevWords words{(uint64_t*)d.out, nullptr, d.nwords};
-    switch (d.kind) {
-      case 1: encode_one<1, float>((const float*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      case 2: encode_one<2, float>((const float*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      case 3: encode_one<3, float>((const float*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      case 9: encode_one<1, double>((const double*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      case 10: encode_one<2, double>((const double*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      case 11: encode_one<3, double>((const double*)d.in, d.g, b, d.maxbits, words, ps, c); break;
-      default: break;
-    }
+    if (b >= d.g.nblocks) return;
+    encode_one<D, T>((const T*)d.in, d.g, b, d.maxbits,
+                     DevWords{(uint64_t*)d.out, nullptr, d.nwords}, ps, c);
   }
 }
 
-// Persistent batch kernel.  NT threads per CTA, bpt blocks per thread per
-// chunk.  With `ahead` the next chunk is claimed as soon as the current one
-// is known, so the claim's latency overlaps the coding; otherwise after it.
-// `counter` must be zero at launch.
-template <int NT, bool DECODE>
-__global__ void __launch_bounds__(NT, (NT == 64 ? 6 : NT == 128 ? 3 : 1))
+// Resident CTAs per SM each kernel's registers are sized for: the plain
+// kernels' choice at 128 threads, scaled to the CTA size.
+template <int NT, int D, typename T>
+struct BatchMinBlocks {
+  static constexpr int v = MinBlocks<D, T>::value * 128 / NT;
+  static constexpr int value = v < 1 ? 1 : v;
+};
+
+// plane-store slots per thread: as the plain encoder, 32 when decoding
+template <bool DECODE, int D, typename T>
+struct BatchSlots {
+  static constexpr int value = DECODE ? 32 : ((D == 3 && sizeof(T) == 8) ? 64 : 32);
+};
+
+// Persistent kernel for one kind: chunks [lo, hi) of the work list.  NT
+// threads per CTA, bpt blocks per thread per chunk.  `counter` must be zero
+// at launch.  Decoding stages items of up to staged_w words per block in
+// shared memory behind the plane store.
+template <int NT, bool DECODE, int D, typename T>
+__global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
     batch_kernel(const BatchDesc* __restrict__ descs, const uint32_t* __restrict__ chunk_item,
-                 uint64_t nchunks, unsigned long long* counter, int bpt, int ahead, Ctx c) {
+                 uint64_t lo, uint64_t hi, unsigned long long* counter, int bpt, int ahead,
+                 uint32_t staged_w, Ctx c) {
   extern __shared__ uint64_t smem[];
   __shared__ unsigned long long s_claim;
+  __shared__ BatchDesc s_desc;  // the claimed chunk's array, read field by field
   BatchPlanes<NT> ps{smem + threadIdx.x};
-  if (threadIdx.x == 0) s_claim = atomicAdd(counter, 1ull);
+  uint64_t* sbuf = smem + BatchSlots<DECODE, D, T>::value * NT;
+  if (threadIdx.x == 0) s_claim = lo + atomicAdd(counter, 1ull);
   __syncthreads();
   for (;;) {
     const unsigned long long chunk = s_claim;
-    if (chunk >= nchunks) break;
-    const BatchDesc d = descs[chunk_item[chunk]];
-    __syncthreads();  // every thread has read the claim
-    if (ahead && threadIdx.x == 0) s_claim = atomicAdd(counter, 1ull);
+    if (chunk >= hi) break;
+    if (threadIdx.x == 0) s_desc = descs[chunk_item[chunk]];
+    __syncthreads();  // every thread has read the claim and sees the descriptor
+    const BatchDesc& d = s_desc;
+    if (ahead && threadIdx.x == 0) s_claim = lo + atomicAdd(counter, 1ull);
     const uint64_t first = (chunk - d.first_chunk) * (uint64_t)(NT * bpt);
 #pragma unroll 1
-    for (int j = 0; j < bpt; j++) batch_block<NT, DECODE>(d, first + (uint64_t)j * NT + threadIdx.x, ps, c);
-    if (!ahead && threadIdx.x == 0) s_claim = atomicAdd(counter, 1ull);
+    for (int j = 0; j < bpt; j++)
+      batch_block<NT, DECODE, D, T>(d, first + (uint64_t)j * NT + threadIdx.x, ps, sbuf,
+                                    staged_w, c);
+    __syncthreads();  // every thread is done with the descriptor
+    if (!ahead && threadIdx.x == 0) s_claim = lo + atomicAdd(counter, 1ull);
     __syncthreads();  // the next claim is visible
   }
 }
 
-// shared memory of a batch CTA: 64 plane-store slots per thread
-constexpr size_t batch_smem_bytes(int nt) { return (size_t)nt * 64 * 8; }
+// shared memory of a batch CTA of one kind: the plane store, and for
+// decoding the staged word buffer (staged_w words per block at pitch NT + 1)
+template <int NT, bool DECODE, int D, typename T>
+size_t batch_smem_bytes(uint32_t staged_w) {
+  return (size_t)NT * BatchSlots<DECODE, D, T>::value * 8 +
+         (DECODE ? (size_t)staged_w * (NT + 1) * 8 : 0);
+}
 
-template <int NT>
-cudaError_t launch_batch_t(bool decode, int grid, int bpt, bool ahead, const BatchDesc* descs,
-                           const uint32_t* chunk_item, uint64_t nchunks,
-                           unsigned long long* counter, cudaStream_t s) {
+template <int NT, bool DECODE, int D, typename T>
+cudaError_t launch_batch_kind(int grid, int bpt, bool ahead, uint32_t staged_w,
+                              const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,
+                              uint64_t hi, unsigned long long* counter, cudaStream_t s) {
   const Ctx c{1u, 0xffffffffu};
-  const size_t sm = batch_smem_bytes(NT);
-  auto k = decode ? batch_kernel<NT, true> : batch_kernel<NT, false>;
+  const size_t sm = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
+  auto k = batch_kernel<NT, DECODE, D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<grid, NT, sm, s>>>(descs, chunk_item, nchunks, counter, bpt, ahead ? 1 : 0, c);
+  k<<<grid, NT, sm, s>>>(descs, chunk_item, lo, hi, counter, bpt, ahead ? 1 : 0, staged_w, c);
   return cudaGetLastError();
 }
 
-template <int NT>
-int batch_occupancy(bool decode) {
+template <int NT, bool DECODE, int D, typename T>
+int batch_occupancy_kind(uint32_t staged_w) {
   int n = 0;
-  auto k = decode ? batch_kernel<NT, true> : batch_kernel<NT, false>;
-  const size_t sm = batch_smem_bytes(NT);
+  auto k = batch_kernel<NT, DECODE, D, T>;
+  const size_t sm = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, sm) != cudaSuccess) return 0;
   return n;
+}
+
+// Dispatch over the six kinds (kind index into kBatchKind).
+template <int NT, bool DECODE>
+cudaError_t launch_batch_t(int kind_index, int grid, int bpt, bool ahead, uint32_t staged_w,
+                           const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,
+                           uint64_t hi, unsigned long long* counter, cudaStream_t s) {
+  switch (kind_index) {
+    case 0:
+      return launch_batch_kind<NT, DECODE, 1, float>(grid, bpt, ahead, staged_w, descs,
+                                                     chunk_item, lo, hi, counter, s);
+    case 1:
+      return launch_batch_kind<NT, DECODE, 2, float>(grid, bpt, ahead, staged_w, descs,
+                                                     chunk_item, lo, hi, counter, s);
+    case 2:
+      return launch_batch_kind<NT, DECODE, 3, float>(grid, bpt, ahead, staged_w, descs,
+                                                     chunk_item, lo, hi, counter, s);
+    case 3:
+      return launch_batch_kind<NT, DECODE, 1, double>(grid, bpt, ahead, staged_w, descs,
+                                                      chunk_item, lo, hi, counter, s);
+    case 4:
+      return launch_batch_kind<NT, DECODE, 2, double>(grid, bpt, ahead, staged_w, descs,
+                                                      chunk_item, lo, hi, counter, s);
+    case 5:
+      return launch_batch_kind<NT, DECODE, 3, double>(grid, bpt, ahead, staged_w, descs,
+                                                      chunk_item, lo, hi, counter, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+template <int NT, bool DECODE>
+int batch_occupancy_t(int kind_index, uint32_t staged_w) {
+  switch (kind_index) {
+    case 0: return batch_occupancy_kind<NT, DECODE, 1, float>(staged_w);
+    case 1: return batch_occupancy_kind<NT, DECODE, 2, float>(staged_w);
+    case 2: return batch_occupancy_kind<NT, DECODE, 3, float>(staged_w);
+    case 3: return batch_occupancy_kind<NT, DECODE, 1, double>(staged_w);
+    case 4: return batch_occupancy_kind<NT, DECODE, 2, double>(staged_w);
+    case 5: return batch_occupancy_kind<NT, DECODE, 3, double>(staged_w);
+    default: return 0;
+  }
 }
 
 }  // namespace gzfp

@@ -17,8 +17,16 @@ namespace bhost {
 // Host-side description of a batch: descriptors, chunk count, and the
 // streams whose blocks share words (zeroed before an encode launch).
 struct Prepared {
-  std::vector<BatchDesc> descs;
+  std::vector<BatchDesc> descs;  // grouped by kind (kBatchKind order)
   uint64_t nchunks = 0;
+  uint64_t kind_lo[kBatchKinds] = {}, kind_hi[kBatchKinds] = {};  // each kind's chunk range
+  uint32_t staged_w = 0;  // decode: largest words per block staged in shared memory
+  // kernels enqueue launches: the chunk table and one per kind present
+  int kernels() const {
+    int n = nchunks ? 1 : 0;
+    for (int k = 0; k < kBatchKinds; k++) n += kind_hi[k] > kind_lo[k];
+    return n;
+  }
   std::vector<std::pair<void*, size_t>> zero;
 };
 
@@ -29,11 +37,12 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
 
 bool valid_config(const gzfp_batch_config& c);
 
-// Resident CTAs per SM of the batch kernel at `threads` per CTA.
-int occupancy(int threads, bool decode);
+// Resident CTAs per SM of the batch kernels at `threads` per CTA (the
+// largest over the kinds).
+int occupancy(int threads, bool decode, uint32_t staged_w);
 
 // Device work list of one batch in flight: descriptors, chunk table and
-// claim counter, a pinned host copy of the descriptors, and an event
+// one claim counter per kind, a pinned host copy of the descriptors, and an event
 // recorded after the batch's kernel so that the next user of the list can
 // wait for it.
 struct WorkList {

@@ -5,7 +5,7 @@
 // The kernels are the batch path's own (gzfp_batch.cuh); only where their
 // scratch lives differs.  Scratch layout, one copy per device (a __device__
 // array is instantiated in every context that loads the module):
-//   [0, 256)                      claim counter (zeroed before every launch)
+//   [0, 256)                      claim counters, one per kind (zeroed every call)
 //   [256, 256 + descs)            array descriptors, uploaded every call
 //   [.., + 4 * kNoAllocMaxChunks) chunk -> array table, built on the device
 // Nothing here calls cudaMalloc, cudaMallocHost, cudaFree or an allocating
@@ -94,9 +94,9 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   gzfp::BatchDesc* descs = (gzfp::BatchDesc*)(base + kDescOffset);
   uint32_t* chunk_item = (uint32_t*)(base + kTableOffset);
 
-  // descriptors: the same validation and layout as the allocating batch path
+  // descriptors: the same validation and layout as the allocating batch
+  // path -- grouped by kind, so each kind's chunks form one range
   const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
-  uint64_t nchunks = 0;
   for (int i = 0; i < count; i++) {
     const gzfp_batch_item& it = items[i];
     if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
@@ -106,21 +106,37 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
     const unsigned ebits = it.type == GZFP_TYPE_FLOAT ? 8 : 11;
     if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
       return nfail(GZFP_ERR_ARG, "bits per block out of range");
-    const int dims = it.nz ? 3 : it.ny ? 2 : 1;
-    gzfp::BatchDesc& d = g_host[i];
-    d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-    if (d.g.nblocks >= (1ull << 32)) return nfail(GZFP_ERR_ARG, "too many blocks");
-    const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
-    d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
-    d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
-    if (it.stream_capacity < d.nwords * 8)
+    const gzfp::Geom g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+    if (g.nblocks >= (1ull << 32)) return nfail(GZFP_ERR_ARG, "too many blocks");
+    if (it.stream_capacity < (g.nblocks * it.maxbits + 63) / 64 * 8)
       return nfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
-    d.maxbits = it.maxbits;
-    d.kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
-    d.in = decode ? it.stream : it.field;
-    d.out = decode ? it.field : it.stream;
-    d.first_chunk = nchunks;
-    nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+  }
+  uint64_t nchunks = 0;
+  uint64_t lo[gzfp::kBatchKinds], hi[gzfp::kBatchKinds];
+  uint32_t sw = 0;  // decode staging depth, as the allocating path chooses it
+  int slot = 0;
+  for (int k = 0; k < gzfp::kBatchKinds; k++) {
+    lo[k] = nchunks;
+    for (int i = 0; i < count; i++) {
+      const gzfp_batch_item& it = items[i];
+      const int dims = it.nz ? 3 : it.ny ? 2 : 1;
+      const uint32_t kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
+      if (kind != gzfp::kBatchKind[k]) continue;
+      gzfp::BatchDesc& d = g_host[slot++];
+      d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+      const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
+      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+      d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
+      d.maxbits = it.maxbits;
+      d.kind = kind;
+      d.in = decode ? it.stream : it.field;
+      d.out = decode ? it.field : it.stream;
+      d.first_chunk = nchunks;
+      nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+      if (decode && it.maxbits % 64 == 0 && it.maxbits / 64 <= gzfp::kBatchMaxStagedWords)
+        sw = it.maxbits / 64 > sw ? it.maxbits / 64 : sw;
+    }
+    hi[k] = nchunks;
   }
   if (nchunks > kMaxChunks) {
     char msg[160];
@@ -131,11 +147,11 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   }
 
   // streams whose blocks share edge words are assembled with atomic ORs and
-  // must start at zero, as must the claim counter
+  // must start at zero, as must the claim counters
   if (!decode)
     for (int i = 0; i < count; i++)
-      if (items[i].maxbits % 64 &&
-          (e = cudaMemsetAsync(items[i].stream, 0, (size_t)(g_host[i].nwords * 8), s)))
+      if (g_host[i].maxbits % 64 &&
+          (e = cudaMemsetAsync(g_host[i].out, 0, (size_t)(g_host[i].nwords * 8), s)))
         return ncuda(e, "cudaMemsetAsync(stream)");
   if ((e = cudaMemcpyAsync(descs, g_host, count * sizeof(gzfp::BatchDesc), cudaMemcpyHostToDevice,
                            s)))
@@ -143,28 +159,20 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   gzfp::batch_chunk_table<<<dim3(64, (unsigned)count), 256, 0, s>>>(descs, count, chunk_item,
                                                                     nchunks);
   if ((e = cudaGetLastError())) return ncuda(e, "chunk table launch");
-  if ((e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s)))
-    return ncuda(e, "cudaMemsetAsync(counter)");
+  if ((e = cudaMemsetAsync(counter, 0, gzfp::kBatchKinds * sizeof(unsigned long long), s)))
+    return ncuda(e, "cudaMemsetAsync(counters)");
 
   int sms = 0;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
     return ncuda(e, "cudaDeviceGetAttribute");
-  int occ = cfg.threads == 64    ? gzfp::batch_occupancy_64(decode)
-            : cfg.threads == 128 ? gzfp::batch_occupancy_128(decode)
-                                 : gzfp::batch_occupancy_256(decode);
-  const int grid = sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : (occ > 1 ? occ : 1));
   const bool ahead = cfg.claim_ahead != 0;
-  const int bpt = cfg.blocks_per_thread;
-  switch (cfg.threads) {
-    case 64:
-      e = gzfp::launch_batch_64(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
-      break;
-    case 128:
-      e = gzfp::launch_batch_128(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
-      break;
-    default:
-      e = gzfp::launch_batch_256(decode, grid, bpt, ahead, descs, chunk_item, nchunks, counter, s);
-      break;
+  for (int k = 0; k < gzfp::kBatchKinds && !e; k++) {
+    if (hi[k] == lo[k]) continue;
+    int occ = gzfp::batch_occupancy(cfg.threads, decode, k, sw);
+    occ = occ > 1 ? occ : 1;
+    const int grid = sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : occ);
+    e = gzfp::launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, descs,
+                           chunk_item, lo[k], hi[k], counter + k, s);
   }
   return e ? ncuda(e, "batch kernel launch") : GZFP_OK;
 }

@@ -52,22 +52,24 @@ struct DevWords {
 };
 
 // One block's slot in the staged word buffer: word j of the block at
-// buf[j * kStride]; words past the slot read as zero.
+// buf[j * PITCH] (PITCH = threads per CTA + 1, so the 32 lanes of a warp
+// hit 32 different banks); words past the slot read as zero.
+template <int PITCH>
 struct StagedWords {
   uint64_t* buf;
   uint64_t w0;  // global index of the slot's first word
   uint32_t W;   // words per block
-  __device__ __forceinline__ void store(uint64_t i, uint64_t v) { buf[(i - w0) * kStride] = v; }
-  __device__ __forceinline__ void merge(uint64_t i, uint64_t v) { buf[(i - w0) * kStride] |= v; }
+  __device__ __forceinline__ void store(uint64_t i, uint64_t v) { buf[(i - w0) * PITCH] = v; }
+  __device__ __forceinline__ void merge(uint64_t i, uint64_t v) { buf[(i - w0) * PITCH] |= v; }
   __device__ __forceinline__ uint64_t load(uint64_t i) const {
     uint64_t j = i - w0;
-    return j < W ? buf[j * kStride] : 0;
+    return j < W ? buf[j * PITCH] : 0;
   }
 };
 
 // Copy a warp's 32 consecutive slots between the staged buffer (word j of
-// lane t at buf[j * kStride + t]) and the stream, 32 words per step.
-template <bool TO_GLOBAL>
+// lane t at buf[j * PITCH + t]) and the stream, 32 words per step.
+template <bool TO_GLOBAL, int PITCH = kStride>
 __device__ __forceinline__ void warp_copy(uint64_t* buf, uint64_t* gwords, uint32_t W,
                                           uint32_t nblocks_valid) {
   const uint32_t lane = threadIdx.x & 31;
@@ -76,9 +78,9 @@ __device__ __forceinline__ void warp_copy(uint64_t* buf, uint64_t* gwords, uint3
   const uint32_t dt = 32 / W, dj = 32 % W;  // advance per step of 32 elements
   for (uint32_t gi = lane; gi < total; gi += 32) {
     if (TO_GLOBAL)
-      gwords[gi] = buf[j * kStride + t];
+      gwords[gi] = buf[j * PITCH + t];
     else
-      buf[j * kStride + t] = __ldg(gwords + gi);
+      buf[j * PITCH + t] = __ldg(gwords + gi);
     t += dt;
     j += dj;
     if (j >= W) {
@@ -134,7 +136,8 @@ __global__ void __launch_bounds__(kThreads, MINB)
     }
     __syncwarp();
     if (b < g.nblocks)
-      decode_one<D, T>(out, g, b, maxbits, StagedWords{buf + threadIdx.x, b * W, W}, ps, c);
+      decode_one<D, T>(out, g, b, maxbits, StagedWords<kStride>{buf + threadIdx.x, b * W, W}, ps,
+                       c);
   } else {
     if (b < g.nblocks) decode_one<D, T>(out, g, b, maxbits, DevWords{nullptr, in, nwords}, ps, c);
   }

@@ -234,7 +234,7 @@ typedef struct {
   double mean_batch;     /* requests per batch */
   size_t peak_bytes;     /* largest arena use */
   double busy;           /* fraction of the run with at least one batch on the device */
-  int kernels;           /* kernels launched (chunk tables and persistent batch kernels) */
+  int kernels;           /* kernels launched (chunk tables and per-kind persistent kernels) */
 } gzfp_serve_stats;
 
 void gzfp_serve_default_config(gzfp_serve_config* cfg);
