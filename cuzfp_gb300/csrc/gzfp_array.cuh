@@ -288,7 +288,7 @@ struct BitReader {
 
 template <int D, typename T, class Words, class PS>
 GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words,
-                      PS& ps, const Ctx& c) {
+                      PS& ps) {
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   uint32_t ix, iy, iz;
@@ -296,20 +296,19 @@ GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, 
   UInt raw[BS];
   gather<D, T>(in, g, ix, iy, iz, raw);
   BitWriter<Words> w(words, b * (uint64_t)maxbits, maxbits);
-  encode_block<D, T>(raw, maxbits, w, ps, c);
+  encode_block<D, T>(raw, maxbits, w, ps);
   w.finish();
 }
 
 template <int D, typename T, class Words, class PS>
-GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words words, PS& ps,
-                      const Ctx& c) {
+GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words words, PS& ps) {
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   uint32_t ix, iy, iz;
   block_coords(g, b, ix, iy, iz);
   BitReader<Words> r(words, b * (uint64_t)maxbits);
   UInt raw[BS];
-  decode_block<D, T>(r, maxbits, raw, ps, c);
+  decode_block<D, T>(r, maxbits, raw, ps);
   scatter<D, T>(out, g, ix, iy, iz, raw);
 }
 

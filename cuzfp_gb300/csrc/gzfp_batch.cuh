@@ -53,7 +53,7 @@ constexpr uint32_t kBatchMaxStagedWords = 32;
 
 template <int NT, bool DECODE, int D, typename T>
 __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, BatchPlanes<NT>& ps,
-                                            uint64_t* sbuf, uint32_t staged_w, const Ctx& c) {
+                                            uint64_t* sbuf, uint32_t staged_w) {
   if (DECODE) {
     const uint32_t W = d.maxbits >> 6;
     if (d.maxbits % 64 == 0 && W <= staged_w) {  // the same for the whole warp (one item)
@@ -67,17 +67,17 @@ __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, Batc
       __syncwarp();
       if (b < d.g.nblocks)
         decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
-                         StagedWords<NT + 1>{sbuf + threadIdx.x, b * W, W}, ps, c);
+                         StagedWords<NT + 1>{sbuf + threadIdx.x, b * W, W}, ps);
       __syncwarp();  // the next chunk's copy reuses the buffer
       return;
     }
     if (b >= d.g.nblocks) return;
     decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
-                     DevWords{nullptr, (const uint64_t*)d.in, d.nwords}, ps, c);
+                     DevWords{nullptr, (const uint64_t*)d.in, d.nwords}, ps);
   } else {
     if (b >= d.g.nblocks) return;
     encode_one<D, T>((const T*)d.in, d.g, b, d.maxbits,
-                     DevWords{(uint64_t*)d.out, nullptr, d.nwords}, ps, c);
+                     DevWords{(uint64_t*)d.out, nullptr, d.nwords}, ps);
   }
 }
 
@@ -103,7 +103,7 @@ template <int NT, bool DECODE, int D, typename T>
 __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
     batch_kernel(const BatchDesc* __restrict__ descs, const uint32_t* __restrict__ chunk_item,
                  uint64_t lo, uint64_t hi, unsigned long long* counter, int bpt, int ahead,
-                 uint32_t staged_w, Ctx c) {
+                 uint32_t staged_w) {
   extern __shared__ uint64_t smem[];
   __shared__ unsigned long long s_claim;
   __shared__ BatchDesc s_desc;  // the claimed chunk's array, read field by field
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
 #pragma unroll 1
     for (int j = 0; j < bpt; j++)
       batch_block<NT, DECODE, D, T>(d, first + (uint64_t)j * NT + threadIdx.x, ps, sbuf,
-                                    staged_w, c);
+                                    staged_w);
     __syncthreads();  // every thread is done with the descriptor
     if (!ahead && threadIdx.x == 0) s_claim = lo + atomicAdd(counter, 1ull);
     __syncthreads();  // the next claim is visible
@@ -141,12 +141,11 @@ template <int NT, bool DECODE, int D, typename T>
 cudaError_t launch_batch_kind(int grid, int bpt, bool ahead, uint32_t staged_w,
                               const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,
                               uint64_t hi, unsigned long long* counter, cudaStream_t s) {
-  const Ctx c{1u, 0xffffffffu};
   const size_t sm = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
   auto k = batch_kernel<NT, DECODE, D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<grid, NT, sm, s>>>(descs, chunk_item, lo, hi, counter, bpt, ahead ? 1 : 0, staged_w, c);
+  k<<<grid, NT, sm, s>>>(descs, chunk_item, lo, hi, counter, bpt, ahead ? 1 : 0, staged_w);
   return cudaGetLastError();
 }
 

@@ -171,43 +171,39 @@ struct Perm<3> {
 
 // ----------------------------------------------------------------- lifting
 
-// Per-launch context (reserved; carries no state today).
-struct Ctx {
-  uint32_t one, m1;
-};
-
-// wrap-around integer arithmetic (zfp's signed overflow is undefined in C;
-// these steps never overflow on streams the encoder produced)
-GZ_HD int32_t add_(int32_t a, int32_t b, const Ctx&) { return (int32_t)((uint32_t)a + (uint32_t)b); }
-GZ_HD int32_t sub_(int32_t a, int32_t b, const Ctx&) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+// Wrap-around integer arithmetic.  zfp writes these steps on signed ints,
+// whose overflow C leaves undefined; two's-complement wrap is what its
+// builds compute, and integer fields near the type limits do overflow.
+GZ_HD int32_t add_(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+GZ_HD int32_t sub_(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
 GZ_HD int32_t shl1_(int32_t a) { return (int32_t)((uint32_t)a << 1); }
-GZ_HD int64_t add_(int64_t a, int64_t b, const Ctx&) { return (int64_t)((uint64_t)a + (uint64_t)b); }
-GZ_HD int64_t sub_(int64_t a, int64_t b, const Ctx&) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+GZ_HD int64_t add_(int64_t a, int64_t b) { return (int64_t)((uint64_t)a + (uint64_t)b); }
+GZ_HD int64_t sub_(int64_t a, int64_t b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
 GZ_HD int64_t shl1_(int64_t a) { return (int64_t)((uint64_t)a << 1); }
 
 // zfp's lifting steps (Z/src/template/encode.c:77-103, decode.c:28-54) in
 // two's-complement wrap-around arithmetic with arithmetic right shifts.
 template <typename Int>
-GZ_HD void fwd_lift(Int& x, Int& y, Int& z, Int& w, const Ctx& c) {
-  x = add_(x, w, c); x >>= 1; w = sub_(w, x, c);
-  z = add_(z, y, c); z >>= 1; y = sub_(y, z, c);
-  x = add_(x, z, c); x >>= 1; z = sub_(z, x, c);
-  w = add_(w, y, c); w >>= 1; y = sub_(y, w, c);
-  w = add_(w, (Int)(y >> 1), c); y = sub_(y, (Int)(w >> 1), c);
+GZ_HD void fwd_lift(Int& x, Int& y, Int& z, Int& w) {
+  x = add_(x, w); x >>= 1; w = sub_(w, x);
+  z = add_(z, y); z >>= 1; y = sub_(y, z);
+  x = add_(x, z); x >>= 1; z = sub_(z, x);
+  w = add_(w, y); w >>= 1; y = sub_(y, w);
+  w = add_(w, (Int)(y >> 1)); y = sub_(y, (Int)(w >> 1));
 }
 
 template <typename Int>
-GZ_HD void inv_lift(Int& x, Int& y, Int& z, Int& w, const Ctx& c) {
-  y = add_(y, (Int)(w >> 1), c); w = sub_(w, (Int)(y >> 1), c);
-  y = add_(y, w, c); w = shl1_(w); w = sub_(w, y, c);
-  z = add_(z, x, c); x = shl1_(x); x = sub_(x, z, c);
-  y = add_(y, z, c); z = shl1_(z); z = sub_(z, y, c);
-  w = add_(w, x, c); x = shl1_(x); x = sub_(x, w, c);
+GZ_HD void inv_lift(Int& x, Int& y, Int& z, Int& w) {
+  y = add_(y, (Int)(w >> 1)); w = sub_(w, (Int)(y >> 1));
+  y = add_(y, w); w = shl1_(w); w = sub_(w, y);
+  z = add_(z, x); x = shl1_(x); x = sub_(x, z);
+  y = add_(y, z); z = shl1_(z); z = sub_(z, y);
+  w = add_(w, x); x = shl1_(x); x = sub_(x, w);
 }
 
 // decorrelating transform: lines along x (stride 1), y (stride 4), z (16)
 template <int D, typename Int>
-GZ_HD void fwd_xform(Int* q, const Ctx& c) {
+GZ_HD void fwd_xform(Int* q) {
   constexpr int L = 1 << (2 * (D - 1));  // lines per axis
 #pragma unroll
   for (int a = 0; a < D; a++) {
@@ -215,13 +211,13 @@ GZ_HD void fwd_xform(Int* q, const Ctx& c) {
 #pragma unroll
     for (int l = 0; l < L; l++) {
       const int base = (l % s) + (l / s) * s * 4;
-      fwd_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s], c);
+      fwd_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
     }
   }
 }
 
 template <int D, typename Int>
-GZ_HD void inv_xform(Int* q, const Ctx& c) {
+GZ_HD void inv_xform(Int* q) {
   constexpr int L = 1 << (2 * (D - 1));
 #pragma unroll
   for (int a = D - 1; a >= 0; a--) {
@@ -229,7 +225,7 @@ GZ_HD void inv_xform(Int* q, const Ctx& c) {
 #pragma unroll
     for (int l = 0; l < L; l++) {
       const int base = (l % s) + (l / s) * s * 4;
-      inv_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s], c);
+      inv_lift(q[base], q[base + s], q[base + 2 * s], q[base + 3 * s]);
     }
   }
 }
@@ -756,23 +752,21 @@ GZ_HD void store_to_coeffs(const PS& ps, int base, int lo, int hi, UInt* u) {
 // Front end of the encoder: block-floating-point conversion, decorrelating
 // transform, sequency reordering and negabinary mapping.
 template <int D, typename T>
-GZ_HD void front_end(const typename FT<T>::UInt* raw, int emax, typename FT<T>::UInt* u,
-                     const Ctx& c) {
+GZ_HD void front_end(const typename FT<T>::UInt* raw, int emax, typename FT<T>::UInt* u) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
   constexpr int BS = 1 << (2 * D);
   Int q[BS];
   quantize(raw, q, BS, emax);
-  fwd_xform<D>(q, c);
+  fwd_xform<D>(q);
 #pragma unroll
   for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
 }
 
 // Front end of the encoder for an integer block: transform, order, map.
 template <int D, typename T>
-GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* u,
-                         const Ctx& c) {
+GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* u) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
@@ -780,7 +774,7 @@ GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* 
   Int q[BS];
 #pragma unroll
   for (int i = 0; i < BS; i++) q[i] = (Int)raw[i];
-  fwd_xform<D>(q, c);
+  fwd_xform<D>(q);
 #pragma unroll
   for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
 }
@@ -792,8 +786,7 @@ GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* 
 // bottom slice waits in plane-store slots 32..63 while the top one is coded,
 // so only half of the block's coefficients stay in registers.
 template <int D, typename T, class W, class PS>
-GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps,
-                        const Ctx& c) {
+GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   constexpr int BS = 1 << (2 * D);
@@ -804,7 +797,7 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
   uint32_t bits;
   int kmin;
   if constexpr (F::INT) {
-    front_end_int<D, T>(raw, u, c);
+    front_end_int<D, T>(raw, u);
     bits = maxbits;
     kmin = 0;
   } else {
@@ -826,7 +819,7 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
     prec = prec < 0 ? 0 : prec > P ? P : prec;
     const uint32_t e = (uint32_t)(emax + F::EBIAS);
     w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
-    front_end<D, T>(raw, emax, u, c);
+    front_end<D, T>(raw, emax, u);
     bits = maxbits - (F::EBITS + 1);
     kmin = P - prec;
   }
@@ -874,8 +867,7 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
 // Decode one block from a reader positioned at its first bit into raw IEEE
 // bit patterns (Z/src/template/decode.c:137-165).
 template <int D, typename T, class R, class PS>
-GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& ps,
-                        const Ctx& c) {
+GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& ps) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
@@ -943,7 +935,7 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& p
   Int q[BS];
 #pragma unroll
   for (int i = 0; i < BS; i++) q[Perm<D>::at(i)] = (Int)((u[i] ^ (UInt)F::NB) - (UInt)F::NB);
-  inv_xform<D>(q, c);
+  inv_xform<D>(q);
   if constexpr (F::INT) {
 #pragma unroll
     for (int i = 0; i < BS; i++) raw[i] = (UInt)q[i];

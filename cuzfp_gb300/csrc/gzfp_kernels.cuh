@@ -107,12 +107,12 @@ constexpr int store_slots() {
 template <int D, typename T>
 __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
     encode_kernel(const T* __restrict__ in, Geom g, uint32_t maxbits, uint64_t* __restrict__ out,
-                  uint64_t nwords, Ctx c) {
+                  uint64_t nwords) {
   extern __shared__ uint64_t smem[];
   SmemPlanes ps{smem + threadIdx.x};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b < g.nblocks)
-    encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps, c);
+    encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps);
 }
 
 // MINB: resident CTAs per SM the register budget is sized for.  The decoder
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
 template <int D, typename T, bool STAGED, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
     decode_kernel(const uint64_t* __restrict__ in, uint64_t nwords, Geom g, uint32_t maxbits,
-                  T* __restrict__ out, Ctx c) {
+                  T* __restrict__ out) {
   extern __shared__ uint64_t smem[];
   SmemPlanes ps{smem + threadIdx.x};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -136,10 +136,9 @@ __global__ void __launch_bounds__(kThreads, MINB)
     }
     __syncwarp();
     if (b < g.nblocks)
-      decode_one<D, T>(out, g, b, maxbits, StagedWords<kStride>{buf + threadIdx.x, b * W, W}, ps,
-                       c);
+      decode_one<D, T>(out, g, b, maxbits, StagedWords<kStride>{buf + threadIdx.x, b * W, W}, ps);
   } else {
-    if (b < g.nblocks) decode_one<D, T>(out, g, b, maxbits, DevWords{nullptr, in, nwords}, ps, c);
+    if (b < g.nblocks) decode_one<D, T>(out, g, b, maxbits, DevWords{nullptr, in, nwords}, ps);
   }
 }
 
@@ -149,12 +148,11 @@ cudaError_t launch_encode_t(const T* in, const Geom& g, uint32_t maxbits, uint64
                             uint64_t nwords, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const Ctx c{1u, 0xffffffffu};
   const size_t sm = smem_bytes(store_slots<D, T>(), false, 0);
   auto k = encode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<grid, kThreads, sm, s>>>(in, g, maxbits, out, nwords, c);
+  k<<<grid, kThreads, sm, s>>>(in, g, maxbits, out, nwords);
   return cudaGetLastError();
 }
 
@@ -167,7 +165,6 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
                             T* out, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const Ctx c{1u, 0xffffffffu};
   const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords;
   const size_t sm = smem_bytes(32, staged, maxbits >> 6);
   constexpr int MB = MinBlocks<D, T>::value;
@@ -176,7 +173,7 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
                                          : decode_kernel<D, T, true, MB>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<grid, kThreads, sm, s>>>(in, nwords, g, maxbits, out, c);
+  k<<<grid, kThreads, sm, s>>>(in, nwords, g, maxbits, out);
   return cudaGetLastError();
 }
 

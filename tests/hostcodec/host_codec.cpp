@@ -48,18 +48,16 @@ template <int D, typename T>
 void enc(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out, uint64_t words) {
   HostWords w{out, nullptr, words};
   gzfp::LocalPlanes ps;
-  const gzfp::Ctx c{1u, 0xffffffffu};
   for (uint64_t b = 0; b < g.nblocks; b++)
-    gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w, ps, c);
+    gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w, ps);
 }
 
 template <int D, typename T>
 void dec(const uint64_t* in, uint64_t words, const gzfp::Geom& g, unsigned maxbits, void* data) {
   HostWords w{nullptr, in, words};
   gzfp::LocalPlanes ps;
-  const gzfp::Ctx c{1u, 0xffffffffu};
   for (uint64_t b = 0; b < g.nblocks; b++)
-    gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w, ps, c);
+    gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w, ps);
 }
 
 template <typename T>
