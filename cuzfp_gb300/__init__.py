@@ -16,8 +16,9 @@ codec, which cuZFP's test driver treats as ground truth):
   in zfp_structs.h:64-69); the two agree for every integer 3D rate.
 * Partial edge blocks are padded by zfp's pad_block rule.
 * Errors raise ``GzfpError`` instead of being printed.
-* Strided fields (non-zero sx/sy/sz), which cuZFP silently ignores, are
-  rejected with ``GzfpError``.
+* Strided fields (non-zero sx/sy/sz), which cuZFP silently codes as
+  contiguous, are coded through their strides as zfp 0.5.0 does; so are
+  non-contiguous tensors and arrays.
 * Integer fields (int32 / int64) are coded as zfp 0.5.0's integer block
   codec does (no exponent, whole budget); a rate that gives 0 bits per
   block is rejected.
@@ -65,6 +66,12 @@ _lib.gzfp_compress_bits.restype = _I
 _lib.gzfp_compress_bits.argtypes = [_I, _U, _U, _U, _U, _VP, _VP, _SZ, ctypes.POINTER(_SZ), _VP]
 _lib.gzfp_decompress_bits.restype = _I
 _lib.gzfp_decompress_bits.argtypes = [_I, _U, _U, _U, _U, _VP, _SZ, _VP, _VP]
+_LL = ctypes.c_longlong
+_lib.gzfp_compress_strided.restype = _I
+_lib.gzfp_compress_strided.argtypes = [_I, _U, _U, _U, _LL, _LL, _LL, _U, _VP, _VP, _SZ,
+                                       ctypes.POINTER(_SZ), _VP]
+_lib.gzfp_decompress_strided.restype = _I
+_lib.gzfp_decompress_strided.argtypes = [_I, _U, _U, _U, _LL, _LL, _LL, _U, _VP, _SZ, _VP, _VP]
 
 # zfp constants (src/cuZFP/zfp_structs.h:9-13)
 ZFP_MAX_PREC = 64
@@ -210,6 +217,31 @@ def _addr_and_size(obj: Any) -> tuple[int, Optional[int]]:
     raise GzfpError(GZFP_ERR_ARG, f"unsupported buffer type {type(obj).__name__}")
 
 
+def _element_strides(obj: Any):
+    """(sx, sy, sz) element strides (x fastest) of a torch tensor or numpy
+    array, or None when it is contiguous."""
+    if hasattr(obj, "data_ptr") and hasattr(obj, "stride"):  # torch.Tensor
+        if obj.is_contiguous():
+            return None
+        st = list(obj.stride())[::-1]
+    elif hasattr(obj, "__array_interface__"):
+        if obj.flags["C_CONTIGUOUS"]:
+            return None
+        st = [b // obj.itemsize for b in obj.strides[::-1]]
+    else:
+        return None
+    return tuple((st + [0, 0])[:3])
+
+
+def _field_addr(obj: Any) -> int:
+    """Address of element (0, 0, 0) of a tensor or array, strided or not."""
+    if hasattr(obj, "data_ptr"):
+        return int(obj.data_ptr())
+    if hasattr(obj, "__array_interface__"):
+        return int(obj.__array_interface__["data"][0])
+    return _addr_and_size(obj)[0]
+
+
 def _cuda_stream_handle(cuda_stream: Any) -> int:
     if cuda_stream is None:
         return 0
@@ -219,8 +251,6 @@ def _cuda_stream_handle(cuda_stream: Any) -> int:
 
 
 def _check_fixed_rate(zfp: zfp_stream, f: zfp_field) -> None:
-    if f.sx or f.sy or f.sz:
-        raise GzfpError(GZFP_ERR_UNSUPPORTED, "strided fields")
     if zfp.minbits != zfp.maxbits:
         raise GzfpError(GZFP_ERR_UNSUPPORTED, "only fixed-rate streams (minbits == maxbits)")
 
@@ -234,16 +264,22 @@ def compress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> int:
     returns when the result is in host memory.
     """
     _check_fixed_rate(zfp, f)
-    src, _ = _addr_and_size(f.data)
+    strides = _field_strides(f)
+    src = _field_addr(f.data) if strides else _addr_and_size(f.data)[0]
     dst, cap = _addr_and_size(zfp.stream)
     if zfp.capacity is not None:
         cap = zfp.capacity
     if cap is None:
         cap = zfp_stream_maximum_size(zfp, f)
     out = _SZ(0)
-    _check(_lib.gzfp_compress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, dst, cap,
-                                   ctypes.byref(out), _cuda_stream_handle(cuda_stream)),
-           "compress")
+    if strides:
+        st = _lib.gzfp_compress_strided(int(f.type), f.nx, f.ny, f.nz, *strides, zfp.maxbits, src,
+                                        dst, cap, ctypes.byref(out),
+                                        _cuda_stream_handle(cuda_stream))
+    else:
+        st = _lib.gzfp_compress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, dst, cap,
+                                     ctypes.byref(out), _cuda_stream_handle(cuda_stream))
+    _check(st, "compress")
     return int(out.value)
 
 
@@ -251,15 +287,28 @@ def decompress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> None:
     """Decompress ``zfp.stream`` into ``f.data`` (cuZFP::decompress,
     src/cuZFP/cuZFP.cu:212-269)."""
     _check_fixed_rate(zfp, f)
+    strides = _field_strides(f)
     src, size = _addr_and_size(zfp.stream)
-    dst, _ = _addr_and_size(f.data)
+    dst = _field_addr(f.data) if strides else _addr_and_size(f.data)[0]
     if zfp.capacity is not None:
         size = zfp.capacity
     if size is None:
         size = stream_size(f.type, f.nx, f.ny, f.nz, zfp.maxbits)
-    _check(_lib.gzfp_decompress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, size, dst,
-                                     _cuda_stream_handle(cuda_stream)),
-           "decompress")
+    if strides:
+        st = _lib.gzfp_decompress_strided(int(f.type), f.nx, f.ny, f.nz, *strides, zfp.maxbits,
+                                          src, size, dst, _cuda_stream_handle(cuda_stream))
+    else:
+        st = _lib.gzfp_decompress_bits(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits, src, size, dst,
+                                       _cuda_stream_handle(cuda_stream))
+    _check(st, "decompress")
+
+
+def _field_strides(f: zfp_field):
+    """The field's strides: its sx/sy/sz when set, else those of a
+    non-contiguous tensor or array; None for a contiguous field."""
+    if f.sx or f.sy or f.sz:
+        return (f.sx, f.sy, f.sz)
+    return _element_strides(f.data) if f.data is not None else None
 
 
 # ------------------------------------------------------- array conveniences
@@ -286,9 +335,10 @@ def _type_of(dtype) -> zfp_type:
 
 
 def compress_tensor(x, rate: float, out=None, cuda_stream: Any = None):
-    """Compress a contiguous CUDA tensor (float32 / float64, 1-3 dims) at
-    ``rate`` bits per value.  Returns the uint64 word tensor of the stream
-    (``out`` if given) on the same device."""
+    """Compress a CUDA tensor (float32 / float64 / int32 / int64, 1-3 dims;
+    a strided view is coded through its strides, as zfp codes a strided
+    field) at ``rate`` bits per value.  Returns the uint64 word tensor of the
+    stream (``out`` if given) on the same device."""
     import torch
     t = _type_of(x.dtype)
     nx, ny, nz = _dims_of(x.shape)
@@ -303,7 +353,8 @@ def compress_tensor(x, rate: float, out=None, cuda_stream: Any = None):
 
 
 def decompress_tensor(words, shape, dtype, rate: float, out=None, cuda_stream: Any = None):
-    """Inverse of compress_tensor."""
+    """Inverse of compress_tensor; ``out`` may be a strided view, whose other
+    elements are left as they are."""
     import torch
     t = _type_of(dtype)
     nx, ny, nz = _dims_of(shape)

@@ -410,6 +410,131 @@ int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsign
   return GZFP_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Apply zfp's stride defaults (0 = contiguous along that axis) and decide
+// whether rows of full blocks can move as vectors: unit x stride and every
+// row start aligned.
+void set_strides(gzfp::Geom& g, int dims, int type, const void* p, long long sx, long long sy,
+                 long long sz) {
+  g.sx = sx ? sx : 1;
+  g.sy = sy ? sy : (long long)g.nx;
+  g.sz = sz ? sz : (long long)g.nx * g.ny;
+  const long long a = 4 * (long long)scalar_size(type), S = (long long)scalar_size(type);
+  g.vec = (g.sx == 1 && g.nx % 4 == 0 && (uintptr_t)p % a == 0 && (dims < 2 || (g.sy * S) % a == 0) &&
+           (dims < 3 || (g.sz * S) % a == 0))
+              ? 1u
+              : 0u;
+}
+
+// The element offsets, relative to the field pointer, of the lowest and the
+// highest value a strided field reaches.
+void stride_span(const gzfp::Geom& g, long long& lo, long long& hi) {
+  lo = hi = 0;
+  const long long n[3] = {g.nx, g.ny, g.nz}, st[3] = {g.sx, g.sy, g.sz};
+  for (int a = 0; a < 3; a++) {
+    const long long e = (n[a] - 1) * st[a];
+    lo += e < 0 ? e : 0;
+    hi += e > 0 ? e : 0;
+  }
+}
+
+int strided_call(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                 long long sy, long long sz, unsigned maxbits, void* field, uint64_t* words,
+                 size_t words_bytes, size_t* out_bytes, void* cuda_stream) {
+  clear_error();
+  gzfp::Geom g;
+  int dims;
+  int st = check_common(type, nx, ny, nz, maxbits, g, dims);
+  if (st) return st;
+  if (!field || !words) return fail(GZFP_ERR_ARG, "null pointer");
+  const uint64_t nwords = stream_words(g, maxbits);
+  const size_t need = (size_t)(nwords * 8);
+  if (words_bytes < need)
+    return fail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY,
+                decode ? "stream shorter than the compressed size"
+                       : "stream buffer smaller than the compressed size");
+  if (out_bytes) *out_bytes = need;
+  if (g.nblocks == 0) return GZFP_OK;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  const size_t S = scalar_size(type);
+  const bool dev_field = is_device_pointer(field), dev_words = is_device_pointer(words);
+  cudaError_t e;
+  if (dev_field && dev_words) {
+    set_strides(g, dims, type, field, sx, sy, sz);
+    if (!decode && maxbits % 64 && (e = cudaMemsetAsync(words, 0, need, s)))
+      return cuda_fail(e, "cudaMemsetAsync(stream)");
+    e = decode ? decode_launch(type, dims, words, nwords, g, maxbits, field, s)
+               : encode_launch(type, dims, field, g, maxbits, words, nwords, s);
+    return e ? cuda_fail(e, decode ? "decode kernel launch" : "encode kernel launch") : GZFP_OK;
+  }
+  // host memory: stage the span the strides reach, and the stream
+  set_strides(g, dims, type, nullptr, sx, sy, sz);
+  long long lo, hi;
+  stride_span(g, lo, hi);
+  const size_t span = (size_t)(hi - lo + 1) * S;
+  int device = 0;
+  if ((e = cudaGetDevice(&device))) return cuda_fail(e, "cudaGetDevice");
+  if (device < 0 || device >= kMaxDevices) return fail(GZFP_ERR_CUDA, "device index out of range");
+  Workspace& ws = g_ws[device];
+  std::lock_guard<std::mutex> lock(ws.mu);
+  Slot& sl = ws.slot[0];
+  char* hfield = (char*)field + lo * (long long)S;  // lowest value reached
+  char* dfield = (char*)field;
+  if (!dev_field) {
+    if ((e = reserve(sl.field, sl.field_cap, span))) return cuda_fail(e, "cudaMalloc(field staging)");
+    dfield = (char*)sl.field - lo * (long long)S;  // the kernel's field pointer
+  }
+  uint64_t* dwords = words;
+  if (!dev_words) {
+    if ((e = reserve(sl.stream, sl.stream_cap, need))) return cuda_fail(e, "cudaMalloc(stream staging)");
+    dwords = (uint64_t*)sl.stream;
+  }
+  set_strides(g, dims, type, dfield, sx, sy, sz);
+  st = GZFP_OK;
+  if (!dev_field && (e = cudaMemcpyAsync(sl.field, hfield, span, cudaMemcpyHostToDevice, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(field H2D)");
+  if (!st && decode && !dev_words &&
+      (e = cudaMemcpyAsync(dwords, words, need, cudaMemcpyHostToDevice, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(stream H2D)");
+  if (!st && !decode && maxbits % 64 && (e = cudaMemsetAsync(dwords, 0, need, s)))
+    st = cuda_fail(e, "cudaMemsetAsync(stream)");
+  if (!st) {
+    e = decode ? decode_launch(type, dims, dwords, nwords, g, maxbits, dfield, s)
+               : encode_launch(type, dims, dfield, g, maxbits, dwords, nwords, s);
+    if (e) st = cuda_fail(e, decode ? "decode kernel launch" : "encode kernel launch");
+  }
+  if (!st && decode && !dev_field &&
+      (e = cudaMemcpyAsync(hfield, sl.field, span, cudaMemcpyDeviceToHost, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(field D2H)");
+  if (!st && !decode && !dev_words &&
+      (e = cudaMemcpyAsync(words, dwords, need, cudaMemcpyDeviceToHost, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(stream D2H)");
+  const cudaError_t es = cudaStreamSynchronize(s);  // nothing stays in flight
+  if (!st && es) st = cuda_fail(es, "cudaStreamSynchronize");
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gzfp_compress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                          long long sy, long long sz, unsigned maxbits, const void* data,
+                          void* stream, size_t capacity, size_t* out_bytes, void* cuda_stream) {
+  return strided_call(false, type, nx, ny, nz, sx, sy, sz, maxbits, (void*)data,
+                      (uint64_t*)stream, capacity, out_bytes, cuda_stream);
+}
+
+int gzfp_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                            long long sy, long long sz, unsigned maxbits, const void* stream,
+                            size_t bytes, void* data, void* cuda_stream) {
+  return strided_call(true, type, nx, ny, nz, sx, sy, sz, maxbits, data, (uint64_t*)stream, bytes,
+                      nullptr, cuda_stream);
+}
+
 int gzfp_compress(int type, unsigned nx, unsigned ny, unsigned nz, double rate, const void* data,
                   void* stream, size_t capacity, size_t* out_bytes, void* cuda_stream) {
   clear_error();

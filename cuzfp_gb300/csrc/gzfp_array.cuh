@@ -33,12 +33,16 @@ GZ_HD uint32_t fast_div(uint32_t n, const FastDiv& f) {
   return (uint32_t)(((uint64_t)hi + n) >> f.s);
 }
 
-// Geometry of a contiguous a[nz][ny][nx] field cut into 4^D blocks (fewer
-// than 2^32 of them); unused axes have size 1.
+// Geometry of an nx x ny x nz field cut into 4^D blocks (fewer than 2^32 of
+// them); unused axes have size 1.  Value (x, y, z) sits at element
+// x*sx + y*sy + z*sz of the field pointer: a contiguous a[nz][ny][nx] has
+// (sx, sy, sz) = (1, nx, nx*ny), and zfp's strided fields any signed strides
+// (Z/src/template/compress.c, compress_strided).
 struct Geom {
   uint32_t nx, ny, nz;
   uint32_t bx, by, bz;  // blocks per axis
   uint64_t nblocks;
+  int64_t sx, sy, sz;   // element strides
   uint32_t vec;  // rows of full blocks may be moved as one 16/32-byte vector
   FastDiv dbx, dby;
 };
@@ -52,6 +56,9 @@ GZ_HD Geom make_geom_blocks(uint32_t nx, uint32_t ny, uint32_t nz) {
   g.by = (ny + 3) / 4;
   g.bz = (nz + 3) / 4;
   g.nblocks = (uint64_t)g.bx * g.by * g.bz;
+  g.sx = 1;
+  g.sy = nx;
+  g.sz = (int64_t)nx * ny;
   g.vec = 0;
   g.dbx = make_fastdiv(g.bx);
   g.dby = make_fastdiv(g.by);
@@ -141,8 +148,8 @@ GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t
   const uint32_t cx = valid_count(g.nx, ix);
   const uint32_t cy = D >= 2 ? valid_count(g.ny, iy) : 1;
   const uint32_t cz = D >= 3 ? valid_count(g.nz, iz) : 1;
-  const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
-  const T* base = in + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
+  const int64_t sx = g.sx, sy = g.sy, sz = g.sz;
+  const T* base = in + 4 * (ix * sx + iy * sy + iz * sz);
   constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
   const bool full = cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4);
   if (full && g.vec) {
@@ -156,7 +163,7 @@ GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t
 #pragma unroll
       for (int y = 0; y < DY; y++)
 #pragma unroll
-        for (int x = 0; x < 4; x++) raw[16 * z + 4 * y + x] = load_bits(base + x + y * sy + z * sz);
+        for (int x = 0; x < 4; x++) raw[16 * z + 4 * y + x] = load_bits(base + x * sx + y * sy + z * sz);
   } else {
 #pragma unroll
     for (int z = 0; z < DZ; z++)
@@ -165,7 +172,7 @@ GZ_HD void gather(const T* in, const Geom& g, uint32_t ix, uint32_t iy, uint32_t
 #pragma unroll
         for (int x = 0; x < 4; x++)
           raw[16 * z + 4 * y + x] =
-              load_bits(base + pad_index(cx, x) + pad_index(cy, y) * sy + pad_index(cz, z) * sz);
+              load_bits(base + pad_index(cx, x) * sx + pad_index(cy, y) * sy + pad_index(cz, z) * sz);
   }
 }
 
@@ -177,14 +184,14 @@ GZ_HD void scatter(T* out, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
   const uint32_t cx = valid_count(g.nx, ix);
   const uint32_t cy = D >= 2 ? valid_count(g.ny, iy) : 1;
   const uint32_t cz = D >= 3 ? valid_count(g.nz, iz) : 1;
-  const uint64_t sy = g.nx, sz = (uint64_t)g.nx * g.ny;
-  UInt* base = (UInt*)out + 4ull * ix + 4ull * iy * sy + 4ull * iz * sz;
+  const int64_t sx = g.sx, sy = g.sy, sz = g.sz;
+  UInt* base = (UInt*)out + 4 * (ix * sx + iy * sy + iz * sz);
   constexpr int DY = D >= 2 ? 4 : 1, DZ = D >= 3 ? 4 : 1;
   if (g.vec && cx == 4 && (D < 2 || cy == 4) && (D < 3 || cz == 4)) {
 #pragma unroll
     for (int z = 0; z < DZ; z++)
 #pragma unroll
-      for (int y = 0; y < DY; y++) store_row(out + 4ull * ix + (4ull * iy + y) * sy + (4ull * iz + z) * sz, raw + 16 * z + 4 * y);
+      for (int y = 0; y < DY; y++) store_row((T*)base + y * sy + z * sz, raw + 16 * z + 4 * y);
     return;
   }
 #pragma unroll
@@ -194,7 +201,7 @@ GZ_HD void scatter(T* out, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
 #pragma unroll
       for (int x = 0; x < 4; x++)
         if ((uint32_t)x < cx && (uint32_t)y < cy && (uint32_t)z < cz)
-          base[x + y * sy + z * sz] = raw[16 * z + 4 * y + x];
+          base[x * sx + y * sy + z * sz] = raw[16 * z + 4 * y + x];
 }
 
 // ------------------------------------------------------------- bit writer

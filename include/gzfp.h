@@ -96,6 +96,22 @@ int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned
 int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
                          const void* stream, size_t bytes, void* data, void* cuda_stream);
 
+/* Strided fields: value (x, y, z) at element x*sx + y*sy + z*sz of `data`,
+   signed strides counted in values, 0 selecting the contiguous stride of
+   that axis (1, nx, nx*ny) -- zfp_field's sx/sy/sz, as zfp 0.5.0 compresses
+   them (zfp-0.5.0/src/template/compress.c, compress_strided).  cuZFP keeps
+   these fields in its zfp_field (src/cuZFP/zfp_structs.h:39-44) but codes
+   every field as contiguous.  The stream is the one zfp_compress writes for
+   the strided field.  A host `data` pointer is staged as the whole span of
+   values the strides reach; decompression into host memory reads that span
+   first, so values between the field's are kept. */
+int gzfp_compress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                          long long sy, long long sz, unsigned maxbits, const void* data,
+                          void* stream, size_t capacity, size_t* out_bytes, void* cuda_stream);
+int gzfp_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                            long long sy, long long sz, unsigned maxbits, const void* stream,
+                            size_t bytes, void* data, void* cuda_stream);
+
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and
    bits per block -- coded by one persistent kernel over a device-side work

@@ -47,7 +47,7 @@ typedef enum {
 typedef struct {
   zfp_type type;              /* scalar type */
   unsigned int nx, ny, nz;    /* sizes (zero for unused dimensions) */
-  int sx, sy, sz;             /* strides (must be zero: contiguous a[nz][ny][nx]) */
+  int sx, sy, sz;             /* strides in values (0: contiguous a[nz][ny][nx]) */
   void* data;                 /* host or device pointer to the array */
 } zfp_field;
 

@@ -63,6 +63,14 @@ def port() -> ctypes.CDLL:
         lib.gzo_stream_bytes.argtypes = _A
         lib.gzo_maxbits.restype = ctypes.c_uint
         lib.gzo_maxbits.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        _L = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_longlong,
+              ctypes.c_longlong, ctypes.c_longlong, ctypes.c_double]
+        lib.gzo_compress_strided.restype = ctypes.c_size_t
+        lib.gzo_compress_strided.argtypes = _L + [ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_size_t, ctypes.c_int]
+        lib.gzo_decompress_strided.restype = ctypes.c_int
+        lib.gzo_decompress_strided.argtypes = _L + [ctypes.c_void_p, ctypes.c_size_t,
+                                                    ctypes.c_void_p, ctypes.c_int]
         _port = lib
     return _port
 
@@ -83,6 +91,14 @@ def ref() -> ctypes.CDLL:
         lib.zref_maximum_size.argtypes = _A
         lib.zref_set_rate_bits.restype = ctypes.c_uint
         lib.zref_set_rate_bits.argtypes = [ctypes.c_int, ctypes.c_uint, ctypes.c_double]
+        _S = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_int,
+              ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        lib.zref_compress_strided.restype = ctypes.c_size_t
+        lib.zref_compress_strided.argtypes = _S + [ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_size_t]
+        lib.zref_decompress_strided.restype = ctypes.c_int
+        lib.zref_decompress_strided.argtypes = _S + [ctypes.c_void_p, ctypes.c_size_t,
+                                                     ctypes.c_void_p]
         lib.zref_compress_int.restype = ctypes.c_size_t
         lib.zref_compress_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         lib.zref_decompress_int.restype = ctypes.c_int
@@ -186,3 +202,50 @@ def ref_fields():
     af = np.ctypeslib.as_array((ctypes.c_float * (3 * 4096)).in_dll(lib, "array_float"))
     ad = np.ctypeslib.as_array((ctypes.c_double * (3 * 4096)).in_dll(lib, "array_double"))
     return af.reshape(3, 4096).copy(), ad.reshape(3, 4096).copy()
+
+
+def view_geometry(v: np.ndarray):
+    """(nx, ny, nz), element strides (sx, sy, sz) and the address of element
+    (0, 0, 0) of a 1-3D numpy view, possibly non-contiguous or reversed."""
+    nx, ny, nz = dims3(v.shape)
+    st = [int(b) // v.itemsize for b in v.strides[::-1]] + [0, 0]
+    return (nx, ny, nz), tuple(st[:3]), int(v.__array_interface__["data"][0])
+
+
+def compress_view(v: np.ndarray, rate: float, nthreads: int = 1) -> np.ndarray:
+    """Oracle stream of a strided view (zfp_field sx/sy/sz)."""
+    (nx, ny, nz), (sx, sy, sz), addr = view_geometry(v)
+    n = stream_bytes(v.shape, v.dtype, rate)
+    out = np.zeros(max(n // 8, 1), np.uint64)
+    lib = port()
+    got = lib.gzo_compress_strided(type_code(v.dtype), nx, ny, nz, sx, sy, sz, float(rate), addr,
+                                   out.ctypes.data, out.nbytes, int(nthreads))
+    if got != n:
+        raise RuntimeError("oracle strided compress failed")
+    return out[: n // 8]
+
+
+def decompress_into(words: np.ndarray, v: np.ndarray, rate: float, nthreads: int = 1) -> None:
+    """Decode into the strided view `v`; other values of its buffer stay."""
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    (nx, ny, nz), (sx, sy, sz), addr = view_geometry(v)
+    if not port().gzo_decompress_strided(type_code(v.dtype), nx, ny, nz, sx, sy, sz, float(rate),
+                                         words.ctypes.data, words.nbytes, addr, int(nthreads)):
+        raise RuntimeError("oracle strided decompress failed")
+
+
+def ref_compress_view(v: np.ndarray, rate: float) -> np.ndarray:
+    (nx, ny, nz), (sx, sy, sz), addr = view_geometry(v)
+    t = type_code(v.dtype)
+    cap = int(ref().zref_maximum_size(t, nx, ny, nz, float(rate)))
+    buf = np.zeros(cap // 8 + 1, np.uint64)
+    n = ref().zref_compress_strided(t, nx, ny, nz, sx, sy, sz, float(rate), addr, buf.ctypes.data,
+                                    cap)
+    return buf[: n // 8]
+
+
+def ref_decompress_into(words: np.ndarray, v: np.ndarray, rate: float) -> None:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    (nx, ny, nz), (sx, sy, sz), addr = view_geometry(v)
+    ref().zref_decompress_strided(type_code(v.dtype), nx, ny, nz, sx, sy, sz, float(rate),
+                                  words.ctypes.data, words.nbytes, addr)

@@ -164,3 +164,48 @@ int zref_decompress_int(int type, unsigned nx, unsigned ny, unsigned nz, double 
                         const void* buffer, size_t bytes, void* out) {
   return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0) != 0;
 }
+
+/* Strided fields through zfp_field_set_stride_<d> (Z/src/zfp.c:230-252):
+   zfp_compress and zfp_decompress then take their strided paths. */
+static zfp_field* make_strided(int type, unsigned nx, unsigned ny, unsigned nz, int sx, int sy,
+                               int sz, void* data) {
+  zfp_field* f = make_field(type, nx, ny, nz, data);
+  if (nz) zfp_field_set_stride_3d(f, sx, sy, sz);
+  else if (ny) zfp_field_set_stride_2d(f, sx, sy);
+  else zfp_field_set_stride_1d(f, sx);
+  return f;
+}
+
+size_t zref_compress_strided(int type, unsigned nx, unsigned ny, unsigned nz, int sx, int sy,
+                             int sz, double rate, const void* data, void* buffer,
+                             size_t capacity) {
+  zfp_field* field = make_strided(type, nx, ny, nz, sx, sy, sz, (void*)data);
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_rate(zfp, rate, (zfp_type)type, zfp_field_dimensionality(field), 0);
+  size_t bytes = 0;
+  if (zfp_stream_maximum_size(zfp, field) <= capacity) {
+    bitstream* s = stream_open(buffer, capacity);
+    zfp_stream_set_bit_stream(zfp, s);
+    zfp_stream_rewind(zfp);
+    bytes = zfp_compress(zfp, field);
+    stream_close(s);
+  }
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return bytes;
+}
+
+int zref_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, int sx, int sy,
+                            int sz, double rate, const void* buffer, size_t bytes, void* out) {
+  zfp_field* field = make_strided(type, nx, ny, nz, sx, sy, sz, out);
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_rate(zfp, rate, (zfp_type)type, zfp_field_dimensionality(field), 0);
+  bitstream* s = stream_open((void*)buffer, bytes);
+  zfp_stream_set_bit_stream(zfp, s);
+  zfp_stream_rewind(zfp);
+  int ok = zfp_decompress(zfp, field);
+  stream_close(s);
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return ok;
+}

@@ -227,6 +227,7 @@ typedef struct {
   int P;      /* bits per integer: 32 or 64 */
   int ebits;  /* exponent bits: 8 or 11 */
   int ebias;  /* 127 or 1023 */
+  long long sx, sy, sz; /* element strides (zfp_field sx/sy/sz, 0 = contiguous) */
 } params;
 
 /* zfp_stream_set_rate, wra = 0 (Z/src/zfp.c:405-430): floor(4^d rate + 0.5)
@@ -252,6 +253,9 @@ static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, dou
   /* integer blocks carry no exponent (Z/src/template/encode.c:176-185) */
   p->ebits = type == GZO_FLOAT ? 8 : type == GZO_DOUBLE ? 11 : 0;
   p->ebias = p->ebits ? (1 << (p->ebits - 1)) - 1 : 0;
+  p->sx = 1;
+  p->sy = p->nx;
+  p->sz = (long long)p->nx * p->ny;
   return 1;
 }
 
@@ -418,7 +422,7 @@ static void gather(const params* p, const void* data, unsigned bx, unsigned by, 
         size_t gx = 4 * bx + padmap(cx, x);
         size_t gy = p->dims >= 2 ? 4 * by + padmap(cy, y) : 0;
         size_t gz = p->dims == 3 ? 4 * bz + padmap(cz, z) : 0;
-        size_t idx = gx + p->nx * (gy + (size_t)p->ny * gz);
+        long long idx = (long long)gx * p->sx + (long long)gy * p->sy + (long long)gz * p->sz;
         unsigned o = x + 4 * y + 16 * z;
         const size_t es = scalar_bytes(p);  /* memcpy: any scalar type, no aliasing */
         memcpy((char*)blk + o * es, (const char*)data + idx * es, es);
@@ -527,7 +531,8 @@ static void scatter(const params* p, void* data, unsigned bx, unsigned by, unsig
   for (z = 0; z < cz; z++)
     for (y = 0; y < cy; y++)
       for (x = 0; x < cx; x++) {
-        size_t idx = (4 * bx + x) + p->nx * ((4 * by + y) + (size_t)p->ny * (4 * bz + z));
+        long long idx = (long long)(4 * bx + x) * p->sx + (long long)(4 * by + y) * p->sy +
+                        (long long)(4 * bz + z) * p->sz;
         unsigned o = x + 4 * y + 16 * z;
         const size_t es = scalar_bytes(p);
         memcpy((char*)data + idx * es, (const char*)blk + o * es, es);
@@ -639,5 +644,47 @@ int gzo_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
   proto.out = data;
   proto.istream = (const uint64_t*)stream;
   run_jobs(&p, &proto, nblocks, nthreads, decode_range);
+  return 1;
+}
+
+/* Strided fields (zfp_field sx/sy/sz; Z/src/template/compress.c,
+   compress_strided / decompress_strided): value (x, y, z) at element
+   x*sx + y*sy + z*sz of `data`, 0 meaning the contiguous stride. */
+static void set_strides(params* p, long long sx, long long sy, long long sz) {
+  p->sx = sx ? sx : 1;
+  p->sy = sy ? sy : (long long)p->nx;
+  p->sz = sz ? sz : (long long)p->nx * p->ny;
+}
+
+size_t gzo_compress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                            long long sy, long long sz, double rate, const void* data,
+                            void* stream, size_t capacity, int nthreads) {
+  params p;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  set_strides(&p, sx, sy, sz);
+  size_t bytes = gzo_stream_bytes(type, nx, ny, nz, rate);
+  if (capacity < bytes) return 0;
+  job proto;
+  memset(&proto, 0, sizeof proto);
+  proto.p = &p;
+  proto.data = data;
+  proto.stream = (uint64_t*)stream;
+  run_jobs(&p, &proto, (uint64_t)p.bx * p.by * p.bz, nthreads, encode_range);
+  return bytes;
+}
+
+int gzo_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                           long long sy, long long sz, double rate, const void* stream,
+                           size_t bytes, void* data, int nthreads) {
+  params p;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  set_strides(&p, sx, sy, sz);
+  if (bytes < gzo_stream_bytes(type, nx, ny, nz, rate)) return 0;
+  job proto;
+  memset(&proto, 0, sizeof proto);
+  proto.p = &p;
+  proto.out = data;
+  proto.istream = (const uint64_t*)stream;
+  run_jobs(&p, &proto, (uint64_t)p.bx * p.by * p.bz, nthreads, decode_range);
   return 1;
 }

@@ -3,11 +3,12 @@
 // Mirrors the checks of cuZFP's own gtest smoke tests: exact integer round
 // trips at rate 8 for 1D (128 values), 2D (4x4) and 3D (16x8x4) float
 // fields (src/tests/t_sanity_check_{1,2,3}.cpp) and the same 3D case with a
-// device-resident stream (src/tests/t_cuda_mem.cu).  Built and run by
+// device-resident stream (src/tests/t_cuda_mem.cu), plus a strided field.  Built and run by
 // tests/test_cpp_dropin.py on a GPU machine; prints "ok" on success.
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include <cuZFP.h>
@@ -62,16 +63,43 @@ int main() {
   fails += roundtrip(4, 4, 0, false);
   fails += roundtrip(16, 8, 4, false);
   fails += roundtrip(16, 8, 4, true);
-  // a strided field is reported, not silently compressed
-  std::vector<float> v(64, 1.0f);
-  zfp_field* f = zfp_field_3d(v.data(), zfp_type_float, 4, 4, 4);
-  f->sx = 2;
-  zfp_stream zfp;
-  stream_set_rate(&zfp, 8, f->type, 3);
-  std::vector<unsigned char> buf(zfp_stream_maximum_size(&zfp, f));
-  zfp.stream = (Word*)buf.data();
-  if (compress(&zfp, f) != 0 || last_status() != GZFP_ERR_UNSUPPORTED) fails++;
-  zfp_field_free(f);
+  // a strided field (every other value of a buffer) is coded through its
+  // strides: the stream of its contiguous copy, decoded back in place
+  {
+    std::vector<float> v(128), c(64);
+    for (int i = 0; i < 128; i++) v[i] = (float)((i * 37) % 101);
+    for (int i = 0; i < 64; i++) c[i] = v[2 * i];
+    zfp_field* fs = zfp_field_3d(v.data(), zfp_type_float, 4, 4, 4);
+    fs->sx = 2;
+    fs->sy = 8;
+    fs->sz = 32;
+    zfp_field* fc = zfp_field_3d(c.data(), zfp_type_float, 4, 4, 4);
+    zfp_stream zs, zc;
+    stream_set_rate(&zs, 8, fs->type, 3);
+    stream_set_rate(&zc, 8, fc->type, 3);
+    std::vector<unsigned char> bs(zfp_stream_maximum_size(&zs, fs)), bc(bs.size());
+    zs.stream = (Word*)bs.data();
+    zc.stream = (Word*)bc.data();
+    const size_t ns = compress(&zs, fs), nc = compress(&zc, fc);
+    if (!ns || ns != nc || std::memcmp(bs.data(), bc.data(), ns)) fails++;
+    std::vector<float> back(128, -7.0f), cback(64);
+    zfp_field* gs = zfp_field_3d(back.data(), zfp_type_float, 4, 4, 4);
+    gs->sx = 2;
+    gs->sy = 8;
+    gs->sz = 32;
+    decompress(&zs, gs);
+    zfp_field* gc = zfp_field_3d(cback.data(), zfp_type_float, 4, 4, 4);
+    decompress(&zc, gc);
+    for (int i = 0; i < 64; i++)
+      if (back[2 * i] != cback[i] || back[2 * i + 1] != -7.0f) {
+        fails++;
+        break;
+      }
+    zfp_field_free(fs);
+    zfp_field_free(fc);
+    zfp_field_free(gs);
+    zfp_field_free(gc);
+  }
   std::printf(fails ? "FAILED %d\n" : "ok\n", fails);
   return fails ? 1 : 0;
 }

@@ -102,9 +102,14 @@ def test_python_mirror_errors(gz):
     gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 3)
     assert zfp.maxbits == zfp.minbits == 512
     f = gz.zfp_field_3d(None, gz.zfp_type.float, 4, 4, 4)
-    f.sx = 2
+    zfp.minbits = 0  # not fixed rate: the only mode of this path
     with pytest.raises(gz.GzfpError) as e:
         gz.compress(zfp, f)
     assert e.value.status == gz.GZFP_ERR_UNSUPPORTED
+    gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 3)
+    f.sx = 2
+    with pytest.raises(gz.GzfpError) as e:  # strided, but no data
+        gz.compress(zfp, f)
+    assert e.value.status == gz.GZFP_ERR_ARG
     assert gz.zfp_field_dimensionality(gz.zfp_field_2d(None, gz.zfp_type.double, 3, 5)) == 2
     assert abs(gz.stream_set_rate(zfp, 2.0, gz.zfp_type.float, 1) - 2.25) < 1e-12

@@ -134,3 +134,73 @@ def test_integer_oracle_matches_reference_block_api(orc, ref):
         assert np.array_equal(s, r), (a.shape, a.dtype, rate)
         assert np.array_equal(orc.decompress(s, a.shape, a.dtype, rate),
                               orc.ref_decompress(r, a.shape, a.dtype, rate)), (a.shape, rate)
+
+
+def _views(rng):
+    """Strided views of C-order arrays: slices, steps, transposes, reversals."""
+    out = []
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        b3 = np.cumsum(rng.standard_normal((30, 26, 22)), axis=2)
+        b3 = (b3 * 1000).astype(dt) if np.dtype(dt).kind == "i" else b3.astype(dt)
+        b2 = b3[:, :, 0].copy()
+        out += [b3[3:20, :, 5:9], b3[::2, 1::3, 2:], b3[1:, 2::2, ::3], b3[:, 7, :], b3[5, ::2, :],
+                b3[2, 3, ::3], b2[::3, 1::2], b3.transpose(2, 1, 0), b3[::-1, ::-1, ::-1],
+                b3.transpose(1, 0, 2)[::2], b2.T, b3[::-2, 3, :]]
+    return out
+
+
+def _zfp_valid(v) -> bool:
+    """zfp 0.5.0 computes its strided offsets (sz - ny*sy, sy - nx*sx and the
+    block steps) in unsigned arithmetic, so it reads out of bounds unless
+    every stride is positive and each axis' stride covers the previous axis'
+    extent -- sub-arrays and stepped slices of C-order arrays."""
+    st = [s // v.itemsize for s in v.strides[::-1]]
+    n = list(v.shape[::-1])
+    if any(s <= 0 for s in st):
+        return False
+    return all(st[a] >= n[a - 1] * st[a - 1] for a in range(1, len(st)))
+
+
+def _offset(v) -> int:
+    """Element offset of v[0, ..., 0] in its base array."""
+    base = v.base if v.base is not None else v
+    return (v.__array_interface__["data"][0] - base.__array_interface__["data"][0]) // v.itemsize
+
+
+def _flat_indices(v) -> np.ndarray:
+    """Base-array element indices of every value of the view."""
+    idx = np.zeros(v.shape, np.int64) + _offset(v)
+    for ax, (n, st) in enumerate(zip(v.shape, v.strides)):
+        sh = [1] * v.ndim
+        sh[ax] = n
+        idx = idx + (np.arange(n) * (st // v.itemsize)).reshape(sh)
+    return idx.reshape(-1)
+
+
+def test_strided_fields(orc):
+    """zfp_field strides: the stream of a strided view is the stream of its
+    contiguous copy, and decoding into a view touches only its values;
+    where zfp 0.5.0's own strided path is valid the streams equal its."""
+    rng = np.random.default_rng(41)
+    ref_ok = orc.ref_available() or orc.build_ref()
+    checked = 0
+    for v in _views(rng):
+        for rate in (2.0, 8.0, 13.5, 32.0):
+            if orc.stream_bytes(v.shape, v.dtype, rate) == 0:
+                continue
+            s = orc.compress_view(v, rate)
+            assert np.array_equal(s, orc.compress(np.ascontiguousarray(v), rate)), (v.shape, rate)
+            if ref_ok and _zfp_valid(v) and np.dtype(v.dtype).kind == "f":  # zfp_compress: float, double
+                assert np.array_equal(s, orc.ref_compress_view(v, rate)), (v.shape, v.strides, rate)
+                checked += 1
+            base = np.full(v.base.shape if v.base is not None else v.shape, 7, v.dtype)
+            # the same view geometry over a fresh buffer
+            w = np.lib.stride_tricks.as_strided(
+                base.reshape(-1)[_offset(v):], shape=v.shape, strides=v.strides)
+            orc.decompress_into(s, w, rate)
+            assert np.array_equal(w, orc.decompress(s, v.shape, v.dtype, rate)), (v.shape, rate)
+            untouched = np.ones(base.size, bool)
+            untouched[_flat_indices(v)] = False
+            assert np.all(base.reshape(-1)[untouched] == 7)
+    if ref_ok:
+        assert checked >= 20
