@@ -70,6 +70,16 @@ _LL = ctypes.c_longlong
 _lib.gzfp_compress_strided.restype = _I
 _lib.gzfp_compress_strided.argtypes = [_I, _U, _U, _U, _LL, _LL, _LL, _U, _VP, _VP, _SZ,
                                        ctypes.POINTER(_SZ), _VP]
+_P = ctypes.POINTER
+_lib.gzfp_write_header.restype = _I
+_lib.gzfp_write_header.argtypes = [_I, _U, _U, _U, _U, _VP, _SZ, _P(_SZ)]
+_lib.gzfp_read_header.restype = _I
+_lib.gzfp_read_header.argtypes = [_VP, _SZ, _P(_I), _P(_U), _P(_U), _P(_U), _P(_U), _P(_SZ)]
+_lib.gzfp_compress_headed.restype = _I
+_lib.gzfp_compress_headed.argtypes = [_I, _U, _U, _U, ctypes.c_double, _VP, _VP, _SZ, _P(_SZ),
+                                      _VP]
+_lib.gzfp_decompress_headed.restype = _I
+_lib.gzfp_decompress_headed.argtypes = [_VP, _SZ, _VP, _SZ, _VP]
 _lib.gzfp_decompress_strided.restype = _I
 _lib.gzfp_decompress_strided.argtypes = [_I, _U, _U, _U, _LL, _LL, _LL, _U, _VP, _SZ, _VP, _VP]
 
@@ -363,6 +373,99 @@ def decompress_tensor(words, shape, dtype, rate: float, out=None, cuda_stream: A
     if out is None:
         out = torch.empty(tuple(shape), dtype=dtype, device=words.device)
     decompress(zfp, zfp_field(type=t, nx=nx, ny=ny, nz=nz, data=out), cuda_stream)
+    return out
+
+
+# ------------------------------------------------------------ headed streams
+# zfp 0.5.0's self-describing header (zfp_write_header / zfp_read_header
+# with ZFP_HEADER_FULL, zfp-0.5.0/src/zfp.c:661-719) in front of the blocks.
+
+HEADER_MAX_BITS = 148
+_DTYPE_NAME = {zfp_type.int32: "int32", zfp_type.int64: "int64", zfp_type.float: "float32",
+               zfp_type.double: "float64"}
+
+
+def write_header(type: zfp_type, nx: int, ny: int, nz: int, maxbits: int) -> tuple[bytes, int]:
+    """The header bytes of a fixed-rate stream and its length in bits."""
+    buf = ctypes.create_string_buffer(24)
+    bits = _SZ(0)
+    _check(_lib.gzfp_write_header(int(type), nx, ny, nz, maxbits, buf, 24, ctypes.byref(bits)),
+           "write_header")
+    return buf.raw[: (bits.value + 7) // 8], int(bits.value)
+
+
+def read_header(buf: Any) -> dict:
+    """Parse the header at the start of a host buffer (bytes, numpy array)
+    or a CUDA tensor: {'type', 'shape', 'dtype', 'maxbits', 'bits'}."""
+    if hasattr(buf, "data_ptr") and getattr(buf, "is_cuda", False):
+        buf = buf[: 3 * 8 // buf.element_size()].cpu().numpy()
+    if isinstance(buf, (bytes, bytearray)):
+        raw = bytes(buf)
+    else:
+        import numpy as np
+        raw = np.ascontiguousarray(buf).view(np.uint8).tobytes()
+    c = ctypes.create_string_buffer(raw, len(raw))
+    t, nx, ny, nz, mb, bits = _I(0), _U(0), _U(0), _U(0), _U(0), _SZ(0)
+    _check(_lib.gzfp_read_header(c, len(raw), ctypes.byref(t), ctypes.byref(nx), ctypes.byref(ny),
+                                 ctypes.byref(nz), ctypes.byref(mb), ctypes.byref(bits)),
+           "read_header")
+    zt = zfp_type(t.value)
+    return {"type": zt, "shape": tuple(v for v in (nz.value, ny.value, nx.value) if v),
+            "dtype": _DTYPE_NAME[zt], "maxbits": int(mb.value), "bits": int(bits.value)}
+
+
+def headed_size(type: zfp_type, nx: int, ny: int, nz: int, maxbits: int) -> int:
+    """Exact bytes of a headed fixed-rate stream."""
+    _, hb = write_header(type, nx, ny, nz, maxbits)
+    blocks = 1
+    for n in (nx, ny, nz):
+        blocks *= (n + 3) // 4 if n else 1
+    return (hb + blocks * maxbits + 63) // 64 * 8
+
+
+def compress_headed(x, rate: float, out=None, cuda_stream: Any = None):
+    """Compress a contiguous CUDA tensor or numpy array (float32 / float64 /
+    int32 / int64, 1-3 dims) into a stream that starts with zfp's full
+    header.  Returns the uint64 words: a tensor on the same device, or a
+    numpy array for host input (``out`` if given)."""
+    t = _type_of(x.dtype)
+    nx, ny, nz = _dims_of(x.shape)
+    mb = int(_lib.gzfp_rate_to_maxbits(int(t), len(x.shape), float(rate)))
+    if mb == 0:
+        raise GzfpError(GZFP_ERR_ARG, "bad type or rate")
+    nbytes = headed_size(t, nx, ny, nz, mb)
+    if out is None:
+        if hasattr(x, "data_ptr"):
+            import torch
+            out = torch.empty(nbytes // 8, dtype=torch.int64, device=x.device)
+        else:
+            import numpy as np
+            out = np.empty(nbytes // 8, np.uint64)
+    src, _ = _addr_and_size(x)
+    dst, cap = _addr_and_size(out)
+    got = _SZ(0)
+    _check(_lib.gzfp_compress_headed(int(t), nx, ny, nz, float(rate), src, dst, cap,
+                                     ctypes.byref(got), _cuda_stream_handle(cuda_stream)),
+           "compress_headed")
+    return out
+
+
+def decompress_headed(words, out=None, cuda_stream: Any = None):
+    """Decompress a headed stream; type and shape come from its header.  The
+    result lands in ``out`` when given, else in a new tensor on the stream's
+    device (numpy array for a host stream)."""
+    h = read_header(words)
+    if out is None:
+        if hasattr(words, "data_ptr"):
+            import torch
+            out = torch.empty(h["shape"], dtype=getattr(torch, h["dtype"]), device=words.device)
+        else:
+            import numpy as np
+            out = np.empty(h["shape"], h["dtype"])
+    src, size = _addr_and_size(words)
+    dst, cap = _addr_and_size(out)
+    _check(_lib.gzfp_decompress_headed(src, size, dst, cap, _cuda_stream_handle(cuda_stream)),
+           "decompress_headed")
     return out
 
 

@@ -441,16 +441,25 @@ void stride_span(const gzfp::Geom& g, long long& lo, long long& hi) {
   }
 }
 
+// One call on a field with element strides (0 = contiguous along that axis),
+// everything staged at once.  `base` is the stream bit of block 0: a headed
+// stream's header length, whose `header` words the encoder writes in front
+// of the blocks.
 int strided_call(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
                  long long sy, long long sz, unsigned maxbits, void* field, uint64_t* words,
-                 size_t words_bytes, size_t* out_bytes, void* cuda_stream) {
+                 size_t words_bytes, size_t* out_bytes, void* cuda_stream, uint64_t base = 0,
+                 const uint64_t* header = nullptr, unsigned header_words = 0) {
   clear_error();
   gzfp::Geom g;
   int dims;
   int st = check_common(type, nx, ny, nz, maxbits, g, dims);
   if (st) return st;
   if (!field || !words) return fail(GZFP_ERR_ARG, "null pointer");
-  const uint64_t nwords = stream_words(g, maxbits);
+  g.base = base;
+  const uint64_t nwords = (base + g.nblocks * maxbits + 63) / 64;
+  // blocks share boundary words (with each other or with the header): the
+  // encoder ORs those into a zeroed stream
+  const bool shared_words = maxbits % 64 || base % 64;
   const size_t need = (size_t)(nwords * 8);
   if (words_bytes < need)
     return fail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY,
@@ -464,8 +473,11 @@ int strided_call(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, l
   cudaError_t e;
   if (dev_field && dev_words) {
     set_strides(g, dims, type, field, sx, sy, sz);
-    if (!decode && maxbits % 64 && (e = cudaMemsetAsync(words, 0, need, s)))
+    if (!decode && shared_words && (e = cudaMemsetAsync(words, 0, need, s)))
       return cuda_fail(e, "cudaMemsetAsync(stream)");
+    if (!decode && header &&
+        (e = cudaMemcpyAsync(words, header, header_words * 8, cudaMemcpyHostToDevice, s)))
+      return cuda_fail(e, "cudaMemcpyAsync(header H2D)");
     e = decode ? decode_launch(type, dims, words, nwords, g, maxbits, field, s)
                : encode_launch(type, dims, field, g, maxbits, words, nwords, s);
     return e ? cuda_fail(e, decode ? "decode kernel launch" : "encode kernel launch") : GZFP_OK;
@@ -499,8 +511,11 @@ int strided_call(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, l
   if (!st && decode && !dev_words &&
       (e = cudaMemcpyAsync(dwords, words, need, cudaMemcpyHostToDevice, s)))
     st = cuda_fail(e, "cudaMemcpyAsync(stream H2D)");
-  if (!st && !decode && maxbits % 64 && (e = cudaMemsetAsync(dwords, 0, need, s)))
+  if (!st && !decode && shared_words && (e = cudaMemsetAsync(dwords, 0, need, s)))
     st = cuda_fail(e, "cudaMemsetAsync(stream)");
+  if (!st && !decode && header &&
+      (e = cudaMemcpyAsync(dwords, header, header_words * 8, cudaMemcpyHostToDevice, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(header H2D)");
   if (!st) {
     e = decode ? decode_launch(type, dims, dwords, nwords, g, maxbits, dfield, s)
                : encode_launch(type, dims, dfield, g, maxbits, dwords, nwords, s);
@@ -556,6 +571,213 @@ int gzfp_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate
   unsigned maxbits = gzfp_rate_to_maxbits(type, (unsigned)dims, rate);
   if (!maxbits) return fail(GZFP_ERR_ARG, "bad type or rate");
   return gzfp_decompress_bits(type, nx, ny, nz, maxbits, stream, bytes, data, cuda_stream);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ headers
+// zfp 0.5.0's full header (zfp_write_header / zfp_read_header with
+// ZFP_HEADER_FULL, Z/src/zfp.c:661-719), for the parameters
+// zfp_stream_set_rate leaves (Z/src/zfp.c:405-430): minbits = maxbits,
+// maxprec = the type's precision, minexp = ZFP_MIN_EXP.
+namespace {
+
+constexpr unsigned kMagicBits = 32, kMetaBits = 52, kModeShortBits = 12, kModeLongBits = 64;
+constexpr uint64_t kModeShortMax = (1u << kModeShortBits) - 2;  // ZFP_MODE_SHORT_MAX
+constexpr int kMinExp = -1074;                                    // ZFP_MIN_EXP
+constexpr int kMinExpBias = 16495;  // minexp offset of the long mode form
+constexpr unsigned kHeaderMaxBits = 1u << 15;  // largest maxbits the long form records
+
+// up to 192 bits, LSB first in 64-bit words (the stream's own layout)
+struct HeaderWords {
+  uint64_t w[3] = {0, 0, 0};
+  unsigned n = 0;
+  void put(uint64_t v, unsigned bits) {  // bits <= 64
+    if (bits < 64) v &= (1ull << bits) - 1;
+    const unsigned i = n >> 6, o = n & 63;
+    w[i] |= v << o;
+    if (o && o + bits > 64) w[i + 1] |= v >> (64 - o);
+    n += bits;
+  }
+  uint64_t get(unsigned& pos, unsigned bits) const {  // bits <= 64
+    const unsigned i = pos >> 6, o = pos & 63;
+    uint64_t v = w[i] >> o;
+    if (o && o + bits > 64) v |= w[i + 1] << (64 - o);
+    pos += bits;
+    return bits < 64 ? v & ((1ull << bits) - 1) : v;
+  }
+};
+
+unsigned type_precision(int type) {
+  return type == GZFP_TYPE_FLOAT || type == GZFP_TYPE_INT32 ? 32 : 64;
+}
+
+// Field sizes a header records: 48 bits of nx - 1 in 1D, 24 bits per axis
+// in 2D, 16 bits per axis in 3D (zfp_field_metadata, Z/src/zfp.c:158-182).
+bool header_sizes_fit(int dims, unsigned nx, unsigned ny, unsigned nz) {
+  if (dims == 2) return nx <= (1u << 24) && ny <= (1u << 24);
+  if (dims == 3) return nx <= (1u << 16) && ny <= (1u << 16) && nz <= (1u << 16);
+  return true;
+}
+
+int build_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                 HeaderWords& h) {
+  gzfp::Geom g;
+  int dims;
+  int st = check_common(type, nx, ny, nz, maxbits, g, dims);
+  if (st) return st;
+  if (!header_sizes_fit(dims, nx, ny, nz))
+    return fail(GZFP_ERR_ARG, "field sizes beyond what a zfp header records");
+  if (maxbits > kHeaderMaxBits) return fail(GZFP_ERR_ARG, "bits per block beyond what a zfp header records");
+  h.put('z', 8);
+  h.put('f', 8);
+  h.put('p', 8);
+  h.put(5, 8);  // ZFP_VERSION >> 4 for 0.5.0
+  uint64_t meta = dims == 1   ? (uint64_t)(nx - 1)
+                  : dims == 2 ? ((uint64_t)(ny - 1) << 24) | (nx - 1)
+                              : ((((uint64_t)(nz - 1) << 16) | (ny - 1)) << 16) | (nx - 1);
+  meta = (meta << 4) | ((uint64_t)(dims - 1) << 2) | (uint64_t)(type - 1);
+  h.put(meta, kMetaBits);
+  const unsigned prec = type_precision(type);
+  if (prec >= 64 && maxbits <= 2048) {
+    h.put(maxbits - 1, kModeShortBits);  // the 12-bit fixed-rate form
+  } else {
+    // each parameter on its own: minexp, maxprec - 1, maxbits - 1, minbits - 1, 0xfff
+    uint64_t mode = (uint64_t)(kMinExp + kMinExpBias);
+    mode = (mode << 7) | (prec - 1);
+    mode = (mode << 15) | (maxbits - 1);
+    mode = (mode << 15) | (maxbits - 1);
+    mode = (mode << 12) | 0xfff;
+    h.put(mode, kModeLongBits);
+  }
+  return GZFP_OK;
+}
+
+int parse_header(const HeaderWords& h, size_t avail_bits, int* type, unsigned* nx, unsigned* ny,
+                 unsigned* nz, unsigned* maxbits, size_t* header_bits) {
+  if (avail_bits < kMagicBits + kMetaBits + kModeShortBits)
+    return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
+  unsigned pos = 0;
+  if (h.get(pos, 8) != 'z' || h.get(pos, 8) != 'f' || h.get(pos, 8) != 'p' || h.get(pos, 8) != 5)
+    return fail(GZFP_ERR_ARG, "no zfp 0.5.0 header (magic mismatch)");
+  uint64_t meta = h.get(pos, kMetaBits);
+  const int t = (int)(meta & 3) + 1;
+  const int dims = (int)((meta >> 2) & 3) + 1;
+  meta >>= 4;
+  unsigned x, y = 0, z = 0;
+  if (dims == 1) {
+    const uint64_t n = (meta & 0xffffffffffffull) + 1;
+    if (n > 0xffffffffull) return fail(GZFP_ERR_UNSUPPORTED, "1D field of 2^32 values or more");
+    x = (unsigned)n;
+  } else if (dims == 2) {
+    x = (unsigned)(meta & 0xffffff) + 1;
+    y = (unsigned)((meta >> 24) & 0xffffff) + 1;
+  } else if (dims == 3) {
+    x = (unsigned)(meta & 0xffff) + 1;
+    y = (unsigned)((meta >> 16) & 0xffff) + 1;
+    z = (unsigned)((meta >> 32) & 0xffff) + 1;
+  } else {
+    return fail(GZFP_ERR_UNSUPPORTED, "4D field (not part of zfp 0.5.0)");
+  }
+  uint64_t mode = h.get(pos, kModeShortBits);
+  unsigned mb;
+  if (mode <= kModeShortMax) {
+    if (mode >= 2048)
+      return fail(GZFP_ERR_UNSUPPORTED, "fixed-precision or fixed-accuracy stream (fixed rate only)");
+    mb = (unsigned)mode + 1;
+  } else {
+    if (avail_bits < kMagicBits + kMetaBits + kModeLongBits)
+      return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
+    mode |= h.get(pos, kModeLongBits - kModeShortBits) << kModeShortBits;
+    const unsigned minbits = (unsigned)((mode >> 12) & 0x7fff) + 1;
+    mb = (unsigned)((mode >> 27) & 0x7fff) + 1;
+    const unsigned maxprec = (unsigned)((mode >> 42) & 0x7f) + 1;
+    const int minexp = (int)((mode >> 49) & 0x7fff) - kMinExpBias;
+    // zfp_stream_set_rate's parameters; anything else codes blocks differently
+    if (minbits != mb || maxprec < type_precision(t) || minexp != kMinExp)
+      return fail(GZFP_ERR_UNSUPPORTED, "stream in a mode other than fixed rate");
+  }
+  if (mb < (unsigned)ebits_of(t) + 1)
+    return fail(GZFP_ERR_UNSUPPORTED, "fewer bits per block than the block header");
+  *type = t;
+  *nx = x;
+  *ny = y;
+  *nz = z;
+  *maxbits = mb;
+  *header_bits = pos;
+  return GZFP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gzfp_write_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                      void* header, size_t capacity, size_t* header_bits) {
+  clear_error();
+  HeaderWords h;
+  int st = build_header(type, nx, ny, nz, maxbits, h);
+  if (st) return st;
+  if (!header) return fail(GZFP_ERR_ARG, "null pointer");
+  const size_t bytes = (h.n + 7) / 8;
+  if (capacity < bytes) return fail(GZFP_ERR_CAPACITY, "header buffer too small");
+  memcpy(header, h.w, bytes);
+  if (header_bits) *header_bits = h.n;
+  return GZFP_OK;
+}
+
+int gzfp_read_header(const void* header, size_t bytes, int* type, unsigned* nx, unsigned* ny,
+                     unsigned* nz, unsigned* maxbits, size_t* header_bits) {
+  clear_error();
+  if (!header || !type || !nx || !ny || !nz || !maxbits || !header_bits)
+    return fail(GZFP_ERR_ARG, "null pointer");
+  HeaderWords h;
+  memcpy(h.w, header, bytes < sizeof h.w ? bytes : sizeof h.w);
+  return parse_header(h, bytes * 8, type, nx, ny, nz, maxbits, header_bits);
+}
+
+int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                         const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                         void* cuda_stream) {
+  clear_error();
+  gzfp::Geom g;
+  int dims;
+  if (!make_geom(nx, ny, nz, g, dims)) return fail(GZFP_ERR_ARG, "bad dimensions");
+  const unsigned maxbits = gzfp_rate_to_maxbits(type, (unsigned)dims, rate);
+  if (!maxbits) return fail(GZFP_ERR_ARG, "bad type or rate");
+  HeaderWords h;
+  int st = build_header(type, nx, ny, nz, maxbits, h);
+  if (st) return st;
+  return strided_call(false, type, nx, ny, nz, 0, 0, 0, maxbits, (void*)data, (uint64_t*)stream,
+                      capacity, out_bytes, cuda_stream, h.n, h.w, (h.n + 63) / 64);
+}
+
+int gzfp_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes,
+                           void* cuda_stream) {
+  clear_error();
+  if (!stream || !data) return fail(GZFP_ERR_ARG, "null pointer");
+  HeaderWords h;
+  const size_t hb = bytes < sizeof h.w ? bytes : sizeof h.w;
+  cudaError_t e;
+  if (is_device_pointer(stream)) {
+    // the header is parsed on the host: wait for work queued before this call
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    if ((e = cudaMemcpyAsync(h.w, stream, hb, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return cuda_fail(e, "cudaMemcpyAsync(header D2H)");
+  } else {
+    memcpy(h.w, stream, hb);
+  }
+  int type;
+  unsigned nx, ny, nz, maxbits;
+  size_t header_bits;
+  int st = parse_header(h, bytes * 8, &type, &nx, &ny, &nz, &maxbits, &header_bits);
+  if (st) return st;
+  const uint64_t values = (uint64_t)nx * (ny ? ny : 1) * (nz ? nz : 1);
+  if (data_bytes < values * scalar_size(type))
+    return fail(GZFP_ERR_CAPACITY, "output buffer smaller than the field in the header");
+  return strided_call(true, type, nx, ny, nz, 0, 0, 0, maxbits, data, (uint64_t*)stream, bytes,
+                      nullptr, cuda_stream, header_bits);
 }
 
 }  // extern "C"

@@ -43,6 +43,7 @@ struct Geom {
   uint32_t bx, by, bz;  // blocks per axis
   uint64_t nblocks;
   int64_t sx, sy, sz;   // element strides
+  uint64_t base;        // stream bit of block 0 (after a header; 0 without)
   uint32_t vec;  // rows of full blocks may be moved as one 16/32-byte vector
   FastDiv dbx, dby;
 };
@@ -59,6 +60,7 @@ GZ_HD Geom make_geom_blocks(uint32_t nx, uint32_t ny, uint32_t nz) {
   g.sx = 1;
   g.sy = nx;
   g.sz = (int64_t)nx * ny;
+  g.base = 0;
   g.vec = 0;
   g.dbx = make_fastdiv(g.bx);
   g.dby = make_fastdiv(g.by);
@@ -302,7 +304,7 @@ GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, 
   block_coords(g, b, ix, iy, iz);
   UInt raw[BS];
   gather<D, T>(in, g, ix, iy, iz, raw);
-  BitWriter<Words> w(words, b * (uint64_t)maxbits, maxbits);
+  BitWriter<Words> w(words, g.base + b * (uint64_t)maxbits, maxbits);
   encode_block<D, T>(raw, maxbits, w, ps);
   w.finish();
 }
@@ -313,7 +315,7 @@ GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words
   constexpr int BS = 1 << (2 * D);
   uint32_t ix, iy, iz;
   block_coords(g, b, ix, iy, iz);
-  BitReader<Words> r(words, b * (uint64_t)maxbits);
+  BitReader<Words> r(words, g.base + b * (uint64_t)maxbits);
   UInt raw[BS];
   decode_block<D, T>(r, maxbits, raw, ps);
   scatter<D, T>(out, g, ix, iy, iz, raw);

@@ -165,7 +165,7 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
                             T* out, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords;
+  const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords && g.base == 0;
   const size_t sm = smem_bytes(32, staged, maxbits >> 6);
   constexpr int MB = MinBlocks<D, T>::value;
   auto k = !staged ? decode_kernel<D, T, false, MB>

@@ -112,6 +112,38 @@ int gzfp_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, lon
                             long long sy, long long sz, unsigned maxbits, const void* stream,
                             size_t bytes, void* data, void* cuda_stream);
 
+/* ------------------------------------------------------------ headers ---
+   zfp 0.5.0's self-describing stream header (zfp_write_header /
+   zfp_read_header with ZFP_HEADER_FULL, zfp-0.5.0/src/zfp.c:661-719): a
+   32-bit magic ('z', 'f', 'p', codec 5), 52 bits of field metadata (scalar
+   type, dimensionality and sizes: up to 2^32 - 1 values in 1D, 2^24 per
+   axis in 2D, 2^16 per axis in 3D) and the fixed-rate mode in 12 bits
+   (blocks up to 2048 bits) or 64 bits (up to 32768).  zfp_compress after
+   zfp_write_header continues the same bit stream, so the first block starts
+   right after the header: the stream zfp's command-line tool writes with -h.
+   No counterpart in cuZFP, whose streams carry no header. */
+#define GZFP_HEADER_MAX_BITS 148
+
+/* Write the header into the host buffer `header` (capacity bytes; 24 are
+   always enough); *header_bits receives its length in bits. */
+int gzfp_write_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                      void* header, size_t capacity, size_t* header_bits);
+
+/* Parse a header from the host buffer `header`.  Streams in zfp's other
+   modes (fixed precision or accuracy, expert parameters) are reported with
+   GZFP_ERR_UNSUPPORTED. */
+int gzfp_read_header(const void* header, size_t bytes, int* type, unsigned* nx, unsigned* ny,
+                     unsigned* nz, unsigned* maxbits, size_t* header_bits);
+
+/* Compress with a header in front, or decompress a stream that has one
+   (the field's type and shape come from the header; `data_bytes` is the
+   capacity of `data`).  Pointers may be host or device memory. */
+int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                         const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                         void* cuda_stream);
+int gzfp_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes,
+                           void* cuda_stream);
+
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and
    bits per block -- coded by one persistent kernel over a device-side work

@@ -71,6 +71,18 @@ def port() -> ctypes.CDLL:
         lib.gzo_decompress_strided.restype = ctypes.c_int
         lib.gzo_decompress_strided.argtypes = _L + [ctypes.c_void_p, ctypes.c_size_t,
                                                     ctypes.c_void_p, ctypes.c_int]
+        lib.gzo_header_bits.restype = ctypes.c_uint
+        lib.gzo_header_bits.argtypes = _A
+        lib.gzo_compress_headed.restype = ctypes.c_size_t
+        lib.gzo_compress_headed.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        _P = ctypes.POINTER
+        lib.gzo_read_header.restype = ctypes.c_long
+        lib.gzo_read_header.argtypes = [ctypes.c_void_p, ctypes.c_size_t, _P(ctypes.c_int),
+                                        _P(ctypes.c_uint), _P(ctypes.c_uint), _P(ctypes.c_uint),
+                                        _P(ctypes.c_uint)]
+        lib.gzo_decompress_headed.restype = ctypes.c_int
+        lib.gzo_decompress_headed.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                              ctypes.c_size_t]
         _port = lib
     return _port
 
@@ -104,6 +116,20 @@ def ref() -> ctypes.CDLL:
         lib.zref_decompress_int.restype = ctypes.c_int
         lib.zref_decompress_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t,
                                                  ctypes.c_void_p]
+        lib.zref_compress_headed.restype = ctypes.c_size_t
+        lib.zref_compress_headed.argtypes = _A + [ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_size_t]
+        _P = ctypes.POINTER
+        lib.zref_read_header.restype = ctypes.c_size_t
+        lib.zref_read_header.argtypes = [ctypes.c_void_p, ctypes.c_size_t, _P(ctypes.c_int),
+                                         _P(ctypes.c_uint), _P(ctypes.c_uint), _P(ctypes.c_uint),
+                                         _P(ctypes.c_uint), _P(ctypes.c_uint), _P(ctypes.c_uint),
+                                         _P(ctypes.c_int)]
+        lib.zref_decompress_headed.restype = ctypes.c_int
+        lib.zref_decompress_headed.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        lib.zref_decompress_headed_int.restype = ctypes.c_int
+        lib.zref_decompress_headed_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t,
+                                                        ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -249,3 +275,100 @@ def ref_decompress_into(words: np.ndarray, v: np.ndarray, rate: float) -> None:
     (nx, ny, nz), (sx, sy, sz), addr = view_geometry(v)
     ref().zref_decompress_strided(type_code(v.dtype), nx, ny, nz, sx, sy, sz, float(rate),
                                   words.ctypes.data, words.nbytes, addr)
+
+
+# ----------------------------------------------------------- headed streams
+_DTYPE_OF = {INT32: np.int32, INT64: np.int64, FLOAT: np.float32, DOUBLE: np.float64}
+
+
+def _shape_of(nx: int, ny: int, nz: int) -> tuple:
+    return tuple(v for v in (nz, ny, nx) if v)
+
+
+def headed_bytes(shape, dtype, rate: float) -> int:
+    nx, ny, nz = dims3(shape)
+    hb = int(port().gzo_header_bits(type_code(dtype), nx, ny, nz, float(rate)))
+    mb = int(port().gzo_maxbits(type_code(dtype), len(tuple(shape)), float(rate)))
+    blocks = 1
+    for n in shape:
+        blocks *= (int(n) + 3) // 4
+    return (hb + blocks * mb + 63) // 64 * 8 if hb else 0
+
+
+def compress_headed(a: np.ndarray, rate: float) -> np.ndarray:
+    """Oracle stream with zfp's full header in front (uint64 words)."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    n = headed_bytes(a.shape, a.dtype, rate)
+    out = np.zeros(max(n // 8, 1), np.uint64)
+    got = port().gzo_compress_headed(type_code(a.dtype), nx, ny, nz, float(rate), a.ctypes.data,
+                                     out.ctypes.data, out.nbytes)
+    if not n or got != n:
+        raise RuntimeError("oracle headed compress failed")
+    return out[: n // 8]
+
+
+def read_header(buf) -> dict:
+    """Parse a header: {'bits', 'dtype', 'shape', 'maxbits'}; bits is 0 for
+    no header and -1 for a stream in a mode other than fixed rate."""
+    b = np.ascontiguousarray(buf).view(np.uint8)
+    t, nx, ny, nz, mb = (ctypes.c_int(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(),
+                         ctypes.c_uint())
+    bits = port().gzo_read_header(b.ctypes.data, b.nbytes, ctypes.byref(t), ctypes.byref(nx),
+                                  ctypes.byref(ny), ctypes.byref(nz), ctypes.byref(mb))
+    if bits <= 0:
+        return {"bits": int(bits)}
+    return {"bits": int(bits), "dtype": np.dtype(_DTYPE_OF[t.value]),
+            "shape": _shape_of(nx.value, ny.value, nz.value), "maxbits": int(mb.value)}
+
+
+def decompress_headed(words: np.ndarray) -> np.ndarray:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    h = read_header(words)
+    if h["bits"] <= 0:
+        raise RuntimeError("oracle: no fixed-rate zfp header")
+    out = np.zeros(h["shape"], h["dtype"])
+    if not port().gzo_decompress_headed(words.ctypes.data, words.nbytes, out.ctypes.data,
+                                        out.nbytes):
+        raise RuntimeError("oracle headed decompress failed")
+    return out
+
+
+def ref_compress_headed(a: np.ndarray, rate: float) -> np.ndarray:
+    """zfp_write_header(ZFP_HEADER_FULL) + zfp_compress of the reference's
+    own build (integer arrays: header + its per-block integer API)."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    t = type_code(a.dtype)
+    cap = int(ref().zref_maximum_size(t, nx, ny, nz, float(rate)))
+    cap = max(cap, headed_bytes(a.shape, a.dtype, rate))
+    buf = np.zeros(cap // 8 + 1, np.uint64)
+    n = ref().zref_compress_headed(t, nx, ny, nz, float(rate), a.ctypes.data, buf.ctypes.data,
+                                   buf.nbytes)
+    if not n:
+        raise RuntimeError("reference headed compress failed")
+    return buf[: n // 8]
+
+
+def ref_read_header(buf) -> dict:
+    b = np.ascontiguousarray(buf).view(np.uint8)
+    c = [ctypes.c_int(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(),
+         ctypes.c_uint(), ctypes.c_uint(), ctypes.c_int()]
+    bits = ref().zref_read_header(b.ctypes.data, b.nbytes, *[ctypes.byref(v) for v in c])
+    t, nx, ny, nz, minbits, maxbits, maxprec, minexp = [v.value for v in c]
+    return {"bits": int(bits), "type": t, "nx": nx, "ny": ny, "nz": nz, "minbits": minbits,
+            "maxbits": maxbits, "maxprec": maxprec, "minexp": minexp}
+
+
+def ref_decompress_headed(words: np.ndarray, shape, dtype, rate: float) -> np.ndarray:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    out = np.zeros(tuple(shape), dtype)
+    if is_int(dtype):
+        nx, ny, nz = dims3(shape)
+        ok = ref().zref_decompress_headed_int(type_code(dtype), nx, ny, nz, float(rate),
+                                              words.ctypes.data, words.nbytes, out.ctypes.data)
+    else:
+        ok = ref().zref_decompress_headed(words.ctypes.data, words.nbytes, out.ctypes.data)
+    if not ok:
+        raise RuntimeError("reference headed decompress failed")
+    return out

@@ -123,7 +123,7 @@ static void int_block_codec(zfp_stream* zfp, int type, int dims, void* blk, int 
 }
 
 static size_t int_array(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
-                        void* data, void* buffer, size_t capacity, int encode) {
+                        void* data, void* buffer, size_t capacity, int encode, int headed) {
   const int dims = nz ? 3 : ny ? 2 : 1;
   const unsigned NY = ny ? ny : 1, NZ = nz ? nz : 1;
   if ((type != zfp_type_int32 && type != zfp_type_int64) || nx % 4 ||
@@ -132,14 +132,23 @@ static size_t int_array(int type, unsigned nx, unsigned ny, unsigned nz, double 
   zfp_stream* zfp = zfp_stream_open(NULL);
   zfp_stream_set_rate(zfp, rate, (zfp_type)type, (uint)dims, 0);
   const size_t blocks = (size_t)(nx / 4) * (dims >= 2 ? NY / 4 : 1) * (dims == 3 ? NZ / 4 : 1);
-  const size_t bytes = (blocks * zfp->maxbits + 63) / 64 * 8;
-  if (bytes > capacity) {
-    zfp_stream_close(zfp);
-    return 0;
-  }
+  size_t hbits = 0;
   bitstream* s = stream_open(buffer, capacity);
   zfp_stream_set_bit_stream(zfp, s);
   zfp_stream_rewind(zfp);
+  if (headed && capacity >= 3 * sizeof(uint64)) {
+    /* the header of the field this array is, then its blocks */
+    zfp_field* f = make_field(type, nx, ny, nz, data);
+    hbits = encode ? zfp_write_header(zfp, f, ZFP_HEADER_FULL)
+                   : zfp_read_header(zfp, f, ZFP_HEADER_FULL);
+    zfp_field_free(f);
+  }
+  const size_t bytes = (hbits + blocks * zfp->maxbits + 63) / 64 * 8;
+  if (bytes > capacity || (headed && !hbits)) {
+    stream_close(s);
+    zfp_stream_close(zfp);
+    return 0;
+  }
   int64 blk[64];
   unsigned bx, by, bz;
   for (bz = 0; bz < (dims == 3 ? NZ / 4 : 1); bz++)
@@ -150,19 +159,20 @@ static size_t int_array(int type, unsigned nx, unsigned ny, unsigned nz, double 
         if (!encode) int_block_io(type, dims, nx, NY, NZ, bx, by, bz, data, blk, 0);
       }
   if (encode) stream_flush(s);
+  const size_t used = encode ? stream_size(s) : bytes;
   stream_close(s);
   zfp_stream_close(zfp);
-  return bytes;
+  return used;
 }
 
 size_t zref_compress_int(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
                          const void* data, void* buffer, size_t capacity) {
-  return int_array(type, nx, ny, nz, rate, (void*)data, buffer, capacity, 1);
+  return int_array(type, nx, ny, nz, rate, (void*)data, buffer, capacity, 1, 0);
 }
 
 int zref_decompress_int(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
                         const void* buffer, size_t bytes, void* out) {
-  return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0) != 0;
+  return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0, 0) != 0;
 }
 
 /* Strided fields through zfp_field_set_stride_<d> (Z/src/zfp.c:230-252):
@@ -208,4 +218,75 @@ int zref_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, int
   zfp_stream_close(zfp);
   zfp_field_free(field);
   return ok;
+}
+
+/* Headed streams, the sequence of zfp's command-line tool with -h
+   (Z/utils/zfp.c:378-427): zfp_write_header(ZFP_HEADER_FULL) and then
+   zfp_compress on the same bit stream, so the first block follows the
+   header bits directly; zfp_read_header then zfp_decompress to read one
+   back.  Integer arrays take the per-block path above after the header. */
+size_t zref_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                            const void* data, void* buffer, size_t capacity) {
+  if (type == zfp_type_int32 || type == zfp_type_int64)
+    return int_array(type, nx, ny, nz, rate, (void*)data, buffer, capacity, 1, 1);
+  zfp_field* field = make_field(type, nx, ny, nz, (void*)data);
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_rate(zfp, rate, (zfp_type)type, zfp_field_dimensionality(field), 0);
+  size_t bytes = 0;
+  if (zfp_stream_maximum_size(zfp, field) <= capacity) {
+    bitstream* s = stream_open(buffer, capacity);
+    zfp_stream_set_bit_stream(zfp, s);
+    zfp_stream_rewind(zfp);
+    if (zfp_write_header(zfp, field, ZFP_HEADER_FULL)) bytes = zfp_compress(zfp, field);
+    stream_close(s);
+  }
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return bytes;
+}
+
+/* Parse a header with zfp_read_header; returns its bits (0 if zfp rejects
+   it) and the field and mode it records. */
+size_t zref_read_header(const void* buffer, size_t bytes, int* type, unsigned* nx, unsigned* ny,
+                        unsigned* nz, unsigned* minbits, unsigned* maxbits, unsigned* maxprec,
+                        int* minexp) {
+  zfp_field* field = zfp_field_alloc();
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  bitstream* s = stream_open((void*)buffer, bytes);
+  zfp_stream_set_bit_stream(zfp, s);
+  zfp_stream_rewind(zfp);
+  size_t bits = zfp_read_header(zfp, field, ZFP_HEADER_FULL);
+  *type = (int)field->type;
+  *nx = field->nx;
+  *ny = field->ny;
+  *nz = field->nz;
+  zfp_stream_params(zfp, minbits, maxbits, maxprec, minexp);
+  stream_close(s);
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return bits;
+}
+
+/* zfp_read_header, then zfp_decompress into `out` (float and double) */
+int zref_decompress_headed(const void* buffer, size_t bytes, void* out) {
+  zfp_field* field = zfp_field_alloc();
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  bitstream* s = stream_open((void*)buffer, bytes);
+  zfp_stream_set_bit_stream(zfp, s);
+  zfp_stream_rewind(zfp);
+  int ok = 0;
+  if (zfp_read_header(zfp, field, ZFP_HEADER_FULL)) {
+    zfp_field_set_pointer(field, out);
+    ok = zfp_decompress(zfp, field);
+  }
+  stream_close(s);
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return ok;
+}
+
+/* Integer arrays of the given sizes: zfp_read_header, then the blocks */
+int zref_decompress_headed_int(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                               const void* buffer, size_t bytes, void* out) {
+  return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0, 1) != 0;
 }

@@ -25,6 +25,10 @@
  *                                   Z/src/template/decompress.c
  *   bit stream (LSB-first u64)      Z/src/inline/bitstream.c:195-373
  *   stream_flush / returned size    Z/src/zfp.c:603-630
+ *   full header (magic, field       Z/src/zfp.c:661-719, zfp_field_metadata
+ *   metadata, mode)                 :158-182, zfp_field_set_metadata
+ *                                   :254-275, zfp_stream_mode :305-345,
+ *                                   zfp_stream_set_mode :461-498
  *   int32 / int64 blocks            Z/src/template/encode.c:154-185 (no
  *                                   exponent, whole budget, maxprec 64),
  *                                   decode.c:116-135; zfp 0.5.0 codes them
@@ -239,7 +243,9 @@ unsigned gzo_maxbits(int type, int dims, double rate) {
   return bits < lo ? lo : bits;
 }
 
-static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
+/* geometry and codec constants for `maxbits` bits per block */
+static int setup_bits(params* p, int type, unsigned nx, unsigned ny, unsigned nz,
+                      unsigned maxbits) {
   if (type != GZO_FLOAT && type != GZO_DOUBLE && !GZO_IS_INT(type)) return 0;
   if (nx == 0) return 0;
   p->dims = nz ? 3 : ny ? 2 : 1;
@@ -247,7 +253,7 @@ static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, dou
   p->type = type;
   p->nx = nx; p->ny = ny ? ny : 1; p->nz = nz ? nz : 1;
   p->bx = (p->nx + 3) / 4; p->by = (p->ny + 3) / 4; p->bz = (p->nz + 3) / 4;
-  p->maxbits = gzo_maxbits(type, p->dims, rate);
+  p->maxbits = maxbits;
   if (p->maxbits == 0) return 0;
   p->P = type == GZO_FLOAT || type == GZO_INT32 ? 32 : 64;
   /* integer blocks carry no exponent (Z/src/template/encode.c:176-185) */
@@ -257,6 +263,10 @@ static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, dou
   p->sy = p->nx;
   p->sz = (long long)p->nx * p->ny;
   return 1;
+}
+
+static int setup(params* p, int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
+  return setup_bits(p, type, nx, ny, nz, gzo_maxbits(type, nz ? 3 : ny ? 2 : 1, rate));
 }
 
 static size_t scalar_bytes(const params* p) { return p->P == 32 ? 4 : 8; }
@@ -686,5 +696,175 @@ int gzo_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long
   proto.out = data;
   proto.istream = (const uint64_t*)stream;
   run_jobs(&p, &proto, (uint64_t)p.bx * p.by * p.bz, nthreads, decode_range);
+  return 1;
+}
+
+/* ---------------------------------------------------------------- header --- */
+
+/* zfp_write_header(zfp, field, ZFP_HEADER_FULL) for the parameters that
+   zfp_stream_set_rate sets (minbits = maxbits, maxprec = the type's
+   precision, minexp = ZFP_MIN_EXP): 'z' 'f' 'p' and ZFP_VERSION >> 4 in 8
+   bits each; 52 bits of metadata (sizes minus one -- 48 bits in 1D, 24 per
+   axis in 2D, 16 per axis in 3D -- then dims - 1 and type - 1 in 2 bits
+   each); the mode in 12 bits (maxbits - 1) when maxprec reaches 64 and
+   maxbits <= 2048, otherwise 64 bits holding minexp + 16495 (15 bits),
+   maxprec - 1 (7), maxbits - 1 (15), minbits - 1 (15) and 0xfff (12).
+   Returns the header length in bits, or 0 for sizes or a rate the header
+   cannot record. */
+static unsigned header_put(wbits* w, const params* p) {
+  uint64_t meta, mode;
+  if (p->dims == 2 && (p->nx > (1u << 24) || p->ny > (1u << 24))) return 0;
+  if (p->dims == 3 && (p->nx > (1u << 16) || p->ny > (1u << 16) || p->nz > (1u << 16))) return 0;
+  if (p->maxbits > 0x8000u) return 0;
+  w_put(w, 'z', 8);
+  w_put(w, 'f', 8);
+  w_put(w, 'p', 8);
+  w_put(w, 0x05, 8);
+  if (p->dims == 1)
+    meta = p->nx - 1u;
+  else if (p->dims == 2)
+    meta = (uint64_t)(p->ny - 1u) << 24 | (p->nx - 1u);
+  else
+    meta = (uint64_t)(p->nz - 1u) << 32 | (uint64_t)(p->ny - 1u) << 16 | (p->nx - 1u);
+  meta = meta << 4 | (uint64_t)(p->dims - 1) << 2 | (uint64_t)(p->type - 1);
+  w_put(w, meta, 52);
+  if (p->P >= 64 && p->maxbits <= 2048) {
+    w_put(w, p->maxbits - 1u, 12);
+    return 32 + 52 + 12;
+  }
+  mode = (uint64_t)(GZO_MIN_EXP + 16495);
+  mode = mode << 7 | (uint64_t)(p->P - 1);
+  mode = mode << 15 | (uint64_t)(p->maxbits - 1);
+  mode = mode << 15 | (uint64_t)(p->maxbits - 1);
+  mode = mode << 12 | 0xfffu;
+  w_put(w, mode, 64);
+  return 32 + 52 + 64;
+}
+
+static size_t headed_bytes(const params* p, unsigned header_bits) {
+  uint64_t blocks = (uint64_t)p->bx * p->by * p->bz;
+  return (size_t)((header_bits + blocks * p->maxbits + 63) / 64 * 8);
+}
+
+/* Header bits a stream of this field and rate starts with (0 if none fits) */
+unsigned gzo_header_bits(int type, unsigned nx, unsigned ny, unsigned nz, double rate) {
+  params p;
+  uint64_t scratch[3];
+  wbits w;
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  w_init(&w, scratch, 0);
+  return header_put(&w, &p);
+}
+
+/* The header, then every block right after it, one thread (the blocks do
+   not start on word boundaries).  Returns the stream size in bytes. */
+size_t gzo_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                           const void* data, void* stream, size_t capacity) {
+  params p;
+  uint64_t scratch[3];
+  wbits w;
+  unsigned hb;
+  size_t bytes;
+  uint64_t b, nblocks;
+  double blk[64];
+  if (!setup(&p, type, nx, ny, nz, rate)) return 0;
+  w_init(&w, scratch, 0);
+  hb = header_put(&w, &p);
+  if (!hb) return 0;
+  bytes = headed_bytes(&p, hb);
+  if (capacity < bytes) return 0;
+  w_init(&w, (uint64_t*)stream, 0);
+  header_put(&w, &p);
+  nblocks = (uint64_t)p.bx * p.by * p.bz;
+  for (b = 0; b < nblocks; b++) {
+    unsigned bx = (unsigned)(b % p.bx);
+    unsigned by = (unsigned)((b / p.bx) % p.by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p.bx * p.by));
+    gather(&p, data, bx, by, bz, blk);
+    encode_block(&w, &p, blk);
+  }
+  w_flush(&w);
+  return bytes;
+}
+
+/* zfp_read_header(ZFP_HEADER_FULL): returns the header bits, 0 for a bad
+   magic or a short buffer, -1 for a stream in a mode other than the fixed
+   rate zfp_stream_set_rate sets.  ny = 0 (1D) and nz = 0 (1D, 2D) as in
+   the rest of this file's entry points. */
+long gzo_read_header(const void* stream, size_t bytes, int* type, unsigned* nx, unsigned* ny,
+                     unsigned* nz, unsigned* maxbits) {
+  uint64_t words[3] = {0, 0, 0};
+  rbits r;
+  uint64_t meta, mode;
+  int dims, t;
+  long bits = 32 + 52 + 12;
+  memcpy(words, stream, bytes < sizeof words ? bytes : sizeof words);
+  if (bytes * 8 < (size_t)bits) return 0;
+  r.words = words;
+  r.bit = 0;
+  if (r_get(&r, 8) != 'z' || r_get(&r, 8) != 'f' || r_get(&r, 8) != 'p' || r_get(&r, 8) != 0x05)
+    return 0;
+  meta = r_get(&r, 52);
+  t = (int)(meta & 3) + 1;
+  dims = (int)(meta >> 2 & 3) + 1;
+  meta >>= 4;
+  *ny = *nz = 0;
+  if (dims == 1) {
+    if ((meta & 0xffffffffffffull) >= 0xffffffffull) return -1;
+    *nx = (unsigned)(meta & 0xffffffffffffull) + 1u;
+  } else if (dims == 2) {
+    *nx = (unsigned)(meta & 0xffffff) + 1u;
+    *ny = (unsigned)(meta >> 24 & 0xffffff) + 1u;
+  } else if (dims == 3) {
+    *nx = (unsigned)(meta & 0xffff) + 1u;
+    *ny = (unsigned)(meta >> 16 & 0xffff) + 1u;
+    *nz = (unsigned)(meta >> 32 & 0xffff) + 1u;
+  } else {
+    return -1;
+  }
+  *type = t;
+  mode = r_get(&r, 12);
+  if (mode < 4095) {
+    if (mode >= 2048) return -1; /* fixed precision or fixed accuracy */
+    *maxbits = (unsigned)mode + 1u;
+  } else {
+    unsigned minbits, maxprec, P = t == GZO_FLOAT || t == GZO_INT32 ? 32u : 64u;
+    int minexp;
+    bits = 32 + 52 + 64;
+    if (bytes * 8 < (size_t)bits) return 0;
+    mode += r_get(&r, 52) << 12;
+    minbits = (unsigned)(mode >> 12 & 0x7fff) + 1u;
+    *maxbits = (unsigned)(mode >> 27 & 0x7fff) + 1u;
+    maxprec = (unsigned)(mode >> 42 & 0x7f) + 1u;
+    minexp = (int)(mode >> 49 & 0x7fff) - 16495;
+    if (minbits != *maxbits || maxprec < P || minexp != GZO_MIN_EXP) return -1;
+  }
+  return bits;
+}
+
+/* Decode a headed stream into `data` (capacity data_bytes); 1 on success */
+int gzo_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes) {
+  params p;
+  rbits r;
+  int type;
+  unsigned nx, ny, nz, maxbits;
+  uint64_t b, nblocks;
+  double blk[64];
+  long hb = gzo_read_header(stream, bytes, &type, &nx, &ny, &nz, &maxbits);
+  if (hb <= 0) return 0;
+  if (!setup_bits(&p, type, nx, ny, nz, maxbits)) return 0;
+  if (maxbits < 1u + (unsigned)p.ebits) return 0;
+  if (bytes < headed_bytes(&p, (unsigned)hb)) return 0;
+  if (data_bytes < (size_t)p.nx * p.ny * p.nz * scalar_bytes(&p)) return 0;
+  r.words = (const uint64_t*)stream;
+  r.bit = (size_t)hb;
+  nblocks = (uint64_t)p.bx * p.by * p.bz;
+  for (b = 0; b < nblocks; b++) {
+    unsigned bx = (unsigned)(b % p.bx);
+    unsigned by = (unsigned)((b / p.bx) % p.by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p.bx * p.by));
+    decode_block(&r, &p, blk);
+    scatter(&p, data, bx, by, bz, blk);
+  }
   return 1;
 }

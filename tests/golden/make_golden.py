@@ -1,9 +1,10 @@
 """Regenerate the golden fixtures from the reference's own zfp 0.5.0 build.
 
 Run in a checkout that has the reference tree (the build reads its zfp
-sources):  python tests/golden/make_golden.py [--ints]
-Writes tests/golden/small_cases.npz, tests/golden/manifest.json and
-tests/golden/int_cases.npz (only the last with --ints).
+sources):  python tests/golden/make_golden.py [--ints | --headed]
+Writes tests/golden/small_cases.npz, tests/golden/manifest.json,
+tests/golden/int_cases.npz and tests/golden/headed_cases.npz (only the
+integer or the headed cases with --ints / --headed).
 """
 from __future__ import annotations
 
@@ -116,9 +117,44 @@ def write_int_cases() -> None:
     print(f"{k} integer cases")
 
 
+def write_headed_cases() -> None:
+    """Streams with zfp's full header in front (zfp_write_header with
+    ZFP_HEADER_FULL, then zfp_compress on the same bit stream), one per
+    scalar type and dimensionality plus the 64-bit mode form for doubles
+    above 2048 bits per block, stored in full in tests/golden/headed_cases.npz."""
+    if not orc.build_ref():
+        raise SystemExit("reference tree not found; cannot regenerate golden fixtures")
+    rng = np.random.default_rng(20261205)
+    arrays = {}
+    k = 0
+    # integer arrays in whole blocks: the reference codes them block by block
+    plan = [(dt, shape, rate)
+            for dt in ("float32", "float64", "int32", "int64")
+            for shape, rate in (((204 if dt.startswith("int") else 203,), 9.5),
+                                ((20, 36), 6.0), ((12, 8, 16), 12.0))]
+    plan += [("float64", (37, 21), 160.0), ("float64", (150,), 600.0),
+             ("float32", (5, 6, 7), 3.0), ("float64", (9, 10, 11), 32.0)]
+    for dt, shape, rate in plan:
+        a = np.cumsum(rng.standard_normal(shape), axis=-1)
+        a = (a * 4096).astype(dt) if dt.startswith("int") else a.astype(dt)
+        s = orc.ref_compress_headed(a, rate)
+        d = orc.ref_decompress_headed(s, a.shape, a.dtype, rate)
+        nm = f"headed{k:02d}_{a.ndim}d_{a.dtype.name}"
+        arrays[nm + "__input"] = a
+        arrays[nm + "__stream"] = s
+        arrays[nm + "__output"] = d
+        arrays[nm + "__rate"] = np.array(rate)
+        k += 1
+    np.savez_compressed(os.path.join(OUT, "headed_cases.npz"), **arrays)
+    print(f"{k} headed cases")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--ints"]:
         write_int_cases()
+    elif sys.argv[1:] == ["--headed"]:
+        write_headed_cases()
     else:
         main()
         write_int_cases()
+        write_headed_cases()

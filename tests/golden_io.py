@@ -59,3 +59,8 @@ def load_all() -> list[dict]:
     """Full-array golden cases: the small floating-point ones and the
     integer ones (int_cases.npz)."""
     return small_cases() + small_cases("int_cases.npz")
+
+
+def headed_cases() -> list[dict]:
+    """Streams that start with zfp's full header (headed_cases.npz)."""
+    return small_cases("headed_cases.npz")

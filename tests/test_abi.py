@@ -113,3 +113,81 @@ def test_python_mirror_errors(gz):
     assert e.value.status == gz.GZFP_ERR_ARG
     assert gz.zfp_field_dimensionality(gz.zfp_field_2d(None, gz.zfp_type.double, 3, 5)) == 2
     assert abs(gz.stream_set_rate(zfp, 2.0, gz.zfp_type.float, 1) - 2.25) < 1e-12
+
+
+def test_header_write_matches_oracle(gz, orc):
+    """gzfp_write_header's bits are the first bits of the oracle's headed
+    stream (zfp_write_header with ZFP_HEADER_FULL), for every scalar type,
+    dimensionality and both mode forms; gzfp_read_header gives them back."""
+    from tests import golden_io
+    dts = {1: np.int32, 2: np.int64, 3: np.float32, 4: np.float64}
+    n = 0
+    for t, dt in dts.items():
+        for shape in ((1,), (203,), (5, 9), (16777216, 3), (3, 4, 5), (65536, 2, 3)):
+            for rate in (0.5, 4, 16, 32, 100, 500):
+                nx, ny, nz = orc.dims3(shape)
+                mb = gz._lib.gzfp_rate_to_maxbits(t, len(shape), rate)
+                hb = orc.port().gzo_header_bits(t, nx, ny, nz, float(rate))
+                if mb == 0 or mb < {1: 1, 2: 1, 3: 9, 4: 12}[t]:
+                    continue
+                buf = ctypes.create_string_buffer(24)
+                bits = ctypes.c_size_t(0)
+                st = gz._lib.gzfp_write_header(t, nx, ny, nz, mb, buf, 24, ctypes.byref(bits))
+                if hb == 0:  # maxbits beyond the 64-bit mode form
+                    assert st == gz.GZFP_ERR_ARG and mb > 32768, (t, shape, rate)
+                    continue
+                assert st == 0 and bits.value == hb, (t, shape, rate)
+                # the oracle's reader and the C ABI's read the same field back
+                h = orc.read_header(np.frombuffer(buf.raw, np.uint8))
+                assert h["bits"] == hb and h["maxbits"] == mb and h["shape"] == tuple(shape)
+                assert h["dtype"] == np.dtype(dt)
+                r = gz.read_header(buf.raw)
+                assert r["bits"] == hb and r["maxbits"] == mb and r["shape"] == tuple(shape)
+                n += 1
+    assert n > 100
+    for c in golden_io.headed_cases():
+        h = gz.read_header(c["stream"])
+        assert h["shape"] == c["input"].shape and h["dtype"] == c["input"].dtype.name
+        nx, ny, nz = gz._dims_of(c["input"].shape)
+        raw, bits = gz.write_header(h["type"], nx, ny, nz, h["maxbits"])
+        sb = np.unpackbits(c["stream"].view(np.uint8), bitorder="little")[:bits]
+        assert np.array_equal(np.unpackbits(np.frombuffer(raw, np.uint8), bitorder="little")[:bits], sb)
+
+
+def test_header_errors(gz):
+    lib = gz._lib
+    buf = ctypes.create_string_buffer(24)
+    bits = ctypes.c_size_t(0)
+    w = lambda *a: lib.gzfp_write_header(*a, buf, 24, ctypes.byref(bits))  # noqa: E731
+    assert w(4, 1 << 24, 5, 0, 64) == 0
+    assert w(4, (1 << 24) + 1, 5, 0, 64) == gz.GZFP_ERR_ARG    # 2D axis beyond 24 bits
+    assert w(3, 8, 8, (1 << 16) + 1, 64) == gz.GZFP_ERR_ARG    # 3D axis beyond 16 bits
+    assert w(4, 8, 8, 8, 32769) == gz.GZFP_ERR_ARG             # beyond the long mode form
+    assert w(3, 8, 8, 8, 8) == gz.GZFP_ERR_ARG                 # under the block header
+    assert w(9, 8, 8, 8, 64) == gz.GZFP_ERR_ARG
+    small = ctypes.create_string_buffer(12)
+    assert lib.gzfp_write_header(3, 8, 0, 0, 64, small, 12, ctypes.byref(bits)) == \
+        gz.GZFP_ERR_CAPACITY                                   # float: 148 bits, 19 bytes
+    assert lib.gzfp_write_header(4, 8, 0, 0, 64, small, 12, ctypes.byref(bits)) == 0
+    assert bits.value == 96
+    with pytest.raises(gz.GzfpError) as e:
+        gz.read_header(b"zfq\x05" + bytes(20))
+    assert e.value.status == gz.GZFP_ERR_ARG
+    with pytest.raises(gz.GzfpError) as e:
+        gz.read_header(small.raw[:11])  # shorter than a header
+    assert e.value.status == gz.GZFP_ERR_ARG
+
+
+@pytest.mark.parametrize("idx", range(7))
+def test_header_modes_abi(gz, idx):
+    """zfp's other modes are reported as unsupported."""
+    from tests.test_oracle import HEADER_MODES, _header_bits, _magic, _meta_3d_double
+    mode, ok, maxbits = HEADER_MODES[idx]
+    w = _header_bits(_magic() + [_meta_3d_double(40, 30, 20), mode])
+    if ok:
+        h = gz.read_header(w)
+        assert h["maxbits"] == maxbits and h["shape"] == (20, 30, 40) and h["dtype"] == "float64"
+    else:
+        with pytest.raises(gz.GzfpError) as e:
+            gz.read_header(w)
+        assert e.value.status == gz.GZFP_ERR_UNSUPPORTED

@@ -204,3 +204,115 @@ def test_strided_fields(orc):
             assert np.all(base.reshape(-1)[untouched] == 7)
     if ref_ok:
         assert checked >= 20
+
+
+# ----------------------------------------------------------- headed streams
+
+def test_headed_golden_streams(orc):
+    """The oracle's header + blocks equal the reference's zfp_write_header +
+    zfp_compress streams in tests/golden/headed_cases.npz, and decode to the
+    reference's output from the header alone."""
+    cs = golden_io.headed_cases()
+    assert len(cs) >= 16
+    for c in cs:
+        a = c["input"]
+        s = orc.compress_headed(a, c["rate"])
+        assert np.array_equal(s, c["stream"]), c["name"]
+        h = orc.read_header(c["stream"])
+        assert h["shape"] == a.shape and h["dtype"] == a.dtype, c["name"]
+        assert np.array_equal(orc.decompress_headed(c["stream"]), c["output"]), c["name"]
+        # the blocks are the plain stream's bits, shifted by the header
+        plain = orc.compress(a, c["rate"])
+        bits = np.unpackbits(s.view(np.uint8), bitorder="little")
+        pbits = np.unpackbits(plain.view(np.uint8), bitorder="little")
+        nb = orc.stream_bytes(a.shape, a.dtype, c["rate"]) * 8
+        hb = h["bits"]
+        blocks = int(np.prod([(n + 3) // 4 for n in a.shape]))
+        used = blocks * h["maxbits"]
+        assert np.array_equal(bits[hb:hb + used], pbits[:used]) and used <= nb, c["name"]
+
+
+def test_headed_streams_match_reference(ref):
+    rng = np.random.default_rng(71)
+    n = 0
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        for shape in ((37,), (9, 13), (5, 6, 7), (64,), (16, 16), (8, 8, 8), (4, 4, 68)):
+            if ref.is_int(dt) and any(s % 4 for s in shape):
+                continue
+            a = np.cumsum(rng.standard_normal(shape), axis=-1)
+            a = (a * 1000).astype(dt) if ref.is_int(dt) else a.astype(dt)
+            for rate in (1, 4, 12.5, 32, 64, 200):
+                if ref.stream_bytes(a.shape, dt, rate) == 0 or ref.headed_bytes(a.shape, dt, rate) == 0:
+                    continue
+                s = ref.compress_headed(a, rate)
+                assert np.array_equal(s, ref.ref_compress_headed(a, rate)), (dt, shape, rate)
+                h, r = ref.read_header(s), ref.ref_read_header(s)
+                assert h["bits"] == r["bits"] and h["maxbits"] == r["maxbits"] == r["minbits"]
+                assert np.array_equal(ref.decompress_headed(s),
+                                      ref.ref_decompress_headed(s, shape, dt, rate))
+                n += 1
+    assert n > 100
+
+
+def _header_bits(fields):
+    """Pack (value, nbits) fields LSB-first into three uint64 words."""
+    v, pos = 0, 0
+    for x, nb in fields:
+        v |= (int(x) & ((1 << nb) - 1)) << pos
+        pos += nb
+    return np.frombuffer(v.to_bytes(24, "little"), np.uint64).copy()
+
+
+def _magic():
+    return [(ord("z"), 8), (ord("f"), 8), (ord("p"), 8), (5, 8)]
+
+
+def _meta_3d_double(nx, ny, nz):
+    m = ((((nz - 1) << 16) | (ny - 1)) << 16) | (nx - 1)
+    return ((m << 4) | (2 << 2) | 3, 52)
+
+
+def _long_mode(minbits, maxbits, maxprec, minexp):
+    m = minexp + 16495
+    m = (m << 7) | (maxprec - 1)
+    m = (m << 15) | (maxbits - 1)
+    m = (m << 15) | (minbits - 1)
+    return ((m << 12) | 0xfff, 64)
+
+
+HEADER_MODES = [
+    # (mode field, accepted as fixed rate, maxbits)
+    ((767, 12), True, 768),                       # 12-bit fixed rate
+    ((2047 + 20, 12), False, 0),                  # fixed precision 20
+    ((3251 - 30, 12), False, 0),                  # fixed accuracy 2^-30
+    (_long_mode(700, 700, 64, -1074), True, 700),
+    (_long_mode(600, 700, 64, -1074), False, 0),  # variable rate
+    (_long_mode(700, 700, 40, -1074), False, 0),  # precision cap
+    (_long_mode(700, 700, 64, -1000), False, 0),  # accuracy floor
+]
+
+
+@pytest.mark.parametrize("mode,ok,maxbits", HEADER_MODES)
+def test_header_modes_oracle_and_reference(orc, mode, ok, maxbits):
+    """Headers of zfp's other modes are recognised as not fixed rate; the
+    reference reads the same parameters from them."""
+    w = _header_bits(_magic() + [_meta_3d_double(40, 30, 20), mode])
+    h = orc.read_header(w)
+    if ok:
+        assert h["bits"] in (96, 148) and h["maxbits"] == maxbits
+        assert h["shape"] == (20, 30, 40) and h["dtype"] == np.float64
+    else:
+        assert h["bits"] == -1
+    if orc.ref_available():
+        r = orc.ref_read_header(w)
+        assert r["bits"] == (96 if mode[1] == 12 else 148)
+        assert (r["nx"], r["ny"], r["nz"], r["type"]) == (40, 30, 20, 4)
+        assert (r["minbits"] == r["maxbits"] and r["maxprec"] >= 64 and r["minexp"] == -1074) == ok
+
+
+def test_header_bad_magic(orc):
+    w = _header_bits([(ord("z"), 8), (ord("f"), 8), (ord("q"), 8), (5, 8),
+                      _meta_3d_double(4, 4, 4), (63, 12)])
+    assert orc.read_header(w)["bits"] == 0
+    w = _header_bits(_magic()[:3] + [(6, 8), _meta_3d_double(4, 4, 4), (63, 12)])
+    assert orc.read_header(w)["bits"] == 0
