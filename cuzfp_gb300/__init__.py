@@ -80,6 +80,10 @@ _lib.gzfp_compress_headed.argtypes = [_I, _U, _U, _U, ctypes.c_double, _VP, _VP,
                                       _VP]
 _lib.gzfp_decompress_headed.restype = _I
 _lib.gzfp_decompress_headed.argtypes = [_VP, _SZ, _VP, _SZ, _VP]
+_lib.gzfp_decode_blocks.restype = _I
+_lib.gzfp_decode_blocks.argtypes = [_I, _U, _U, _VP, _SZ, _VP, _VP, _SZ, _VP, _VP]
+_lib.gzfp_encode_blocks.restype = _I
+_lib.gzfp_encode_blocks.argtypes = [_I, _U, _U, _VP, _VP, _VP, _SZ, _VP, _SZ, _VP]
 _lib.gzfp_decompress_strided.restype = _I
 _lib.gzfp_decompress_strided.argtypes = [_I, _U, _U, _U, _LL, _LL, _LL, _U, _VP, _SZ, _VP, _VP]
 
@@ -467,6 +471,66 @@ def decompress_headed(words, out=None, cuda_stream: Any = None):
     _check(_lib.gzfp_decompress_headed(src, size, dst, cap, _cuda_stream_handle(cuda_stream)),
            "decompress_headed")
     return out
+
+
+# -------------------------------------------------------------- block access
+# Random access to single blocks of a fixed-rate stream, as zfp's compressed
+# arrays fetch and write back cached blocks (zfp-0.5.0/array/zfparray3.h:
+# 225-255): block i sits at bit i * maxbits; each listed block maps to a
+# tile of 4^dims values (x fastest); shape codes mark partial blocks.
+
+def _block_buffers(indices, shapes, like):
+    """Indices (uint64) and shape codes (uint8) as buffers on the side of
+    `like` (a CUDA tensor: device tensors; else numpy)."""
+    if hasattr(like, "data_ptr") and getattr(like, "is_cuda", False):
+        import torch
+        idx = torch.as_tensor(indices, dtype=torch.int64, device=like.device).contiguous()
+        shp = None if shapes is None else torch.as_tensor(
+            shapes, dtype=torch.uint8, device=like.device).contiguous()
+    else:
+        import numpy as np
+        idx = np.ascontiguousarray(indices, dtype=np.uint64)
+        shp = None if shapes is None else np.ascontiguousarray(shapes, dtype=np.uint8)
+    n = int(idx.numel() if hasattr(idx, "numel") else idx.size)
+    if shp is not None and int(shp.numel() if hasattr(shp, "numel") else shp.size) != n:
+        raise GzfpError(GZFP_ERR_ARG, "one shape code per index")
+    return idx, shp, n
+
+
+def decode_blocks(words, dtype, dims: int, maxbits: int, indices, shapes=None, out=None,
+                  cuda_stream: Any = None):
+    """Decode the listed blocks of ``words`` into tiles (count x 4^dims).  A
+    partial block (non-zero shape code) writes only its valid values of its
+    tile.  Device words give a device result; host words a numpy one."""
+    t = _type_of(dtype)
+    idx, shp, n = _block_buffers(indices, shapes, words)
+    if out is None:
+        if hasattr(words, "data_ptr"):
+            import torch
+            out = torch.zeros((n, 4 ** dims), dtype=dtype, device=words.device)
+        else:
+            import numpy as np
+            out = np.zeros((n, 4 ** dims), dtype)
+    src, size = _addr_and_size(words)
+    dst, _ = _addr_and_size(out)
+    _check(_lib.gzfp_decode_blocks(int(t), dims, maxbits, src, size, _addr_and_size(idx)[0],
+                                   _addr_and_size(shp)[0], n, dst,
+                                   _cuda_stream_handle(cuda_stream)), "decode_blocks")
+    return out
+
+
+def encode_blocks(tiles, dims: int, maxbits: int, indices, words, shapes=None,
+                  cuda_stream: Any = None):
+    """Encode tile i into the slot of indices[i] of ``words``, in place; the
+    other bits of ``words`` are kept."""
+    t = _type_of(tiles.dtype)
+    idx, shp, n = _block_buffers(indices, shapes, tiles)
+    src, _ = _addr_and_size(tiles)
+    dst, size = _addr_and_size(words)
+    _check(_lib.gzfp_encode_blocks(int(t), dims, maxbits, src, _addr_and_size(idx)[0],
+                                   _addr_and_size(shp)[0], n, dst, size,
+                                   _cuda_stream_handle(cuda_stream)), "encode_blocks")
+    return words
 
 
 def version() -> int:

@@ -144,6 +144,30 @@ int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double
 int gzfp_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes,
                            void* cuda_stream);
 
+/* ------------------------------------------------------- block access ---
+   Random access to single blocks of a fixed-rate stream: zfp's per-block
+   API (zfp_encode_block_* / zfp_decode_block_* and their partial-block
+   forms, zfp-0.5.0/inc/zfp.h:452-521) over a list of blocks, as zfp's
+   compressed arrays use it to fetch and write back cached blocks
+   (zfp::array3::decode / encode, zfp-0.5.0/array/zfparray3.h:225-255).
+   Block indices[i] occupies bits [indices[i] * maxbits, (indices[i] + 1) *
+   maxbits) of the stream; tile i of `tiles` holds its 4^dims values, x
+   fastest.  `shapes` (NULL: every block whole) holds zfp's partial-block
+   codes, two bits per axis with x lowest, each 4 minus the block's extent
+   along that axis: a partial block is encoded from its valid values with
+   zfp's padding, and decoding one writes only those values of its tile.
+   Encoding rewrites each listed slot in place and keeps every other bit of
+   the stream; the indices of one call must be distinct.  Indices past the
+   end of the stream are skipped.  Pointers may be host or device memory
+   (host buffers, the stream included, are staged whole).
+   No counterpart in cuZFP. */
+int gzfp_decode_blocks(int type, unsigned dims, unsigned maxbits, const void* stream,
+                       size_t bytes, const unsigned long long* indices,
+                       const unsigned char* shapes, size_t count, void* tiles, void* cuda_stream);
+int gzfp_encode_blocks(int type, unsigned dims, unsigned maxbits, const void* tiles,
+                       const unsigned long long* indices, const unsigned char* shapes,
+                       size_t count, void* stream, size_t bytes, void* cuda_stream);
+
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and
    bits per block -- coded by one persistent kernel over a device-side work

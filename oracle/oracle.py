@@ -83,6 +83,14 @@ def port() -> ctypes.CDLL:
         lib.gzo_decompress_headed.restype = ctypes.c_int
         lib.gzo_decompress_headed.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                               ctypes.c_size_t]
+        _B = [ctypes.c_int, ctypes.c_int, ctypes.c_uint]
+        _IDX = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]  # indices, shapes, count
+        lib.gzo_decode_blocks.restype = ctypes.c_int
+        lib.gzo_decode_blocks.argtypes = _B + [ctypes.c_void_p, ctypes.c_size_t] + _IDX + \
+            [ctypes.c_void_p]
+        lib.gzo_encode_blocks.restype = ctypes.c_int
+        lib.gzo_encode_blocks.argtypes = _B + [ctypes.c_void_p] + _IDX + [ctypes.c_void_p,
+                                                                          ctypes.c_size_t]
         _port = lib
     return _port
 
@@ -130,6 +138,14 @@ def ref() -> ctypes.CDLL:
         lib.zref_decompress_headed_int.restype = ctypes.c_int
         lib.zref_decompress_headed_int.argtypes = _A + [ctypes.c_void_p, ctypes.c_size_t,
                                                         ctypes.c_void_p]
+        _B = [ctypes.c_int, ctypes.c_int, ctypes.c_uint]
+        _IDX = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        lib.zref_decode_blocks.restype = ctypes.c_int
+        lib.zref_decode_blocks.argtypes = _B + [ctypes.c_void_p, ctypes.c_size_t] + _IDX + \
+            [ctypes.c_void_p]
+        lib.zref_encode_blocks.restype = ctypes.c_int
+        lib.zref_encode_blocks.argtypes = _B + [ctypes.c_void_p] + _IDX + [ctypes.c_void_p,
+                                                                           ctypes.c_size_t]
         _ref = lib
     return _ref
 
@@ -372,3 +388,69 @@ def ref_decompress_headed(words: np.ndarray, shape, dtype, rate: float) -> np.nd
     if not ok:
         raise RuntimeError("reference headed decompress failed")
     return out
+
+
+# ------------------------------------------------------------- block access
+def _block_args(indices, shapes):
+    idx = np.ascontiguousarray(indices, dtype=np.uint64)
+    shp = None if shapes is None else np.ascontiguousarray(shapes, dtype=np.uint8)
+    return idx, shp, (shp.ctypes.data if shp is not None else None)
+
+
+def decode_blocks(words, dtype, dims: int, maxbits: int, indices, shapes=None,
+                  tiles=None, lib=None) -> np.ndarray:
+    """Decode the listed blocks into tiles of 4^dims values (a partial block
+    writes only its valid values of `tiles`, zeros by default)."""
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    idx, shp, shp_ptr = _block_args(indices, shapes)
+    if tiles is None:
+        tiles = np.zeros((idx.size, 4 ** dims), dtype)
+    fn = port().gzo_decode_blocks if lib is None else lib.zref_decode_blocks
+    if not fn(type_code(dtype), dims, maxbits, words.ctypes.data, words.nbytes, idx.ctypes.data,
+              shp_ptr, idx.size, tiles.ctypes.data):
+        raise RuntimeError("decode_blocks failed")
+    return tiles
+
+
+def encode_blocks(tiles: np.ndarray, dims: int, maxbits: int, indices, words: np.ndarray,
+                  shapes=None, lib=None) -> np.ndarray:
+    """Encode tile i into the slot of indices[i] of `words` (in place)."""
+    tiles = np.ascontiguousarray(tiles)
+    idx, shp, shp_ptr = _block_args(indices, shapes)
+    fn = port().gzo_encode_blocks if lib is None else lib.zref_encode_blocks
+    if not fn(type_code(tiles.dtype), dims, maxbits, tiles.ctypes.data, idx.ctypes.data, shp_ptr,
+              idx.size, words.ctypes.data, words.nbytes):
+        raise RuntimeError("encode_blocks failed")
+    return words
+
+
+def ref_decode_blocks(words, dtype, dims, maxbits, indices, shapes=None, tiles=None):
+    return decode_blocks(words, dtype, dims, maxbits, indices, shapes, tiles, lib=ref())
+
+
+def ref_encode_blocks(tiles, dims, maxbits, indices, words, shapes=None):
+    return encode_blocks(tiles, dims, maxbits, indices, words, shapes, lib=ref())
+
+
+def field_tiles(a: np.ndarray):
+    """The blocks of a contiguous field as tiles (block order x fastest, as
+    the stream), with zfp's partial-block shape codes; padded positions hold
+    zeros."""
+    shape = a.shape
+    d = a.ndim
+    nb = [(n + 3) // 4 for n in shape]  # per axis, slowest first
+    pad = np.zeros(tuple(4 * b for b in nb), a.dtype)
+    pad[tuple(slice(0, n) for n in shape)] = a
+    # (bz, 4, by, 4, bx, 4) -> (bz, by, bx, 4z, 4y, 4x)
+    t = pad.reshape(sum(([b, 4] for b in nb), []))
+    order = list(range(0, 2 * d, 2)) + list(range(1, 2 * d, 2))
+    t = np.ascontiguousarray(t.transpose(order)).reshape(-1, 4 ** d)
+    codes = np.zeros(nb, np.uint8)
+    for ax in range(d):  # axis ax of the array is zfp axis d-1-ax
+        n = shape[ax]
+        ext = np.full(nb[ax], 4, np.int64)
+        ext[-1] = n - 4 * (nb[ax] - 1)
+        sh = [1] * d
+        sh[ax] = nb[ax]
+        codes = codes + ((4 - ext).reshape(sh) << (2 * (d - 1 - ax))).astype(np.uint8)
+    return t, codes.reshape(-1)

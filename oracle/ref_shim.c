@@ -290,3 +290,94 @@ int zref_decompress_headed_int(int type, unsigned nx, unsigned ny, unsigned nz, 
                                const void* buffer, size_t bytes, void* out) {
   return int_array(type, nx, ny, nz, rate, out, (void*)buffer, bytes, 0, 1) != 0;
 }
+
+/* Random access through the per-block API (Z/inc/zfp.h:452-521), the way
+   zfp's compressed arrays fetch and write back blocks
+   (Z/array/zfparray3.h:225-255): stream_rseek / stream_wseek to
+   index * maxbits, one zfp_{en,de}code_{,partial_}block_* call, and after
+   an encode stream_flush.  The stream parameters are those
+   zfp_stream_set_rate leaves (zfp_stream_set_params, Z/src/zfp.c:500-511).
+   zfp 0.5.0 has no partial-block calls for integer blocks: those return 0. */
+static void float_block(zfp_stream* zfp, int dims, float* t, unsigned shape, int encode) {
+  uint nx = 4 - (shape & 3u), ny = 4 - (shape >> 2 & 3u), nz = 4 - (shape >> 4 & 3u);
+  if (encode && !shape) {
+    if (dims == 1) zfp_encode_block_float_1(zfp, t);
+    else if (dims == 2) zfp_encode_block_float_2(zfp, t);
+    else zfp_encode_block_float_3(zfp, t);
+  } else if (encode) {
+    if (dims == 1) zfp_encode_partial_block_strided_float_1(zfp, t, nx, 1);
+    else if (dims == 2) zfp_encode_partial_block_strided_float_2(zfp, t, nx, ny, 1, 4);
+    else zfp_encode_partial_block_strided_float_3(zfp, t, nx, ny, nz, 1, 4, 16);
+  } else if (!shape) {
+    if (dims == 1) zfp_decode_block_float_1(zfp, t);
+    else if (dims == 2) zfp_decode_block_float_2(zfp, t);
+    else zfp_decode_block_float_3(zfp, t);
+  } else {
+    if (dims == 1) zfp_decode_partial_block_strided_float_1(zfp, t, nx, 1);
+    else if (dims == 2) zfp_decode_partial_block_strided_float_2(zfp, t, nx, ny, 1, 4);
+    else zfp_decode_partial_block_strided_float_3(zfp, t, nx, ny, nz, 1, 4, 16);
+  }
+}
+
+static void double_block(zfp_stream* zfp, int dims, double* t, unsigned shape, int encode) {
+  uint nx = 4 - (shape & 3u), ny = 4 - (shape >> 2 & 3u), nz = 4 - (shape >> 4 & 3u);
+  if (encode && !shape) {
+    if (dims == 1) zfp_encode_block_double_1(zfp, t);
+    else if (dims == 2) zfp_encode_block_double_2(zfp, t);
+    else zfp_encode_block_double_3(zfp, t);
+  } else if (encode) {
+    if (dims == 1) zfp_encode_partial_block_strided_double_1(zfp, t, nx, 1);
+    else if (dims == 2) zfp_encode_partial_block_strided_double_2(zfp, t, nx, ny, 1, 4);
+    else zfp_encode_partial_block_strided_double_3(zfp, t, nx, ny, nz, 1, 4, 16);
+  } else if (!shape) {
+    if (dims == 1) zfp_decode_block_double_1(zfp, t);
+    else if (dims == 2) zfp_decode_block_double_2(zfp, t);
+    else zfp_decode_block_double_3(zfp, t);
+  } else {
+    if (dims == 1) zfp_decode_partial_block_strided_double_1(zfp, t, nx, 1);
+    else if (dims == 2) zfp_decode_partial_block_strided_double_2(zfp, t, nx, ny, 1, 4);
+    else zfp_decode_partial_block_strided_double_3(zfp, t, nx, ny, nz, 1, 4, 16);
+  }
+}
+
+static int block_io(zfp_stream* zfp, int type, int dims, void* tile, unsigned shape, int encode) {
+  if (type == zfp_type_float) float_block(zfp, dims, (float*)tile, shape, encode);
+  else if (type == zfp_type_double) double_block(zfp, dims, (double*)tile, shape, encode);
+  else if (shape) return 0;
+  else int_block_codec(zfp, type, dims, tile, encode);
+  return 1;
+}
+
+static int blocks(int type, int dims, unsigned maxbits, void* tiles,
+                  const unsigned long long* index, const unsigned char* shape, size_t count,
+                  void* buffer, size_t bytes, int encode) {
+  const size_t es = type == zfp_type_float || type == zfp_type_int32 ? 4 : 8;
+  const uint prec = es == 4 ? 32 : 64;
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  bitstream* s = stream_open(buffer, bytes);
+  size_t i;
+  int ok = zfp_stream_set_params(zfp, maxbits, maxbits, prec, ZFP_MIN_EXP);
+  zfp_stream_set_bit_stream(zfp, s);
+  for (i = 0; ok && i < count; i++) {
+    void* tile = (char*)tiles + i * ((size_t)1 << (2 * dims)) * es;
+    if (encode) stream_wseek(s, (size_t)(index[i] * maxbits));
+    else stream_rseek(s, (size_t)(index[i] * maxbits));
+    ok = block_io(zfp, type, dims, tile, shape ? shape[i] : 0u, encode);
+    if (encode) stream_flush(s);
+  }
+  stream_close(s);
+  zfp_stream_close(zfp);
+  return ok;
+}
+
+int zref_encode_blocks(int type, int dims, unsigned maxbits, const void* tiles,
+                       const unsigned long long* index, const unsigned char* shape, size_t count,
+                       void* buffer, size_t bytes) {
+  return blocks(type, dims, maxbits, (void*)tiles, index, shape, count, buffer, bytes, 1);
+}
+
+int zref_decode_blocks(int type, int dims, unsigned maxbits, const void* buffer, size_t bytes,
+                       const unsigned long long* index, const unsigned char* shape, size_t count,
+                       void* tiles) {
+  return blocks(type, dims, maxbits, tiles, index, shape, count, (void*)buffer, bytes, 0);
+}

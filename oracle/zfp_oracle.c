@@ -868,3 +868,86 @@ int gzo_decompress_headed(const void* stream, size_t bytes, void* data, size_t d
   }
   return 1;
 }
+
+/* ---------------------------------------------------------- block access --- */
+
+/* One listed block as a one-block field of its tile: extents from zfp's
+   partial-block shape code (two bits per axis, x lowest, each 4 minus the
+   extent; Z/array/zfpcodecd.h:5-75), values at strides 1, 4, 16. */
+static int tile_params(params* p, int type, int dims, unsigned shape, unsigned maxbits) {
+  unsigned cx = 4 - (shape & 3), cy = 4 - (shape >> 2 & 3), cz = 4 - (shape >> 4 & 3);
+  if (!setup_bits(p, type, cx, dims >= 2 ? cy : 0, dims >= 3 ? cz : 0, maxbits)) return 0;
+  p->sx = 1;
+  p->sy = 4;
+  p->sz = 16;
+  return 1;
+}
+
+/* zfp_decode_block_* / zfp_decode_partial_block_strided_* at bit
+   index[i] * maxbits (stream_rseek, Z/src/inline/bitstream.c:309-322), into
+   tile i; a partial block writes only its valid values.  Indices past the
+   stream are skipped.  Returns 1, or 0 on a bad argument. */
+int gzo_decode_blocks(int type, int dims, unsigned maxbits, const void* stream, size_t bytes,
+                      const unsigned long long* index, const unsigned char* shape, size_t count,
+                      void* tiles) {
+  size_t i, es = type == GZO_FLOAT || type == GZO_INT32 ? 4 : 8;
+  size_t slots = bytes / 8 * 64 / (maxbits ? maxbits : 1);
+  double blk[64];
+  for (i = 0; i < count; i++) {
+    params p;
+    rbits r;
+    if (!tile_params(&p, type, dims, shape ? shape[i] : 0u, maxbits)) return 0;
+    if (index[i] >= slots) continue;
+    r.words = (const uint64_t*)stream;
+    r.bit = (size_t)(index[i] * maxbits);
+    decode_block(&r, &p, blk);
+    scatter(&p, (char*)tiles + i * ((size_t)1 << (2 * dims)) * es, 0, 0, 0, blk);
+  }
+  return 1;
+}
+
+/* zfp_encode_block_* / zfp_encode_partial_block_strided_* of tile i into
+   the slot of index[i], keeping every other bit of the stream (zfp's own
+   stream_wseek + stream_flush zero the rest of the slot's last word,
+   Z/src/inline/bitstream.c:89-96; that agrees with this for word-aligned
+   slots).  Indices past the stream are skipped. */
+int gzo_encode_blocks(int type, int dims, unsigned maxbits, const void* tiles,
+                      const unsigned long long* index, const unsigned char* shape, size_t count,
+                      void* stream, size_t bytes) {
+  size_t i, es = type == GZO_FLOAT || type == GZO_INT32 ? 4 : 8;
+  size_t nwords = bytes / 8, slots = nwords * 64 / (maxbits ? maxbits : 1);
+  uint64_t* words = (uint64_t*)stream;
+  uint64_t* tmp = (uint64_t*)calloc(maxbits / 64 + 3, 8);
+  double blk[64];
+  if (!tmp) return 0;
+  for (i = 0; i < count; i++) {
+    params p;
+    wbits w;
+    uint64_t pos, end, k;
+    unsigned off;
+    if (!tile_params(&p, type, dims, shape ? shape[i] : 0u, maxbits)) {
+      free(tmp);
+      return 0;
+    }
+    if (index[i] >= slots) continue;
+    pos = index[i] * maxbits;
+    end = pos + maxbits;
+    off = (unsigned)(pos % 64);
+    /* code the block into tmp, at the slot's offset within its first word */
+    memset(tmp, 0, (maxbits / 64 + 3) * 8);
+    w_init(&w, tmp, 0);
+    w_put(&w, 0, off);
+    gather(&p, (const char*)tiles + i * ((size_t)1 << (2 * dims)) * es, 0, 0, 0, blk);
+    encode_block(&w, &p, blk);
+    w_flush(&w);
+    /* replace the slot's bits, word by word */
+    for (k = pos / 64; k * 64 < end; k++) {
+      uint64_t lo = k * 64 < pos ? pos - k * 64 : 0;
+      uint64_t hi = end - k * 64 < 64 ? end - k * 64 : 64;
+      uint64_t mask = (hi >= 64 ? ~0ull : ((1ull << hi) - 1)) & ~((1ull << lo) - 1);
+      words[k] = (words[k] & ~mask) | (tmp[k - pos / 64] & mask);
+    }
+  }
+  free(tmp);
+  return 1;
+}
