@@ -594,7 +594,8 @@ def default_batch_config() -> BatchConfig:
 
 def batch_items(fields, streams, rates):
     """ctypes array of gzfp_batch_item for CUDA tensors `fields` (float32 /
-    float64, 1-3 dims), stream word tensors `streams` and per-array rates."""
+    float64 / int32 / int64, 1-3 dims), stream word tensors `streams` and
+    per-array rates."""
     items = (BatchItem * len(fields))()
     for i, (f, w, r) in enumerate(zip(fields, streams, rates)):
         t = _type_of(f.dtype)
@@ -758,5 +759,6 @@ __all__ = [
     "default_batch_config", "compress_batch", "decompress_batch", "BatchPlan", "autotune_batch",
     "batch_stream_buffers", "ServeRequest", "ServeResult", "ServeConfig", "ServeStats",
     "default_serve_config", "serve_request", "serve", "GZFP_SERVE_COMPRESS",
-    "GZFP_SERVE_DECOMPRESS",
+    "GZFP_SERVE_DECOMPRESS", "HEADER_MAX_BITS", "write_header", "read_header", "headed_size",
+    "compress_headed", "decompress_headed", "decode_blocks", "encode_blocks",
 ]

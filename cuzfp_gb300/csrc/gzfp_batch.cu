@@ -73,12 +73,10 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
   std::vector<int> kind_of(count);
   for (int i = 0; i < count; i++) {
     const gzfp_batch_item& it = items[i];
-    if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
-      return bfail(GZFP_ERR_UNSUPPORTED, "batch items must be float or double");
+    if (!batch_type_ok(it.type)) return bfail(GZFP_ERR_UNSUPPORTED, "unknown scalar type");
     if (it.nx == 0 || (it.nz != 0 && it.ny == 0)) return bfail(GZFP_ERR_ARG, "bad dimensions");
     if (!it.field || !it.stream) return bfail(GZFP_ERR_ARG, "null pointer");
-    const unsigned ebits = it.type == GZFP_TYPE_FLOAT ? 8 : 11;
-    if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
+    if (it.maxbits < batch_ebits(it.type) + 1 || it.maxbits > (1u << 20))
       return bfail(GZFP_ERR_ARG, "bits per block out of range");
     const int dims = it.nz ? 3 : it.ny ? 2 : 1;
     const Geom g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
@@ -86,7 +84,7 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
     const uint64_t nwords = (g.nblocks * it.maxbits + 63) / 64;
     if (it.stream_capacity < nwords * 8)
       return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
-    kind_of[i] = batch_kind_index((uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? kKindDouble : 0u));
+    kind_of[i] = batch_kind_index(batch_kind(it.type, dims));
   }
   // descriptors grouped by kind, so each kind's chunks form one range
   int slot = 0;
@@ -97,8 +95,7 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
       const gzfp_batch_item& it = items[i];
       BatchDesc& d = p.descs[slot++];
       d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-      const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
-      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % batch_row_align(it.type) == 0) ? 1u : 0u;
       d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
       d.maxbits = it.maxbits;
       d.kind = kBatchKind[k];

@@ -2,7 +2,8 @@
 // shape, scalar type, dimensionality and rate coded by a few launches.
 //
 // Work list (device memory, built per batch): one descriptor per array,
-// grouped by kind (dimensionality x scalar type), and a table mapping every
+// grouped by kind (dimensionality x scalar type: float, double, int32,
+// int64), and a table mapping every
 // chunk -- NT * BPT consecutive zfp blocks of one array -- to its array.
 // The chunks of one kind form one contiguous range.  Each kind present in
 // the batch gets one persistent kernel specialised for it (so its register
@@ -13,6 +14,8 @@
 // per-thread code.  Every block's bits are the same as a plain launch on
 // that array would produce.
 #pragma once
+
+#include <type_traits>
 
 #include "gzfp_kernels.cuh"
 
@@ -26,12 +29,15 @@ struct BatchDesc {
   uint64_t nwords;       // stream words
   uint64_t first_chunk;  // index of the array's first chunk in the batch
   uint32_t maxbits;
-  uint32_t kind;         // dims | (8 for double)
+  uint32_t kind;         // batch_kind(type, dims), gzfp_batch_launch.h
 };
 
-constexpr uint32_t kKindDouble = 8;
-constexpr int kBatchKinds = 6;  // 1D/2D/3D x float/double
-constexpr uint32_t kBatchKind[kBatchKinds] = {1, 2, 3, 9, 10, 11};
+// An array's kind: dims | 8 * (0 float, 1 double, 2 int32, 3 int64).  The
+// first six kinds (floating point) and the last six (integer) are compiled
+// in separate translation units.
+constexpr int kBatchKinds = 12;
+constexpr int kBatchFloatKinds = 6;
+constexpr uint32_t kBatchKind[kBatchKinds] = {1, 2, 3, 9, 10, 11, 17, 18, 19, 25, 26, 27};
 
 inline int batch_kind_index(uint32_t kind) {
   for (int i = 0; i < kBatchKinds; i++)
@@ -160,44 +166,39 @@ int batch_occupancy_kind(uint32_t staged_w) {
   return n;
 }
 
-// Dispatch over the six kinds (kind index into kBatchKind).
-template <int NT, bool DECODE>
+// Dispatch over the six kinds of one group (INTS: kind indices 6..11, the
+// integer kinds; else 0..5).
+template <int NT, bool DECODE, bool INTS>
 cudaError_t launch_batch_t(int kind_index, int grid, int bpt, bool ahead, uint32_t staged_w,
                            const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,
                            uint64_t hi, unsigned long long* counter, cudaStream_t s) {
-  switch (kind_index) {
-    case 0:
-      return launch_batch_kind<NT, DECODE, 1, float>(grid, bpt, ahead, staged_w, descs,
-                                                     chunk_item, lo, hi, counter, s);
-    case 1:
-      return launch_batch_kind<NT, DECODE, 2, float>(grid, bpt, ahead, staged_w, descs,
-                                                     chunk_item, lo, hi, counter, s);
-    case 2:
-      return launch_batch_kind<NT, DECODE, 3, float>(grid, bpt, ahead, staged_w, descs,
-                                                     chunk_item, lo, hi, counter, s);
-    case 3:
-      return launch_batch_kind<NT, DECODE, 1, double>(grid, bpt, ahead, staged_w, descs,
-                                                      chunk_item, lo, hi, counter, s);
-    case 4:
-      return launch_batch_kind<NT, DECODE, 2, double>(grid, bpt, ahead, staged_w, descs,
-                                                      chunk_item, lo, hi, counter, s);
-    case 5:
-      return launch_batch_kind<NT, DECODE, 3, double>(grid, bpt, ahead, staged_w, descs,
-                                                      chunk_item, lo, hi, counter, s);
-    default:
-      return cudaErrorInvalidValue;
+  typedef typename std::conditional<INTS, int32_t, float>::type T4;
+  typedef typename std::conditional<INTS, int64_t, double>::type T8;
+#define GZFP_KIND(D, T) \
+  launch_batch_kind<NT, DECODE, D, T>(grid, bpt, ahead, staged_w, descs, chunk_item, lo, hi, counter, s)
+  switch (kind_index - (INTS ? kBatchFloatKinds : 0)) {
+    case 0: return GZFP_KIND(1, T4);
+    case 1: return GZFP_KIND(2, T4);
+    case 2: return GZFP_KIND(3, T4);
+    case 3: return GZFP_KIND(1, T8);
+    case 4: return GZFP_KIND(2, T8);
+    case 5: return GZFP_KIND(3, T8);
+    default: return cudaErrorInvalidValue;
   }
+#undef GZFP_KIND
 }
 
-template <int NT, bool DECODE>
+template <int NT, bool DECODE, bool INTS>
 int batch_occupancy_t(int kind_index, uint32_t staged_w) {
-  switch (kind_index) {
-    case 0: return batch_occupancy_kind<NT, DECODE, 1, float>(staged_w);
-    case 1: return batch_occupancy_kind<NT, DECODE, 2, float>(staged_w);
-    case 2: return batch_occupancy_kind<NT, DECODE, 3, float>(staged_w);
-    case 3: return batch_occupancy_kind<NT, DECODE, 1, double>(staged_w);
-    case 4: return batch_occupancy_kind<NT, DECODE, 2, double>(staged_w);
-    case 5: return batch_occupancy_kind<NT, DECODE, 3, double>(staged_w);
+  typedef typename std::conditional<INTS, int32_t, float>::type T4;
+  typedef typename std::conditional<INTS, int64_t, double>::type T8;
+  switch (kind_index - (INTS ? kBatchFloatKinds : 0)) {
+    case 0: return batch_occupancy_kind<NT, DECODE, 1, T4>(staged_w);
+    case 1: return batch_occupancy_kind<NT, DECODE, 2, T4>(staged_w);
+    case 2: return batch_occupancy_kind<NT, DECODE, 3, T4>(staged_w);
+    case 3: return batch_occupancy_kind<NT, DECODE, 1, T8>(staged_w);
+    case 4: return batch_occupancy_kind<NT, DECODE, 2, T8>(staged_w);
+    case 5: return batch_occupancy_kind<NT, DECODE, 3, T8>(staged_w);
     default: return 0;
   }
 }

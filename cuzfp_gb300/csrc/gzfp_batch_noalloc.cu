@@ -99,12 +99,10 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
   for (int i = 0; i < count; i++) {
     const gzfp_batch_item& it = items[i];
-    if (it.type != GZFP_TYPE_FLOAT && it.type != GZFP_TYPE_DOUBLE)
-      return nfail(GZFP_ERR_UNSUPPORTED, "batch items must be float or double");
+    if (!gzfp::batch_type_ok(it.type)) return nfail(GZFP_ERR_UNSUPPORTED, "unknown scalar type");
     if (it.nx == 0 || (it.nz != 0 && it.ny == 0)) return nfail(GZFP_ERR_ARG, "bad dimensions");
     if (!it.field || !it.stream) return nfail(GZFP_ERR_ARG, "null pointer");
-    const unsigned ebits = it.type == GZFP_TYPE_FLOAT ? 8 : 11;
-    if (it.maxbits < ebits + 1 || it.maxbits > (1u << 20))
+    if (it.maxbits < gzfp::batch_ebits(it.type) + 1 || it.maxbits > (1u << 20))
       return nfail(GZFP_ERR_ARG, "bits per block out of range");
     const gzfp::Geom g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
     if (g.nblocks >= (1ull << 32)) return nfail(GZFP_ERR_ARG, "too many blocks");
@@ -120,12 +118,12 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
     for (int i = 0; i < count; i++) {
       const gzfp_batch_item& it = items[i];
       const int dims = it.nz ? 3 : it.ny ? 2 : 1;
-      const uint32_t kind = (uint32_t)dims | (it.type == GZFP_TYPE_DOUBLE ? gzfp::kKindDouble : 0u);
+      const uint32_t kind = gzfp::batch_kind(it.type, dims);
       if (kind != gzfp::kBatchKind[k]) continue;
       gzfp::BatchDesc& d = g_host[slot++];
       d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-      const uintptr_t align = it.type == GZFP_TYPE_FLOAT ? 16 : 32;
-      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % align == 0) ? 1u : 0u;
+      d.g.vec =
+          (it.nx % 4 == 0 && (uintptr_t)it.field % gzfp::batch_row_align(it.type) == 0) ? 1u : 0u;
       d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
       d.maxbits = it.maxbits;
       d.kind = kind;

@@ -88,8 +88,7 @@ size_t output_bytes(const gzfp_serve_request& r) {
   const unsigned ny = r.ny ? r.ny : 1, nz = r.nz ? r.nz : 1;
   if (r.op == GZFP_SERVE_COMPRESS)
     return gzfp_stream_size(r.type, r.nx, r.ny, r.nz, r.maxbits);
-  const size_t scalar = r.type == GZFP_TYPE_FLOAT ? 4 : 8;
-  return (size_t)r.nx * ny * nz * scalar;
+  return (size_t)r.nx * ny * nz * gzfp::batch_scalar_size(r.type);
 }
 
 struct Slot {
@@ -133,7 +132,7 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
   for (int i = 0; i < count; i++) {
     const gzfp_serve_request& r = reqs[i];
     if ((r.op != GZFP_SERVE_COMPRESS && r.op != GZFP_SERVE_DECOMPRESS) || !r.input ||
-        (r.type != GZFP_TYPE_FLOAT && r.type != GZFP_TYPE_DOUBLE) || output_bytes(r) == 0)
+        !gzfp::batch_type_ok(r.type) || output_bytes(r) == 0)
       return sfail(GZFP_ERR_ARG, "bad request");
     results[i] = gzfp_serve_result{0.0, 0.0, output_bytes(r), -1, GZFP_OK};
   }

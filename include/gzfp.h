@@ -177,7 +177,7 @@ int gzfp_encode_blocks(int type, unsigned dims, unsigned maxbits, const void* ti
    array per call (src/cuZFP/cuZFP.cu:174-269). */
 
 typedef struct {
-  int type;               /* GZFP_TYPE_FLOAT or GZFP_TYPE_DOUBLE */
+  int type;               /* GZFP_TYPE_FLOAT, _DOUBLE, _INT32 or _INT64 */
   unsigned nx, ny, nz;    /* as gzfp_compress: ny = 0 for 1D, nz = 0 for 2D */
   unsigned maxbits;       /* bits per block (gzfp_rate_to_maxbits) */
   void* field;            /* device array: input of compress, output of decompress */
@@ -276,7 +276,7 @@ int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompre
 
 typedef struct {
   int op;                /* GZFP_SERVE_COMPRESS or GZFP_SERVE_DECOMPRESS */
-  int type;              /* GZFP_TYPE_FLOAT or GZFP_TYPE_DOUBLE */
+  int type;              /* GZFP_TYPE_FLOAT, _DOUBLE, _INT32 or _INT64 */
   unsigned nx, ny, nz;   /* as gzfp_compress */
   unsigned maxbits;      /* bits per block */
   const void* input;     /* device: the field (compress) or stream words (decompress) */

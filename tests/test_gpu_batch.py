@@ -10,20 +10,23 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def mixed_batch(rng, count=40):
-    """Arrays of every dimensionality and type, ragged shapes, rates whose
-    blocks are and are not whole 64-bit words."""
+def mixed_batch(rng, count=40, ints=True):
+    """Arrays of every dimensionality and scalar type (integers too unless
+    `ints` is false), ragged shapes, rates whose blocks are and are not
+    whole 64-bit words."""
     arrs, rates = [], []
+    types = (np.float32, np.float64, np.int32, np.int64) if ints else (np.float32, np.float64)
     for i in range(count):
         dims = 1 + i % 3
-        dt = np.float32 if rng.random() < 0.5 else np.float64
+        dt = types[int(rng.integers(0, len(types)))]
         if dims == 1:
             shape = (int(rng.integers(1, 3000)),)
         elif dims == 2:
             shape = tuple(int(v) for v in rng.integers(1, 90, 2))
         else:
             shape = tuple(int(v) for v in rng.integers(1, 40, 3))
-        a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape).astype(dt)
+        a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+        a = (a * 5000).astype(dt) if np.dtype(dt).kind == "i" else a.astype(dt)
         arrs.append(a)
         rates.append(float(rng.choice([1, 2.5, 4, 8, 12, 16, 21.3, 32])))
     return arrs, rates
@@ -67,7 +70,7 @@ def test_batch_plan_replays(gz, cuda):
     torch.cuda.synchronize()
     for f, r, o in zip(fields, rates, outs):
         exp = gz.decompress_tensor(gz.compress_tensor(f, r), f.shape, f.dtype, r)
-        bits = torch.int64 if exp.dtype == torch.float64 else torch.int32
+        bits = torch.int64 if exp.element_size() == 8 else torch.int32
         assert torch.equal(exp.view(bits), o.view(bits))
     plan.close()
     dplan.close()

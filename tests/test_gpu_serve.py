@@ -24,10 +24,12 @@ def _requests(gz, cuda, rng, count, max_edge, gap):
             shape = tuple(int(v) for v in rng.integers(1, max_edge * 5, 2))
         else:
             shape = tuple(int(v) for v in rng.integers(1, max_edge, 3))
-        dt = torch.float32 if rng.random() < 0.5 else torch.float64
+        dt = (torch.float32, torch.float64, torch.int32, torch.int64)[int(rng.integers(0, 4))]
         rate = float(rng.choice([4, 8, 12.5, 16, 32]))
-        x = torch.from_numpy(np.cumsum(rng.standard_normal(int(np.prod(shape))))
-                             .reshape(shape)).to(dt).to(cuda)
+        walk = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+        if not dt.is_floating_point:
+            walk = walk * 5000
+        x = torch.from_numpy(walk).to(dt).to(cuda)
         w = gz.compress_tensor(x, rate)  # alone
         t += float(rng.exponential(gap))
         if rng.random() < 0.5:
@@ -36,7 +38,7 @@ def _requests(gz, cuda, rng, count, max_edge, gap):
             expect.append(w)
         else:
             y = gz.decompress_tensor(w, shape, dt, rate)  # alone
-            out = torch.full_like(y, float("nan"))
+            out = torch.full_like(y, float("nan") if dt.is_floating_point else -7)
             reqs.append(gz.serve_request(gz.GZFP_SERVE_DECOMPRESS, w, rate, t, shape=shape,
                                          dtype=dt, copy_to=out))
             expect.append(y)

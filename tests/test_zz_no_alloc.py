@@ -28,14 +28,15 @@ def _batch(rng, count):
     arrs, rates = [], []
     for i in range(count):
         dims = 1 + i % 3
-        dt = np.float32 if rng.random() < 0.5 else np.float64
+        dt = (np.float32, np.float64, np.int32, np.int64)[int(rng.integers(0, 4))]
         if dims == 1:
             shape = (int(rng.integers(1, 5000)),)
         elif dims == 2:
             shape = tuple(int(v) for v in rng.integers(1, 120, 2))
         else:
             shape = tuple(int(v) for v in rng.integers(1, 50, 3))
-        a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape).astype(dt)
+        a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+        a = (a * 5000).astype(dt) if np.dtype(dt).kind == "i" else a.astype(dt)
         arrs.append(a)
         rates.append(float(rng.choice([1, 3, 4, 8, 13.5, 16, 32])))
     return arrs, rates
@@ -43,7 +44,7 @@ def _batch(rng, count):
 
 def _bits(t):
     import torch
-    return t.view(torch.int64 if t.dtype == torch.float64 else torch.int32)
+    return t.view(torch.int64 if t.element_size() == 8 else torch.int32)
 
 
 def test_noalloc_matches_batch_entry_points(gz, cuda):
@@ -63,7 +64,8 @@ def test_noalloc_matches_batch_entry_points(gz, cuda):
         got_s = gz.batch_stream_buffers(fields, rates)
         for s in got_s:
             s.fill_(-1)  # anything the kernel leaves unwritten shows
-        got_o = [torch.full_like(f, float("nan")) for f in fields]
+        got_o = [torch.full_like(f, float("nan") if f.is_floating_point() else -7)
+                 for f in fields]
         torch.cuda.synchronize()
         free_before = torch.cuda.mem_get_info()[0]
         items = gz.batch_items(fields, got_s, rates)
