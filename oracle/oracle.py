@@ -91,6 +91,21 @@ def port() -> ctypes.CDLL:
         lib.gzo_encode_blocks.restype = ctypes.c_int
         lib.gzo_encode_blocks.argtypes = _B + [ctypes.c_void_p] + _IDX + [ctypes.c_void_p,
                                                                           ctypes.c_size_t]
+        _PR = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_int]  # minbits..minexp
+        _PP = [ctypes.POINTER(ctypes.c_uint)] * 3 + [ctypes.POINTER(ctypes.c_int)]
+        lib.gzo_mode_precision.restype = None
+        lib.gzo_mode_precision.argtypes = [ctypes.c_int, ctypes.c_uint] + _PP
+        lib.gzo_mode_accuracy.restype = None
+        lib.gzo_mode_accuracy.argtypes = [ctypes.c_int, ctypes.c_double] + _PP
+        _F = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint] + _PR
+        lib.gzo_bound_params.restype = ctypes.c_size_t
+        lib.gzo_bound_params.argtypes = _F
+        lib.gzo_compress_params.restype = ctypes.c_size_t
+        lib.gzo_compress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                 ctypes.c_void_p]
+        lib.gzo_decompress_params.restype = ctypes.c_int
+        lib.gzo_decompress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_size_t,
+                                                   ctypes.c_void_p, ctypes.c_void_p]
         _port = lib
     return _port
 
@@ -146,6 +161,19 @@ def ref() -> ctypes.CDLL:
         lib.zref_encode_blocks.restype = ctypes.c_int
         lib.zref_encode_blocks.argtypes = _B + [ctypes.c_void_p] + _IDX + [ctypes.c_void_p,
                                                                            ctypes.c_size_t]
+        _PR = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_int]
+        _PP = [ctypes.POINTER(ctypes.c_uint)] * 3 + [ctypes.POINTER(ctypes.c_int)]
+        _F = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint] + _PR
+        lib.zref_compress_params.restype = ctypes.c_size_t
+        lib.zref_compress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_size_t]
+        lib.zref_decompress_params.restype = ctypes.c_int
+        lib.zref_decompress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_size_t,
+                                                    ctypes.c_void_p]
+        lib.zref_set_precision.restype = None
+        lib.zref_set_precision.argtypes = [ctypes.c_int, ctypes.c_uint] + _PP
+        lib.zref_set_accuracy.restype = None
+        lib.zref_set_accuracy.argtypes = [ctypes.c_int, ctypes.c_double] + _PP
         _ref = lib
     return _ref
 
@@ -454,3 +482,79 @@ def field_tiles(a: np.ndarray):
         sh[ax] = nb[ax]
         codes = codes + ((4 - ext).reshape(sh) << (2 * (d - 1 - ax))).astype(np.uint8)
     return t, codes.reshape(-1)
+
+
+# ------------------------------------------- general parameters (zfp modes)
+def _mode_out(fn, t, v):
+    mn, mx, mp, me = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_int()
+    fn(t, v, ctypes.byref(mn), ctypes.byref(mx), ctypes.byref(mp), ctypes.byref(me))
+    return (mn.value, mx.value, mp.value, me.value)
+
+
+def mode_precision(dtype, precision: int, lib=None) -> tuple:
+    """(minbits, maxbits, maxprec, minexp) of zfp_stream_set_precision."""
+    fn = port().gzo_mode_precision if lib is None else lib.zref_set_precision
+    return _mode_out(fn, type_code(dtype), int(precision))
+
+
+def mode_accuracy(dtype, tolerance: float, lib=None) -> tuple:
+    """(minbits, maxbits, maxprec, minexp) of zfp_stream_set_accuracy."""
+    fn = port().gzo_mode_accuracy if lib is None else lib.zref_set_accuracy
+    return _mode_out(fn, type_code(dtype), float(tolerance))
+
+
+def compress_params(a: np.ndarray, params: tuple, with_offsets: bool = False):
+    """Oracle stream of a contiguous array under zfp's general parameters
+    (minbits, maxbits, maxprec, minexp); with_offsets also returns every
+    block's start bit."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    t = type_code(a.dtype)
+    cap = int(port().gzo_bound_params(t, nx, ny, nz, *params))
+    if cap == 0:
+        raise RuntimeError("bad parameters")
+    out = np.zeros(cap // 8 + 1, np.uint64)
+    nb = int(np.prod([(n + 3) // 4 for n in a.shape]))
+    offs = np.zeros(nb, np.uint64)
+    n = port().gzo_compress_params(t, nx, ny, nz, *params, a.ctypes.data, out.ctypes.data,
+                                   out.nbytes, offs.ctypes.data)
+    if n == 0:
+        raise RuntimeError("oracle compress failed")
+    return (out[: n // 8], offs) if with_offsets else out[: n // 8]
+
+
+def decompress_params(words, shape, dtype, params: tuple, with_offsets: bool = False):
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    out = np.zeros(tuple(shape), dtype)
+    nx, ny, nz = dims3(shape)
+    nb = int(np.prod([(n + 3) // 4 for n in shape]))
+    offs = np.zeros(nb, np.uint64)
+    if not port().gzo_decompress_params(type_code(dtype), nx, ny, nz, *params, words.ctypes.data,
+                                        words.nbytes, out.ctypes.data, offs.ctypes.data):
+        raise RuntimeError("oracle decompress failed")
+    return (out, offs) if with_offsets else out
+
+
+def ref_compress_params(a: np.ndarray, params: tuple) -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    t = type_code(a.dtype)
+    cap = int(port().gzo_bound_params(t, nx, ny, nz, *params)) + 64
+    buf = np.zeros(cap // 8 + 1, np.uint64)
+    n = ref().zref_compress_params(t, nx, ny, nz, *params, a.ctypes.data, buf.ctypes.data,
+                                   buf.nbytes)
+    if n == 0:
+        raise RuntimeError("reference compress failed")
+    return buf[: n // 8]
+
+
+def ref_decompress_params(words, shape, dtype, params: tuple) -> np.ndarray:
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    # zfp's reader may look a word past the stream: give it zeros there
+    padded = np.concatenate([words, np.zeros(72, np.uint64)])
+    out = np.zeros(tuple(shape), dtype)
+    nx, ny, nz = dims3(shape)
+    if not ref().zref_decompress_params(type_code(dtype), nx, ny, nz, *params,
+                                        padded.ctypes.data, padded.nbytes, out.ctypes.data):
+        raise RuntimeError("reference decompress failed")
+    return out

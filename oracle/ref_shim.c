@@ -381,3 +381,82 @@ int zref_decode_blocks(int type, int dims, unsigned maxbits, const void* buffer,
                        void* tiles) {
   return blocks(type, dims, maxbits, tiles, index, shape, count, (void*)buffer, bytes, 0);
 }
+
+/* zfp's general parameters (zfp_stream_set_params, Z/src/zfp.c:499-510;
+   fixed precision and fixed accuracy are two settings of them,
+   zfp_stream_set_precision / _accuracy, :432-458): zfp_compress and
+   zfp_decompress for float and double fields; integer arrays (whole blocks
+   only) through the per-block API in zfp's block order.  Blocks follow one
+   another at their own lengths. */
+static size_t params_array(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                           unsigned maxbits, unsigned maxprec, int minexp, void* data,
+                           void* buffer, size_t capacity, int encode) {
+  const int dims = nz ? 3 : ny ? 2 : 1;
+  const unsigned NY = ny ? ny : 1, NZ = nz ? nz : 1;
+  zfp_field* field = make_field(type, nx, ny, nz, data);
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  size_t result = 0;
+  if (zfp_stream_set_params(zfp, minbits, maxbits, maxprec, minexp) &&
+      (!encode || zfp_stream_maximum_size(zfp, field) <= capacity)) {
+    bitstream* s = stream_open(buffer, capacity);
+    zfp_stream_set_bit_stream(zfp, s);
+    zfp_stream_rewind(zfp);
+    if (type == zfp_type_float || type == zfp_type_double) {
+      result = encode ? zfp_compress(zfp, field) : (size_t)zfp_decompress(zfp, field);
+    } else if (!(nx % 4 || (dims >= 2 && NY % 4) || (dims == 3 && NZ % 4))) {
+      int64 blk[64];
+      unsigned bx, by, bz;
+      for (bz = 0; bz < (dims == 3 ? NZ / 4 : 1); bz++)
+        for (by = 0; by < (dims >= 2 ? NY / 4 : 1); by++)
+          for (bx = 0; bx < nx / 4; bx++) {
+            if (encode) int_block_io(type, dims, nx, NY, NZ, bx, by, bz, data, blk, 1);
+            int_block_codec(zfp, type, dims, blk, encode);
+            if (!encode) int_block_io(type, dims, nx, NY, NZ, bx, by, bz, data, blk, 0);
+          }
+      if (encode) stream_flush(s);
+      result = encode ? stream_size(s) : 1;
+    }
+    stream_close(s);
+  }
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return result;
+}
+
+size_t zref_compress_params(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                            unsigned maxbits, unsigned maxprec, int minexp, const void* data,
+                            void* buffer, size_t capacity) {
+  return params_array(type, nx, ny, nz, minbits, maxbits, maxprec, minexp, (void*)data, buffer,
+                      capacity, 1);
+}
+
+int zref_decompress_params(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                           unsigned maxbits, unsigned maxprec, int minexp, const void* buffer,
+                           size_t bytes, void* out) {
+  return params_array(type, nx, ny, nz, minbits, maxbits, maxprec, minexp, out, (void*)buffer,
+                      bytes, 0) != 0;
+}
+
+static void stream_params(const zfp_stream* zfp, unsigned* minbits, unsigned* maxbits,
+                          unsigned* maxprec, int* minexp) {
+  *minbits = zfp->minbits;
+  *maxbits = zfp->maxbits;
+  *maxprec = zfp->maxprec;
+  *minexp = zfp->minexp;
+}
+
+void zref_set_precision(int type, unsigned precision, unsigned* minbits, unsigned* maxbits,
+                        unsigned* maxprec, int* minexp) {
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_precision(zfp, precision, (zfp_type)type);
+  stream_params(zfp, minbits, maxbits, maxprec, minexp);
+  zfp_stream_close(zfp);
+}
+
+void zref_set_accuracy(int type, double tolerance, unsigned* minbits, unsigned* maxbits,
+                       unsigned* maxprec, int* minexp) {
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  zfp_stream_set_accuracy(zfp, tolerance, (zfp_type)type);
+  stream_params(zfp, minbits, maxbits, maxprec, minexp);
+  zfp_stream_close(zfp);
+}

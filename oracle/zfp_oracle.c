@@ -228,6 +228,11 @@ typedef struct {
   unsigned nx, ny, nz; /* per-axis sizes (1 for unused axes) */
   unsigned bx, by, bz; /* blocks per axis */
   unsigned maxbits;
+  /* the rest of zfp_stream's parameters (Z/inc/zfp.h:129-135); fixed rate
+     as zfp_stream_set_rate leaves them: minbits = maxbits, maxprec = P,
+     minexp = ZFP_MIN_EXP */
+  unsigned minbits, maxprec;
+  int minexp;
   int P;      /* bits per integer: 32 or 64 */
   int ebits;  /* exponent bits: 8 or 11 */
   int ebias;  /* 127 or 1023 */
@@ -256,6 +261,9 @@ static int setup_bits(params* p, int type, unsigned nx, unsigned ny, unsigned nz
   p->maxbits = maxbits;
   if (p->maxbits == 0) return 0;
   p->P = type == GZO_FLOAT || type == GZO_INT32 ? 32 : 64;
+  p->minbits = maxbits;
+  p->maxprec = (unsigned)p->P;
+  p->minexp = GZO_MIN_EXP;
   /* integer blocks carry no exponent (Z/src/template/encode.c:176-185) */
   p->ebits = type == GZO_FLOAT ? 8 : type == GZO_DOUBLE ? 11 : 0;
   p->ebias = p->ebits ? (1 << (p->ebits - 1)) - 1 : 0;
@@ -330,9 +338,26 @@ static unsigned encode_planes(wbits* w, unsigned budget, int intprec, int kmin,
   return budget - bits;
 }
 
-/* integer block: decorrelating transform, order, embedded coding of the
-   whole budget with maxprec 64 (kmin 0), zero padding to maxbits
-   (encode_block for Int, Z/src/template/encode.c:154-171, called by
+/* lowest plane an integer block codes: P - maxprec (Z/src/template/
+   encode.c:127, kmin) */
+static int int_kmin(const params* p) {
+  return (unsigned)p->P > p->maxprec ? p->P - (int)p->maxprec : 0;
+}
+
+/* the planes a floating-point block with exponent emax codes: precision()
+   of Z/src/template/codec{1,2,3}.c, MIN(maxprec, MAX(0, emax - minexp +
+   2 * (dims + 1))) */
+static int float_precision(const params* p, int emax) {
+  int prec = emax - p->minexp + 2 * p->dims + 2;
+  if (prec < 0) prec = 0;
+  if (prec > (int)p->maxprec) prec = (int)p->maxprec;
+  if (prec > p->P) prec = p->P;
+  return prec;
+}
+
+/* integer block: decorrelating transform, order, embedded coding of up to
+   maxbits bits and maxprec planes, zero padding to minbits (encode_block
+   for Int, Z/src/template/encode.c:154-171, called by
    zfp_encode_block_int32_<d> / int64, :176-185) */
 static void encode_int_block(wbits* w, const params* p, const void* iblock) {
   int size = 1 << (2 * p->dims);
@@ -352,8 +377,8 @@ static void encode_int_block(wbits* w, const params* p, const void* iblock) {
     for (i = 0; i < size; i++)
       u[i] = ((uint64_t)q[perm[i]] + 0xaaaaaaaaaaaaaaaaull) ^ 0xaaaaaaaaaaaaaaaaull;
   }
-  unsigned used = encode_planes(w, p->maxbits, p->P, 0, u, size);
-  w_zeros(w, p->maxbits - used);
+  unsigned used = encode_planes(w, p->maxbits, p->P, int_kmin(p), u, size);
+  if (used < p->minbits) w_zeros(w, p->minbits - used);
 }
 
 static void encode_block(wbits* w, const params* p, const void* fblock) {
@@ -378,13 +403,12 @@ static void encode_block(wbits* w, const params* p, const void* fblock) {
     if (mx > 0) { int e; frexp(mx, &e); emax = e < 1 - p->ebias ? 1 - p->ebias : e; }
     else emax = -p->ebias;
   }
-  int prec = emax - GZO_MIN_EXP + 2 * p->dims + 2;
-  if (prec < 0) prec = 0;
-  if (prec > p->P) prec = p->P;
+  int prec = float_precision(p, emax);
   unsigned e = prec ? (unsigned)(emax + p->ebias) : 0;
   if (!e) {
-    /* all-zero block: one 0 bit, then zero padding up to maxbits */
-    w_zeros(w, p->maxbits);
+    /* all-zero block (or nothing above minexp): one 0 bit, then zero
+       padding up to minbits */
+    w_zeros(w, p->minbits > 1 ? p->minbits : 1);
     return;
   }
   unsigned hbits = (unsigned)p->ebits + 1;
@@ -410,7 +434,7 @@ static void encode_block(wbits* w, const params* p, const void* fblock) {
   }
   unsigned budget = p->maxbits - hbits;
   unsigned used = encode_planes(w, budget, p->P, p->P - prec, u, size);
-  w_zeros(w, budget - used);
+  if (used + hbits < p->minbits) w_zeros(w, p->minbits - hbits - used);
 }
 
 /* pad rule of Z/src/template/encode.c:55-74 expressed as an index map */
@@ -441,8 +465,8 @@ static void gather(const params* p, const void* data, unsigned bx, unsigned by, 
 
 /* ------------------------------------------------------------- decoder --- */
 
-static void decode_planes(rbits* r, unsigned budget, int intprec, int kmin, uint64_t* u,
-                          int size) {
+static unsigned decode_planes(rbits* r, unsigned budget, int intprec, int kmin, uint64_t* u,
+                              int size) {
   unsigned bits = budget;
   int k = intprec, n = 0, i;
   for (i = 0; i < size; i++) u[i] = 0;
@@ -465,6 +489,7 @@ static void decode_planes(rbits* r, unsigned budget, int intprec, int kmin, uint
     }
     for (i = 0; x; i++, x >>= 1) u[i] += (x & 1u) << k;
   }
+  return budget - bits;
 }
 
 /* inverse of encode_int_block (zfp_decode_block_int32_<d> / int64) */
@@ -473,8 +498,8 @@ static void decode_int_block(rbits* r, const params* p, void* iblock) {
   int i;
   size_t start = r->bit;
   uint64_t u[64];
-  decode_planes(r, p->maxbits, p->P, 0, u, size);
-  r->bit = start + p->maxbits;
+  unsigned used = decode_planes(r, p->maxbits, p->P, int_kmin(p), u, size);
+  r->bit = start + (used < p->minbits ? p->minbits : used);
   const unsigned char* perm = perm_for(p->dims);
   if (p->P == 32) {
     int32_t q[64];
@@ -502,17 +527,15 @@ static void decode_block(rbits* r, const params* p, void* fblock) {
   if (!r_get(r, 1)) {
     if (p->type == GZO_FLOAT) for (i = 0; i < size; i++) ((float*)fblock)[i] = 0;
     else for (i = 0; i < size; i++) ((double*)fblock)[i] = 0;
-    r->bit = start + p->maxbits;
+    r->bit = start + (p->minbits > 1 ? p->minbits : 1);
     return;
   }
   unsigned hbits = (unsigned)p->ebits + 1;
   int emax = (int)r_get(r, (unsigned)p->ebits) - p->ebias;
-  int prec = emax - GZO_MIN_EXP + 2 * p->dims + 2;
-  if (prec < 0) prec = 0;
-  if (prec > p->P) prec = p->P;
+  int prec = float_precision(p, emax);
   uint64_t u[64];
-  decode_planes(r, p->maxbits - hbits, p->P, p->P - prec, u, size);
-  r->bit = start + p->maxbits;
+  unsigned used = hbits + decode_planes(r, p->maxbits - hbits, p->P, p->P - prec, u, size);
+  r->bit = start + (used < p->minbits ? p->minbits : used);
   const unsigned char* perm = perm_for(p->dims);
   if (p->type == GZO_FLOAT) {
     int32_t q[64];
@@ -950,4 +973,124 @@ int gzo_encode_blocks(int type, int dims, unsigned maxbits, const void* tiles,
   }
   free(tmp);
   return 1;
+}
+
+/* ------------------------------------------------ general stream params --- */
+
+/* zfp_stream_set_precision (Z/src/zfp.c:432-441) and
+   zfp_stream_set_accuracy (:443-458): blocks of up to ZFP_MAX_BITS = 4171
+   bits and no minimum, coded down to a number of planes or to an absolute
+   exponent */
+void gzo_mode_precision(int type, unsigned precision, unsigned* minbits, unsigned* maxbits,
+                        unsigned* maxprec, int* minexp) {
+  unsigned P = type == GZO_FLOAT || type == GZO_INT32 ? 32 : 64;
+  *minbits = 0;
+  *maxbits = 4171;
+  *maxprec = precision ? (precision < P ? precision : P) : P;
+  *minexp = GZO_MIN_EXP;
+}
+
+void gzo_mode_accuracy(int type, double tolerance, unsigned* minbits, unsigned* maxbits,
+                       unsigned* maxprec, int* minexp) {
+  int emin = GZO_MIN_EXP;
+  if (tolerance > 0) {
+    frexp(tolerance, &emin); /* tolerance = x * 2^emin, 0.5 <= x < 1 */
+    emin--;
+  }
+  *minbits = 0;
+  *maxbits = 4171;
+  *maxprec = type == GZO_FLOAT || type == GZO_INT32 ? 32 : 64;
+  *minexp = emin;
+}
+
+static int setup_params(params* p, int type, unsigned nx, unsigned ny, unsigned nz,
+                        unsigned minbits, unsigned maxbits, unsigned maxprec, int minexp) {
+  /* zfp_stream_set_params' checks (Z/src/zfp.c:499-510), and room for the
+     block header that every nonzero floating-point block writes */
+  if (minbits > maxbits || maxprec == 0 || maxprec > 64) return 0;
+  if (!setup_bits(p, type, nx, ny, nz, maxbits)) return 0;
+  if (maxbits < (unsigned)p->ebits + 1) return 0;
+  p->minbits = minbits;
+  p->maxprec = maxprec;
+  p->minexp = minexp;
+  return 1;
+}
+
+/* the most bits a block can take: zfp_stream_maximum_size's per-block bound
+   (Z/src/zfp.c:368-397) */
+static unsigned block_bound(const params* p) {
+  unsigned values = 1u << (2 * p->dims);
+  unsigned prec = p->maxprec < (unsigned)p->P ? p->maxprec : (unsigned)p->P;
+  unsigned b = 1 + (unsigned)p->ebits + values - 1 + values * prec;
+  if (b > p->maxbits) b = p->maxbits;
+  if (b < p->minbits) b = p->minbits;
+  return b;
+}
+
+size_t gzo_bound_params(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                        unsigned maxbits, unsigned maxprec, int minexp) {
+  params p;
+  if (!setup_params(&p, type, nx, ny, nz, minbits, maxbits, maxprec, minexp)) return 0;
+  return (size_t)(((uint64_t)p.bx * p.by * p.bz * block_bound(&p) + 63) / 64 * 8);
+}
+
+/* zfp_compress with these parameters: every block right after the
+   previous one, in zfp's block order, then a flush to a whole word.  The
+   start bit of every block goes to offsets[] when it is given.  Returns
+   the stream size in bytes, 0 on a bad argument or a buffer smaller than
+   the bound above. */
+size_t gzo_compress_params(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                           unsigned maxbits, unsigned maxprec, int minexp, const void* data,
+                           void* stream, size_t capacity, unsigned long long* offsets) {
+  params p;
+  wbits w;
+  uint64_t b, nblocks, pos = 0;
+  double blk[64];
+  if (!setup_params(&p, type, nx, ny, nz, minbits, maxbits, maxprec, minexp)) return 0;
+  if (capacity < gzo_bound_params(type, nx, ny, nz, minbits, maxbits, maxprec, minexp)) return 0;
+  w_init(&w, (uint64_t*)stream, 0);
+  nblocks = (uint64_t)p.bx * p.by * p.bz;
+  for (b = 0; b < nblocks; b++) {
+    unsigned bx = (unsigned)(b % p.bx);
+    unsigned by = (unsigned)((b / p.bx) % p.by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p.bx * p.by));
+    if (offsets) offsets[b] = pos;
+    gather(&p, data, bx, by, bz, blk);
+    encode_block(&w, &p, blk);
+    pos = (uint64_t)w.pos * 64 + w.fill;
+  }
+  w_flush(&w);
+  return (size_t)((pos + 63) / 64 * 8);
+}
+
+/* zfp_decompress with these parameters; offsets[] (optional) receives every
+   block's start bit.  Returns 1, or 0 on a bad argument or a stream that
+   ends before its last block. */
+int gzo_decompress_params(int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                          unsigned maxbits, unsigned maxprec, int minexp, const void* stream,
+                          size_t bytes, void* data, unsigned long long* offsets) {
+  params p;
+  rbits r;
+  uint64_t b, nblocks;
+  double blk[64];
+  uint64_t* padded;
+  if (!setup_params(&p, type, nx, ny, nz, minbits, maxbits, maxprec, minexp)) return 0;
+  /* read through a copy with zero words after the end, as many as one
+     block can span (4171 bits) and the word a bit reader looks ahead */
+  padded = (uint64_t*)calloc(bytes / 8 + 70, 8);
+  if (!padded) return 0;
+  memcpy(padded, stream, bytes / 8 * 8);
+  r.words = padded;
+  r.bit = 0;
+  nblocks = (uint64_t)p.bx * p.by * p.bz;
+  for (b = 0; b < nblocks && r.bit <= bytes / 8 * 64; b++) {
+    unsigned bx = (unsigned)(b % p.bx);
+    unsigned by = (unsigned)((b / p.bx) % p.by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p.bx * p.by));
+    if (offsets) offsets[b] = r.bit;
+    decode_block(&r, &p, blk);
+    scatter(&p, data, bx, by, bz, blk);
+  }
+  free(padded);
+  return b == nblocks && r.bit <= bytes / 8 * 64;
 }

@@ -1,10 +1,10 @@
 """Regenerate the golden fixtures from the reference's own zfp 0.5.0 build.
 
 Run in a checkout that has the reference tree (the build reads its zfp
-sources):  python tests/golden/make_golden.py [--ints | --headed]
+sources):  python tests/golden/make_golden.py [--ints | --headed | --modes]
 Writes tests/golden/small_cases.npz, tests/golden/manifest.json,
-tests/golden/int_cases.npz and tests/golden/headed_cases.npz (only the
-integer or the headed cases with --ints / --headed).
+tests/golden/int_cases.npz, tests/golden/headed_cases.npz and
+tests/golden/mode_cases.npz (only one of the last three with a flag).
 """
 from __future__ import annotations
 
@@ -149,12 +149,47 @@ def write_headed_cases() -> None:
     print(f"{k} headed cases")
 
 
+def write_mode_cases() -> None:
+    """Streams of zfp's fixed-precision and fixed-accuracy modes and of
+    other parameter sets (zfp_stream_set_precision / _accuracy / _params,
+    then zfp_compress; integer arrays through the per-block API), stored in
+    full in tests/golden/mode_cases.npz with their parameters."""
+    if not orc.build_ref():
+        raise SystemExit("reference tree not found; cannot regenerate golden fixtures")
+    rng = np.random.default_rng(20261206)
+    arrays = {}
+    plan = []
+    for dt in ("float32", "float64"):
+        plan += [(dt, (203,), ("precision", 14)), (dt, (20, 36), ("accuracy", 1e-4)),
+                 (dt, (12, 9, 16), ("precision", 30)), (dt, (10, 11, 13), ("accuracy", 1e-9))]
+    for dt in ("int32", "int64"):
+        plan += [(dt, (64,), ("precision", 20)), (dt, (8, 12, 16), ("params", (64, 900, 48, -1074)))]
+    plan += [("float64", (33, 17), ("params", (100, 700, 40, -40)))]
+    for k, (dt, shape, (kind, v)) in enumerate(plan):
+        a = np.cumsum(rng.standard_normal(shape), axis=-1)
+        a = (a * 4096).astype(dt) if dt.startswith("int") else a.astype(dt)
+        pr = (orc.mode_precision(a.dtype, v, lib=orc.ref()) if kind == "precision" else
+              orc.mode_accuracy(a.dtype, v, lib=orc.ref()) if kind == "accuracy" else v)
+        s = orc.ref_compress_params(a, pr)
+        d = orc.ref_decompress_params(s, a.shape, a.dtype, pr)
+        nm = f"mode{k:02d}_{kind}_{a.ndim}d_{a.dtype.name}"
+        arrays[nm + "__input"] = a
+        arrays[nm + "__stream"] = s
+        arrays[nm + "__output"] = d
+        arrays[nm + "__params"] = np.array(pr, np.int64)
+    np.savez_compressed(os.path.join(OUT, "mode_cases.npz"), **arrays)
+    print(f"{len(plan)} mode cases")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--ints"]:
         write_int_cases()
     elif sys.argv[1:] == ["--headed"]:
         write_headed_cases()
+    elif sys.argv[1:] == ["--modes"]:
+        write_mode_cases()
     else:
         main()
         write_int_cases()
         write_headed_cases()
+        write_mode_cases()

@@ -64,3 +64,13 @@ def load_all() -> list[dict]:
 def headed_cases() -> list[dict]:
     """Streams that start with zfp's full header (headed_cases.npz)."""
     return small_cases("headed_cases.npz")
+
+
+def mode_cases() -> list[dict]:
+    """Streams of zfp's other modes (mode_cases.npz): each case carries its
+    (minbits, maxbits, maxprec, minexp)."""
+    z = np.load(os.path.join(GOLDEN, "mode_cases.npz"))
+    names = sorted({k.rsplit("__", 1)[0] for k in z.files})
+    return [{"name": nm, "input": z[nm + "__input"], "stream": z[nm + "__stream"],
+             "output": z[nm + "__output"], "params": tuple(int(v) for v in z[nm + "__params"])}
+            for nm in names]

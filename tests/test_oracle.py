@@ -398,3 +398,56 @@ def test_block_rewrite_keeps_neighbours(orc):
         orc.encode_blocks(tiles[pick], b.ndim, mb, pick, changed, codes[pick])
         assert np.array_equal(changed, orc.compress(b, rate)), (dt, shape)
         assert not np.array_equal(changed, s)
+
+
+# ------------------------------------------- general parameters (zfp modes)
+
+def _mode_list(orc, dt):
+    ms = [orc.mode_precision(dt, p) for p in (3, 10, 24, 64)]
+    ms += [orc.mode_accuracy(dt, t) for t in (1e-8, 1e-3, 0.5, 100.0)]
+    ms += [(100, 300, 40, -30), (0, 64, 64, -1074), (200, 200, 64, -1074), (0, 4171, 16, -20)]
+    lo = {np.float32: 9, np.float64: 12}.get(dt, 1)
+    return [m for m in ms if m[1] >= lo]
+
+
+def test_mode_setters_match_reference(ref):
+    """zfp_stream_set_precision / _accuracy restated: the same four
+    parameters for every type and a spread of arguments."""
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        for prec in (0, 1, 5, 12, 20, 31, 32, 40, 64, 100):
+            assert ref.mode_precision(dt, prec) == ref.mode_precision(dt, prec, lib=ref.ref())
+        for tol in (0, 1e-300, 1e-12, 1e-3, 0.1, 0.5, 1.0, 3.0, 1e10):
+            assert ref.mode_accuracy(dt, tol) == ref.mode_accuracy(dt, tol, lib=ref.ref())
+
+
+def test_general_params_match_reference(ref):
+    """Fixed precision, fixed accuracy and other parameter sets: the oracle's
+    variable-length streams equal zfp_compress's, and decode to
+    zfp_decompress's arrays."""
+    rng = np.random.default_rng(111)
+    n = 0
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        for shape in ((37,), (9, 13), (5, 6, 7), (64,), (16, 16), (8, 8, 12)):
+            if ref.is_int(dt) and any(s % 4 for s in shape):
+                continue
+            a = np.cumsum(rng.standard_normal(shape), axis=-1)
+            a = (a * 1000).astype(dt) if ref.is_int(dt) else a.astype(dt)
+            for pr in _mode_list(ref, dt):
+                s, offs = ref.compress_params(a, pr, with_offsets=True)
+                assert np.array_equal(s, ref.ref_compress_params(a, pr)), (dt, shape, pr)
+                d, offs2 = ref.decompress_params(s, shape, dt, pr, with_offsets=True)
+                assert np.array_equal(offs, offs2)
+                assert np.array_equal(d, ref.ref_decompress_params(s, shape, dt, pr)), (dt, shape)
+                n += 1
+    assert n > 150
+
+
+def test_general_params_golden(orc):
+    cs = golden_io.mode_cases()
+    assert len(cs) >= 12
+    for c in cs:
+        a = c["input"]
+        s = orc.compress_params(a, c["params"])
+        assert np.array_equal(s, c["stream"]), c["name"]
+        assert np.array_equal(orc.decompress_params(c["stream"], a.shape, a.dtype, c["params"]),
+                              c["output"]), c["name"]
