@@ -533,6 +533,131 @@ def encode_blocks(tiles, dims: int, maxbits: int, indices, words, shapes=None,
     return words
 
 
+# ------------------------------------------------------------ general modes
+# zfp's fixed-precision and fixed-accuracy modes and any other setting of
+# its four stream parameters (zfp_stream_set_precision / _accuracy /
+# _params, zfp-0.5.0/src/zfp.c:432-510): blocks of their own lengths.
+
+class Mode(ctypes.Structure):
+    _fields_ = [("minbits", _U), ("maxbits", _U), ("maxprec", _U), ("minexp", _I)]
+
+    def as_tuple(self) -> tuple:
+        return (self.minbits, self.maxbits, self.maxprec, self.minexp)
+
+
+_PM = ctypes.POINTER(Mode)
+_lib.gzfp_mode_rate.restype = _I
+_lib.gzfp_mode_rate.argtypes = [_I, _U, ctypes.c_double, _PM]
+_lib.gzfp_mode_precision.restype = _I
+_lib.gzfp_mode_precision.argtypes = [_I, _U, _PM]
+_lib.gzfp_mode_accuracy.restype = _I
+_lib.gzfp_mode_accuracy.argtypes = [_I, ctypes.c_double, _PM]
+_lib.gzfp_mode_maximum_size.restype = _SZ
+_lib.gzfp_mode_maximum_size.argtypes = [_I, _U, _U, _U, _PM]
+_lib.gzfp_compress_mode.restype = _I
+_lib.gzfp_compress_mode.argtypes = [_I, _U, _U, _U, _PM, _VP, _VP, _SZ, _P(_SZ), _VP, _VP]
+_lib.gzfp_decompress_mode.restype = _I
+_lib.gzfp_decompress_mode.argtypes = [_I, _U, _U, _U, _PM, _VP, _SZ, _VP, _VP, _VP]
+_lib.gzfp_index_blocks.restype = _I
+_lib.gzfp_index_blocks.argtypes = [_I, _U, _U, _U, _PM, _VP, _SZ, _VP, _VP]
+
+
+def mode_rate(type: zfp_type, dims: int, rate: float) -> Mode:
+    m = Mode()
+    _check(_lib.gzfp_mode_rate(int(type), dims, float(rate), ctypes.byref(m)), "mode_rate")
+    return m
+
+
+def mode_precision(type: zfp_type, precision: int) -> Mode:
+    m = Mode()
+    _check(_lib.gzfp_mode_precision(int(type), int(precision), ctypes.byref(m)), "mode_precision")
+    return m
+
+
+def mode_accuracy(type: zfp_type, tolerance: float) -> Mode:
+    m = Mode()
+    _check(_lib.gzfp_mode_accuracy(int(type), float(tolerance), ctypes.byref(m)), "mode_accuracy")
+    return m
+
+
+def mode_maximum_size(type: zfp_type, nx: int, ny: int, nz: int, mode: Mode) -> int:
+    return int(_lib.gzfp_mode_maximum_size(int(type), nx, ny, nz, ctypes.byref(mode)))
+
+
+def _nblocks(shape) -> int:
+    n = 1
+    for v in shape:
+        n *= (int(v) + 3) // 4
+    return n
+
+
+def compress_mode(x, mode: Mode, with_offsets: bool = False, cuda_stream: Any = None):
+    """Compress a contiguous CUDA tensor or numpy array under `mode`; returns
+    the stream words (trimmed to the stream's size) and, with_offsets, every
+    block's start bit (int64, on the same side as the input)."""
+    t = _type_of(x.dtype)
+    nx, ny, nz = _dims_of(x.shape)
+    cap = mode_maximum_size(t, nx, ny, nz, mode)
+    if cap == 0:
+        raise GzfpError(GZFP_ERR_ARG, "bad mode or shape")
+    nb = _nblocks(x.shape)
+    if hasattr(x, "data_ptr"):
+        import torch
+        out = torch.empty(cap // 8, dtype=torch.int64, device=x.device)
+        offs = torch.empty(nb, dtype=torch.int64, device=x.device) if with_offsets else None
+    else:
+        import numpy as np
+        out = np.empty(cap // 8, np.uint64)
+        offs = np.empty(nb, np.uint64) if with_offsets else None
+    got = _SZ(0)
+    _check(_lib.gzfp_compress_mode(int(t), nx, ny, nz, ctypes.byref(mode), _addr_and_size(x)[0],
+                                   _addr_and_size(out)[0], cap, ctypes.byref(got),
+                                   _addr_and_size(offs)[0] if offs is not None else None,
+                                   _cuda_stream_handle(cuda_stream)), "compress_mode")
+    words = out[: got.value // 8]
+    return (words, offs) if with_offsets else words
+
+
+def decompress_mode(words, shape, dtype, mode: Mode, offsets=None, out=None,
+                    cuda_stream: Any = None):
+    """Decompress a stream written under `mode`; `offsets` (the blocks' start
+    bits, as compress_mode returns them) lets every block decode at once."""
+    t = _type_of(dtype)
+    nx, ny, nz = _dims_of(shape)
+    if out is None:
+        if hasattr(words, "data_ptr"):
+            import torch
+            out = torch.empty(tuple(shape), dtype=dtype, device=words.device)
+        else:
+            import numpy as np
+            out = np.empty(tuple(shape), dtype)
+    src, size = _addr_and_size(words)
+    _check(_lib.gzfp_decompress_mode(int(t), nx, ny, nz, ctypes.byref(mode), src, size,
+                                     _addr_and_size(offsets)[0] if offsets is not None else None,
+                                     _addr_and_size(out)[0], _cuda_stream_handle(cuda_stream)),
+           "decompress_mode")
+    return out
+
+
+def index_blocks(words, shape, dtype, mode: Mode, cuda_stream: Any = None):
+    """Every block's start bit in a stream written under `mode` (one GPU
+    thread walks the blocks)."""
+    t = _type_of(dtype)
+    nx, ny, nz = _dims_of(shape)
+    nb = _nblocks(shape)
+    if hasattr(words, "data_ptr"):
+        import torch
+        offs = torch.empty(nb, dtype=torch.int64, device=words.device)
+    else:
+        import numpy as np
+        offs = np.empty(nb, np.uint64)
+    src, size = _addr_and_size(words)
+    _check(_lib.gzfp_index_blocks(int(t), nx, ny, nz, ctypes.byref(mode), src, size,
+                                  _addr_and_size(offs)[0], _cuda_stream_handle(cuda_stream)),
+           "index_blocks")
+    return offs
+
+
 def version() -> int:
     return int(_lib.gzfp_version())
 
@@ -760,5 +885,7 @@ __all__ = [
     "batch_stream_buffers", "ServeRequest", "ServeResult", "ServeConfig", "ServeStats",
     "default_serve_config", "serve_request", "serve", "GZFP_SERVE_COMPRESS",
     "GZFP_SERVE_DECOMPRESS", "HEADER_MAX_BITS", "write_header", "read_header", "headed_size",
-    "compress_headed", "decompress_headed", "decode_blocks", "encode_blocks",
+    "compress_headed", "decompress_headed", "decode_blocks", "encode_blocks", "Mode",
+    "mode_rate", "mode_precision", "mode_accuracy", "mode_maximum_size", "compress_mode",
+    "decompress_mode", "index_blocks",
 ]

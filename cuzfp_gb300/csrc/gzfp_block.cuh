@@ -779,19 +779,63 @@ GZ_HD void front_end_int(const typename FT<T>::UInt* raw, typename FT<T>::UInt* 
   for (int i = 0; i < BS; i++) u[i] = (UInt)(((UInt)q[Perm<D>::at(i)] + (UInt)F::NB) ^ (UInt)F::NB);
 }
 
-// Encode one block of raw IEEE bit patterns (gathered and padded) into
-// exactly maxbits bits (Z/src/template/encode.c:154-234).
+// ----------------------------------------------------------- coding modes
+// zfp's four stream parameters (zfp_stream minbits, maxbits, maxprec,
+// minexp; Z/inc/zfp.h:129-135).  FixedRate is the setting of
+// zfp_stream_set_rate -- minbits = maxbits, maxprec = the type's precision,
+// minexp = ZFP_MIN_EXP -- with only maxbits left open, which is what the
+// fixed-rate kernels compile; General holds all four (fixed precision,
+// fixed accuracy, or any setting of zfp_stream_set_params).
+struct FixedRate {
+  static constexpr bool kGeneral = false;
+  uint32_t maxbits;
+  GZ_HD uint32_t min_bits() const { return maxbits; }
+  // planes a floating-point block codes: precision() of
+  // Z/src/template/codec{1,2,3}.c with maxprec = P, minexp = ZFP_MIN_EXP
+  template <int D, int P>
+  GZ_HD int precision(int emax) const {
+    const int prec = emax - kMinExp + 2 * D + 2;
+    return prec < 0 ? 0 : prec > P ? P : prec;
+  }
+  template <int P>
+  GZ_HD int int_kmin() const { return 0; }
+};
+
+struct General {
+  static constexpr bool kGeneral = true;
+  uint32_t minbits, maxbits, maxprec;
+  int minexp;
+  GZ_HD uint32_t min_bits() const { return minbits; }
+  // MIN(maxprec, MAX(0, emax - minexp + 2 * (D + 1))), at most P
+  template <int D, int P>
+  GZ_HD int precision(int emax) const {
+    int prec = emax - minexp + 2 * D + 2;
+    prec = prec < 0 ? 0 : prec;
+    prec = prec > (int)maxprec ? (int)maxprec : prec;
+    return prec > P ? P : prec;
+  }
+  // lowest plane of an integer block: P - maxprec (Z/src/template/encode.c:127)
+  template <int P>
+  GZ_HD int int_kmin() const { return (uint32_t)P > maxprec ? P - (int)maxprec : 0; }
+};
+
+// Encode one block of raw IEEE bit patterns (gathered and padded)
+// (Z/src/template/encode.c:154-234): exactly maxbits bits in fixed-rate
+// mode; in general mode as many as the block takes (at most maxbits, at
+// least minbits).  Returns the bits written.
 //
 // 4^3 double blocks are coded one 32-bit slice (32 planes) at a time; the
 // bottom slice waits in plane-store slots 32..63 while the top one is coded,
 // so only half of the block's coefficients stay in registers.
-template <int D, typename T, class W, class PS>
-GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps) {
+template <int D, typename T, class Mode, class W, class PS>
+GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mode, W& w,
+                                 PS& ps) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   constexpr int P = F::P;
   typedef Planes<D, P> PL;
+  const uint32_t maxbits = mode.maxbits;
 
   UInt u[BS];
   uint32_t bits;
@@ -799,7 +843,7 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
   if constexpr (F::INT) {
     front_end_int<D, T>(raw, u);
     bits = maxbits;
-    kmin = 0;
+    kmin = mode.template int_kmin<P>();
   } else {
     // largest exponent field and a nonzero test, from the IEEE bits
     uint32_t maxh = 0, orl = 0;
@@ -809,20 +853,30 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
       maxh = h > maxh ? h : maxh;
       if (P == 64) orl |= (uint32_t)raw[i];
     }
-    if ((maxh | orl) == 0) {  // all zero: one 0 bit, zero padding
-      w.zeros(maxbits);
-      return;
+    if constexpr (!Mode::kGeneral) {
+      if ((maxh | orl) == 0) {  // all zero: one 0 bit, zero padding
+        w.zeros(maxbits);
+        return maxbits;
+      }
     }
     const int maxE = (int)(maxh >> (F::MANT - (P - 32)));
     const int emax = maxE - (F::EBIAS - 1);  // frexp exponent, >= 1 - EBIAS
-    int prec = emax - kMinExp + 2 * D + 2;
-    prec = prec < 0 ? 0 : prec > P ? P : prec;
+    const int prec = mode.template precision<D, P>(emax);
+    if constexpr (Mode::kGeneral) {
+      // all zero, or nothing above minexp: one 0 bit, zero padding to minbits
+      if ((maxh | orl) == 0 || prec == 0) {
+        const uint32_t z = mode.min_bits() > 1 ? mode.min_bits() : 1;
+        w.zeros(z);
+        return z;
+      }
+    }
     const uint32_t e = (uint32_t)(emax + F::EBIAS);
     w.put(2 * (uint64_t)e + 1, F::EBITS + 1);
     front_end<D, T>(raw, emax, u);
     bits = maxbits - (F::EBITS + 1);
     kmin = P - prec;
   }
+  const uint32_t budget = bits;
   uint32_t n = 0;
   int k = P - 1;
   if constexpr (BS == 64 && P == 64) {
@@ -861,36 +915,53 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
       return (uint64_t)((word >> (g * PL::N)) & ((1u << PL::N) - 1));
     });
   }
-  w.zeros(bits);
+  if constexpr (!Mode::kGeneral) {
+    w.zeros(bits);  // pad to exactly maxbits
+    return maxbits;
+  } else {
+    const uint32_t used = (maxbits - budget) + (budget - bits);  // header + coded planes
+    const uint32_t pad = used < mode.minbits ? mode.minbits - used : 0;
+    w.zeros(pad);
+    return used + pad;
+  }
+}
+
+template <int D, typename T, class W, class PS>
+GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w, PS& ps) {
+  encode_block_mode<D, T>(raw, FixedRate{maxbits}, w, ps);
 }
 
 // Decode one block from a reader positioned at its first bit into raw IEEE
-// bit patterns (Z/src/template/decode.c:137-165).
-template <int D, typename T, class R, class PS>
-GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& ps) {
+// bit patterns (Z/src/template/decode.c:137-165).  Returns the bits the
+// block takes in the stream (fixed rate: maxbits; the reader is not moved
+// past a block's padding).
+template <int D, typename T, class Mode, class R, class PS>
+GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* raw, PS& ps) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
   constexpr int BS = 1 << (2 * D);
   constexpr int P = F::P;
   typedef Planes<D, P> PL;
+  const uint32_t maxbits = mode.maxbits;
 
   int emax = 0, kmin = 0;
   uint32_t bits = maxbits;
-  if constexpr (!F::INT) {
+  if constexpr (F::INT) {
+    kmin = mode.template int_kmin<P>();
+  } else {
     const uint64_t head = r.peek64();
     if (!(head & 1)) {
 #pragma unroll
       for (int i = 0; i < BS; i++) raw[i] = 0;
-      return;
+      return mode.min_bits() > 1 ? mode.min_bits() : 1;
     }
     r.skip(F::EBITS + 1);
     emax = (int)((head >> 1) & ((1u << F::EBITS) - 1)) - F::EBIAS;
-    int prec = emax - kMinExp + 2 * D + 2;
-    prec = prec < 0 ? 0 : prec > P ? P : prec;
-    kmin = P - prec;
+    kmin = P - mode.template precision<D, P>(emax);
     bits = maxbits - (F::EBITS + 1);
   }
+  const uint32_t budget = bits;
 
   uint32_t n = 0;
   int k = P - 1;
@@ -942,6 +1013,42 @@ GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& p
   } else {
     dequantize(q, raw, BS, emax);
   }
+  const uint32_t used = (maxbits - budget) + (budget - bits);
+  return used < mode.min_bits() ? mode.min_bits() : used;
+}
+
+template <int D, typename T, class R, class PS>
+GZ_HD void decode_block(R& r, uint32_t maxbits, typename FT<T>::UInt* raw, PS& ps) {
+  decode_block_mode<D, T>(r, FixedRate{maxbits}, raw, ps);
+}
+
+// The bits a block takes in a general-mode stream, from a reader at its
+// first bit: the plane decoding of decode_block without the deposit, the
+// transform or the values (for locating the blocks of a stream whose block
+// offsets are not known).
+template <int D, typename T, class R>
+GZ_HD uint32_t block_bits(R& r, const General& mode) {
+  typedef FT<T> F;
+  constexpr int BS = 1 << (2 * D);
+  constexpr int P = F::P;
+  int kmin;
+  uint32_t bits = mode.maxbits, hdr = 0;
+  if constexpr (F::INT) {
+    kmin = mode.template int_kmin<P>();
+  } else {
+    const uint64_t head = r.peek64();
+    if (!(head & 1)) return mode.minbits > 1 ? mode.minbits : 1;
+    r.skip(F::EBITS + 1);
+    const int emax = (int)((head >> 1) & ((1u << F::EBITS) - 1)) - F::EBIAS;
+    kmin = P - mode.template precision<D, P>(emax);
+    hdr = F::EBITS + 1;
+    bits -= hdr;
+  }
+  const uint32_t budget = bits;
+  uint32_t n = 0;
+  uncode_planes<BS>(P - 1, kmin, n, bits, r, [](int, uint64_t) {});
+  const uint32_t used = hdr + (budget - bits);
+  return used < mode.minbits ? mode.minbits : used;
 }
 
 // Plane store backed by a plain array (host builds and tests).

@@ -1,0 +1,17 @@
+// General-mode kernels (fixed precision, fixed accuracy, any zfp stream
+// parameters) for int32 fields.
+#include "gzfp_launch.h"
+#include "gzfp_modes.cuh"
+
+namespace gzfp {
+
+template cudaError_t launch_encode_mode<int32_t>(int, const int32_t*, const Geom&, const General&,
+                                            uint64_t*, uint32_t, uint32_t*, cudaStream_t);
+template cudaError_t launch_decode_mode<int32_t>(int, const uint64_t*, uint64_t,
+                                            const unsigned long long*, const Geom&,
+                                            const General&, int32_t*, cudaStream_t);
+template cudaError_t launch_index_blocks<int32_t>(int, const uint64_t*, uint64_t, uint64_t,
+                                             const General&, unsigned long long*,
+                                             unsigned long long*, cudaStream_t);
+
+}  // namespace gzfp

@@ -168,6 +168,56 @@ int gzfp_encode_blocks(int type, unsigned dims, unsigned maxbits, const void* ti
                        const unsigned long long* indices, const unsigned char* shapes,
                        size_t count, void* stream, size_t bytes, void* cuda_stream);
 
+/* ------------------------------------------------------ general modes ---
+   zfp's other compression modes -- fixed precision, fixed accuracy, or any
+   setting of its four stream parameters (zfp_stream_set_precision,
+   zfp_stream_set_accuracy, zfp_stream_set_params; zfp-0.5.0/src/zfp.c:
+   432-510) -- in which every block takes as many bits as it needs (at
+   least minbits, at most maxbits) and follows the previous one directly.
+   The stream is the one zfp_compress writes with those parameters.
+   No counterpart in cuZFP, which is fixed-rate only
+   (src/utils/cuda_zfp.cpp:350-354). */
+typedef struct {
+  unsigned minbits;  /* fewest bits per block */
+  unsigned maxbits;  /* most bits per block */
+  unsigned maxprec;  /* most bit planes per block, 1..64 */
+  int minexp;        /* exponent of the lowest bit plane coded (floating point) */
+} gzfp_mode;
+
+/* The parameters zfp_stream_set_rate (wra = 0), zfp_stream_set_precision
+   and zfp_stream_set_accuracy set. */
+int gzfp_mode_rate(int type, unsigned dims, double rate, gzfp_mode* mode);
+int gzfp_mode_precision(int type, unsigned precision, gzfp_mode* mode);
+int gzfp_mode_accuracy(int type, double tolerance, gzfp_mode* mode);
+
+/* Bytes a stream can take at most (zfp_stream_maximum_size without the
+   header allowance); 0 for bad arguments. */
+size_t gzfp_mode_maximum_size(int type, unsigned nx, unsigned ny, unsigned nz,
+                              const gzfp_mode* mode);
+
+/* Compress.  Every block is coded on the GPU into a scratch slot of its
+   largest size, the start bits follow from a scan of the block lengths,
+   and the blocks are moved into place: the call returns when the stream
+   is complete (its size is only known then).  `offsets` (optional, host or
+   device, one entry per block) receives every block's start bit; keep them
+   to decode in parallel.  Fixed-rate parameters take the fixed-rate path. */
+int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                       const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                       unsigned long long* offsets, void* cuda_stream);
+
+/* Decompress.  With `offsets` every block decodes in parallel from its
+   start bit; without, gzfp_index_blocks finds them first. */
+int gzfp_decompress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                         const void* stream, size_t bytes, const unsigned long long* offsets,
+                         void* data, void* cuda_stream);
+
+/* Every block's start bit in a stream written with `mode` (by zfp or by
+   gzfp_compress_mode), found by one GPU thread walking the blocks in
+   order: its time grows with the number of blocks, not with the GPU. */
+int gzfp_index_blocks(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                      const void* stream, size_t bytes, unsigned long long* offsets,
+                      void* cuda_stream);
+
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and
    bits per block -- coded by one persistent kernel over a device-side work

@@ -191,3 +191,34 @@ def test_header_modes_abi(gz, idx):
         with pytest.raises(gz.GzfpError) as e:
             gz.read_header(w)
         assert e.value.status == gz.GZFP_ERR_UNSUPPORTED
+
+
+def test_mode_setters_match_oracle(gz, orc):
+    """gzfp_mode_precision / _accuracy / _rate give zfp's parameters (the
+    oracle's restatement, itself pinned to the reference)."""
+    for t, dt in ((1, np.int32), (2, np.int64), (3, np.float32), (4, np.float64)):
+        for prec in (0, 1, 7, 32, 40, 64, 99):
+            assert gz.mode_precision(t, prec).as_tuple() == orc.mode_precision(dt, prec)
+        for tol in (0.0, 1e-300, 1e-9, 0.25, 1.0, 7.5, 1e12):
+            assert gz.mode_accuracy(t, tol).as_tuple() == orc.mode_accuracy(dt, tol)
+        m = gz.mode_rate(t, 3, 16.0)
+        assert m.minbits == m.maxbits == 1024 and m.minexp == -1074
+
+
+def test_mode_maximum_size_matches_oracle(gz, orc):
+    for t, dt in ((3, np.float32), (4, np.float64), (1, np.int32), (2, np.int64)):
+        for shape in ((1,), (203,), (9, 13), (5, 6, 7), (64, 64, 64)):
+            nx, ny, nz = orc.dims3(shape)
+            for pr in ((0, 4171, 20, -1074), (0, 4171, 64, -30), (100, 300, 40, -30),
+                       (64, 64, 64, -1074)):
+                got = gz.mode_maximum_size(t, nx, ny, nz, gz.Mode(*pr))
+                assert got == orc.port().gzo_bound_params(t, nx, ny, nz, *pr), (t, shape, pr)
+
+
+def test_mode_argument_errors(gz):
+    bad = [gz.Mode(10, 5, 64, -1074), gz.Mode(0, 4171, 0, -1074), gz.Mode(0, 4171, 65, -1074)]
+    for m in bad:
+        assert gz.mode_maximum_size(4, 8, 8, 8, m) == 0
+    assert gz.mode_maximum_size(3, 8, 8, 8, gz.Mode(0, 8, 32, -1074)) == 0  # under the block header
+    with pytest.raises(gz.GzfpError):
+        gz.mode_accuracy(4, float("nan"))
