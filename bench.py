@@ -51,10 +51,14 @@ def parse():
     p.add_argument("--edge", type=int, default=512,
                    help="cube edge of the field (smaller cases for profiling)")
     p.add_argument("--rate", type=float, default=16.0)
-    p.add_argument("--workload", default="plain3d", choices=["plain3d", "batched", "serving"],
+    p.add_argument("--workload", default="plain3d",
+                   choices=["plain3d", "batched", "serving", "accuracy"],
                    help="plain3d: the 1 GiB 3D float64 field (default); batched: 512 mixed "
                         "3D arrays in one persistent launch vs 512 plain launches; serving: "
-                        "Poisson request arrivals through the request server")
+                        "Poisson request arrivals through the request server; accuracy: the "
+                        "plain3d field in zfp's fixed-accuracy mode")
+    p.add_argument("--tolerance", type=float, default=1e-6,
+                   help="accuracy workload: absolute error tolerance")
     p.add_argument("--arrays", type=int, default=512, help="batched workload: array count")
     p.add_argument("--requests", type=int, default=20000, help="serving workload: requests")
     p.add_argument("--inflight", type=int, default=3, help="serving workload: batches in flight")
@@ -503,6 +507,93 @@ def run_serving(args, rank, world, local):
     print(json.dumps(res_line), flush=True)
 
 
+def run_accuracy(args, rank, world, local):
+    """The plain3d field in zfp's fixed-accuracy mode: variable-length blocks,
+    compressed on the device with their start bits and decompressed from
+    them (each call ends when its result is complete).  Also times the
+    serial block walk that decoding needs without start bits, on a 64^3
+    field."""
+    import torch
+
+    import cuzfp_gb300 as gz
+    from cuzfp_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    field = synth.sinusoids_device(SHAPE, 16, 32, seed=rank, dtype=torch.float64, device=dev)
+    nbytes = field.numel() * field.element_size()
+    mode = gz.mode_accuracy(gz.zfp_type.double, args.tolerance)
+    out = torch.empty_like(field)
+    words, offs = gz.compress_mode(field, mode, with_offsets=True, cuda_stream=stream)
+    sbytes = words.numel() * 8
+    for _ in range(max(args.warmup, 3)):
+        words, offs = gz.compress_mode(field, mode, with_offsets=True, cuda_stream=stream)
+        gz.decompress_mode(words, SHAPE, torch.float64, mode, offsets=offs, out=out,
+                           cuda_stream=stream)
+    torch.cuda.synchronize()
+    err = float((out - field).abs().max())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            ev[3 * i].record(stream)
+            words, offs = gz.compress_mode(field, mode, with_offsets=True, cuda_stream=stream)
+            ev[3 * i + 1].record(stream)
+            gz.decompress_mode(words, SHAPE, torch.float64, mode, offsets=offs, out=out,
+                               cuda_stream=stream)
+            ev[3 * i + 2].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    enc_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
+    dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
+    ms_per_step = max_over_ranks(enc_ms + dec_ms, world, dev)
+    # the serial walk, on a small field
+    small = synth.sinusoids_device((64, 64, 64), 16, 32, seed=rank, dtype=torch.float64,
+                                   device=dev)
+    sw = gz.compress_mode(small, mode, cuda_stream=stream)
+    gz.index_blocks(sw, small.shape, torch.float64, mode, cuda_stream=stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    gz.index_blocks(sw, small.shape, torch.float64, mode, cuda_stream=stream)
+    b.record(stream)
+    b.synchronize()
+    walk_us = a.elapsed_time(b) * 1e3 / (16 ** 3)
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    alg = nbytes + sbytes
+    res = {
+        "metric": "zfp fixed-accuracy compress+decompress throughput",
+        "value": round(2 * nbytes * world / (ms_per_step * 1e-3) / 1e9, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"3d_f64_{args.edge}cube_sinusoids16_accuracy{args.tolerance:g}",
+                   "shape": list(SHAPE), "mode": list(mode.as_tuple()), "stream_bytes": sbytes,
+                   "bits_per_value": round(8 * sbytes / field.numel(), 3),
+                   "max_abs_error": err,
+                   "l2": "inputs larger than L2 (1 GiB field)",
+                   "parallelism": f"replicas x{world}"},
+        "compress_gbs": round(nbytes / (enc_ms * 1e-3) / 1e9, 3),
+        "decompress_gbs": round(nbytes / (dec_ms * 1e-3) / 1e9, 3),
+        "calls": {"compress_ms": round(enc_ms, 4), "decompress_ms": round(dec_ms, 4),
+                  "compress_alg_gbs": round(alg / (enc_ms * 1e-3) / 1e9, 2),
+                  "decompress_alg_gbs": round(alg / (dec_ms * 1e-3) / 1e9, 2)},
+        "roofline": {"bound": "hbm", "kernel": "compress+decompress calls",
+                     "achieved": round(2 * alg / (ms_per_step * 1e-3) / 1e9, 2), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": round(2 * alg / (ms_per_step * 1e-3) / 1e9 / peak, 4),
+                     "traffic": None},
+        "block_walk_us_per_block": round(walk_us, 3),
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(res), flush=True)
+
+
 # --------------------------------------------------------------- GPU side
 
 def main():
@@ -529,6 +620,9 @@ def run(args, rank, world, local):
         return
     if args.workload == "serving":
         run_serving(args, rank, world, local)
+        return
+    if args.workload == "accuracy":
+        run_accuracy(args, rank, world, local)
         return
     import numpy as np
     import torch
