@@ -75,6 +75,12 @@ _lib.gzfp_write_header.restype = _I
 _lib.gzfp_write_header.argtypes = [_I, _U, _U, _U, _U, _VP, _SZ, _P(_SZ)]
 _lib.gzfp_read_header.restype = _I
 _lib.gzfp_read_header.argtypes = [_VP, _SZ, _P(_I), _P(_U), _P(_U), _P(_U), _P(_U), _P(_SZ)]
+_lib.gzfp_read_header_mode.restype = _I
+_lib.gzfp_read_header_mode.argtypes = [_VP, _SZ, _P(_I), _P(_U), _P(_U), _P(_U), _VP, _P(_SZ)]
+_lib.gzfp_write_header_mode.restype = _I
+_lib.gzfp_write_header_mode.argtypes = [_I, _U, _U, _U, _VP, _VP, _SZ, _P(_SZ)]
+_lib.gzfp_compress_mode_headed.restype = _I
+_lib.gzfp_compress_mode_headed.argtypes = [_I, _U, _U, _U, _VP, _VP, _VP, _SZ, _P(_SZ), _VP, _VP]
 _lib.gzfp_compress_headed.restype = _I
 _lib.gzfp_compress_headed.argtypes = [_I, _U, _U, _U, ctypes.c_double, _VP, _VP, _SZ, _P(_SZ),
                                       _VP]
@@ -418,6 +424,62 @@ def read_header(buf: Any) -> dict:
             "dtype": _DTYPE_NAME[zt], "maxbits": int(mb.value), "bits": int(bits.value)}
 
 
+def read_header_mode(buf: Any) -> dict:
+    """Parse the header of a stream of any mode: {'type', 'shape', 'dtype',
+    'mode' (a Mode), 'bits'}."""
+    if hasattr(buf, "data_ptr") and getattr(buf, "is_cuda", False):
+        buf = buf[: 3 * 8 // buf.element_size()].cpu().numpy()
+    if isinstance(buf, (bytes, bytearray)):
+        raw = bytes(buf)
+    else:
+        import numpy as np
+        raw = np.ascontiguousarray(buf).view(np.uint8).tobytes()
+    c = ctypes.create_string_buffer(raw, len(raw))
+    t, nx, ny, nz, bits = _I(0), _U(0), _U(0), _U(0), _SZ(0)
+    m = Mode()
+    _check(_lib.gzfp_read_header_mode(c, len(raw), ctypes.byref(t), ctypes.byref(nx),
+                                      ctypes.byref(ny), ctypes.byref(nz), ctypes.byref(m),
+                                      ctypes.byref(bits)), "read_header_mode")
+    zt = zfp_type(t.value)
+    return {"type": zt, "shape": tuple(v for v in (nz.value, ny.value, nx.value) if v),
+            "dtype": _DTYPE_NAME[zt], "mode": m, "bits": int(bits.value)}
+
+
+def write_header_mode(type: zfp_type, nx: int, ny: int, nz: int, mode) -> tuple[bytes, int]:
+    """The header bytes of a stream with these parameters, and its bits."""
+    buf = ctypes.create_string_buffer(24)
+    bits = _SZ(0)
+    _check(_lib.gzfp_write_header_mode(int(type), nx, ny, nz, ctypes.byref(mode), buf, 24,
+                                       ctypes.byref(bits)), "write_header_mode")
+    return buf.raw[: (bits.value + 7) // 8], int(bits.value)
+
+
+def compress_mode_headed(x, mode, with_offsets: bool = False, cuda_stream: Any = None):
+    """compress_mode with zfp's full header in front (offsets count from
+    the stream's first bit)."""
+    t = _type_of(x.dtype)
+    nx, ny, nz = _dims_of(x.shape)
+    cap = mode_maximum_size(t, nx, ny, nz, mode) + 24
+    nb = _nblocks(x.shape)
+    if hasattr(x, "data_ptr"):
+        import torch
+        out = torch.empty(cap // 8, dtype=torch.int64, device=x.device)
+        offs = torch.empty(nb, dtype=torch.int64, device=x.device) if with_offsets else None
+    else:
+        import numpy as np
+        out = np.empty(cap // 8, np.uint64)
+        offs = np.empty(nb, np.uint64) if with_offsets else None
+    got = _SZ(0)
+    _check(_lib.gzfp_compress_mode_headed(int(t), nx, ny, nz, ctypes.byref(mode),
+                                          _addr_and_size(x)[0], _addr_and_size(out)[0],
+                                          out.nbytes if hasattr(out, "nbytes") else cap,
+                                          ctypes.byref(got),
+                                          _addr_and_size(offs)[0] if offs is not None else None,
+                                          _cuda_stream_handle(cuda_stream)), "compress_mode_headed")
+    words = out[: got.value // 8]
+    return (words, offs) if with_offsets else words
+
+
 def headed_size(type: zfp_type, nx: int, ny: int, nz: int, maxbits: int) -> int:
     """Exact bytes of a headed fixed-rate stream."""
     _, hb = write_header(type, nx, ny, nz, maxbits)
@@ -457,8 +519,8 @@ def compress_headed(x, rate: float, out=None, cuda_stream: Any = None):
 def decompress_headed(words, out=None, cuda_stream: Any = None):
     """Decompress a headed stream; type and shape come from its header.  The
     result lands in ``out`` when given, else in a new tensor on the stream's
-    device (numpy array for a host stream)."""
-    h = read_header(words)
+    device (numpy array for a host stream).  Streams of every mode decode."""
+    h = read_header_mode(words)
     if out is None:
         if hasattr(words, "data_ptr"):
             import torch
@@ -887,5 +949,6 @@ __all__ = [
     "GZFP_SERVE_DECOMPRESS", "HEADER_MAX_BITS", "write_header", "read_header", "headed_size",
     "compress_headed", "decompress_headed", "decode_blocks", "encode_blocks", "Mode",
     "mode_rate", "mode_precision", "mode_accuracy", "mode_maximum_size", "compress_mode",
-    "decompress_mode", "index_blocks",
+    "decompress_mode", "index_blocks", "read_header_mode", "write_header_mode",
+    "compress_mode_headed",
 ]

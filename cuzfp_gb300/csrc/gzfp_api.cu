@@ -575,213 +575,6 @@ int gzfp_decompress(int type, unsigned nx, unsigned ny, unsigned nz, double rate
 
 }  // extern "C"
 
-// ------------------------------------------------------------------ headers
-// zfp 0.5.0's full header (zfp_write_header / zfp_read_header with
-// ZFP_HEADER_FULL, Z/src/zfp.c:661-719), for the parameters
-// zfp_stream_set_rate leaves (Z/src/zfp.c:405-430): minbits = maxbits,
-// maxprec = the type's precision, minexp = ZFP_MIN_EXP.
-namespace {
-
-constexpr unsigned kMagicBits = 32, kMetaBits = 52, kModeShortBits = 12, kModeLongBits = 64;
-constexpr uint64_t kModeShortMax = (1u << kModeShortBits) - 2;  // ZFP_MODE_SHORT_MAX
-constexpr int kMinExp = -1074;                                    // ZFP_MIN_EXP
-constexpr int kMinExpBias = 16495;  // minexp offset of the long mode form
-constexpr unsigned kHeaderMaxBits = 1u << 15;  // largest maxbits the long form records
-
-// up to 192 bits, LSB first in 64-bit words (the stream's own layout)
-struct HeaderWords {
-  uint64_t w[3] = {0, 0, 0};
-  unsigned n = 0;
-  void put(uint64_t v, unsigned bits) {  // bits <= 64
-    if (bits < 64) v &= (1ull << bits) - 1;
-    const unsigned i = n >> 6, o = n & 63;
-    w[i] |= v << o;
-    if (o && o + bits > 64) w[i + 1] |= v >> (64 - o);
-    n += bits;
-  }
-  uint64_t get(unsigned& pos, unsigned bits) const {  // bits <= 64
-    const unsigned i = pos >> 6, o = pos & 63;
-    uint64_t v = w[i] >> o;
-    if (o && o + bits > 64) v |= w[i + 1] << (64 - o);
-    pos += bits;
-    return bits < 64 ? v & ((1ull << bits) - 1) : v;
-  }
-};
-
-unsigned type_precision(int type) {
-  return type == GZFP_TYPE_FLOAT || type == GZFP_TYPE_INT32 ? 32 : 64;
-}
-
-// Field sizes a header records: 48 bits of nx - 1 in 1D, 24 bits per axis
-// in 2D, 16 bits per axis in 3D (zfp_field_metadata, Z/src/zfp.c:158-182).
-bool header_sizes_fit(int dims, unsigned nx, unsigned ny, unsigned nz) {
-  if (dims == 2) return nx <= (1u << 24) && ny <= (1u << 24);
-  if (dims == 3) return nx <= (1u << 16) && ny <= (1u << 16) && nz <= (1u << 16);
-  return true;
-}
-
-int build_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
-                 HeaderWords& h) {
-  gzfp::Geom g;
-  int dims;
-  int st = check_common(type, nx, ny, nz, maxbits, g, dims);
-  if (st) return st;
-  if (!header_sizes_fit(dims, nx, ny, nz))
-    return fail(GZFP_ERR_ARG, "field sizes beyond what a zfp header records");
-  if (maxbits > kHeaderMaxBits) return fail(GZFP_ERR_ARG, "bits per block beyond what a zfp header records");
-  h.put('z', 8);
-  h.put('f', 8);
-  h.put('p', 8);
-  h.put(5, 8);  // ZFP_VERSION >> 4 for 0.5.0
-  uint64_t meta = dims == 1   ? (uint64_t)(nx - 1)
-                  : dims == 2 ? ((uint64_t)(ny - 1) << 24) | (nx - 1)
-                              : ((((uint64_t)(nz - 1) << 16) | (ny - 1)) << 16) | (nx - 1);
-  meta = (meta << 4) | ((uint64_t)(dims - 1) << 2) | (uint64_t)(type - 1);
-  h.put(meta, kMetaBits);
-  const unsigned prec = type_precision(type);
-  if (prec >= 64 && maxbits <= 2048) {
-    h.put(maxbits - 1, kModeShortBits);  // the 12-bit fixed-rate form
-  } else {
-    // each parameter on its own: minexp, maxprec - 1, maxbits - 1, minbits - 1, 0xfff
-    uint64_t mode = (uint64_t)(kMinExp + kMinExpBias);
-    mode = (mode << 7) | (prec - 1);
-    mode = (mode << 15) | (maxbits - 1);
-    mode = (mode << 15) | (maxbits - 1);
-    mode = (mode << 12) | 0xfff;
-    h.put(mode, kModeLongBits);
-  }
-  return GZFP_OK;
-}
-
-int parse_header(const HeaderWords& h, size_t avail_bits, int* type, unsigned* nx, unsigned* ny,
-                 unsigned* nz, unsigned* maxbits, size_t* header_bits) {
-  if (avail_bits < kMagicBits + kMetaBits + kModeShortBits)
-    return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
-  unsigned pos = 0;
-  if (h.get(pos, 8) != 'z' || h.get(pos, 8) != 'f' || h.get(pos, 8) != 'p' || h.get(pos, 8) != 5)
-    return fail(GZFP_ERR_ARG, "no zfp 0.5.0 header (magic mismatch)");
-  uint64_t meta = h.get(pos, kMetaBits);
-  const int t = (int)(meta & 3) + 1;
-  const int dims = (int)((meta >> 2) & 3) + 1;
-  meta >>= 4;
-  unsigned x, y = 0, z = 0;
-  if (dims == 1) {
-    const uint64_t n = (meta & 0xffffffffffffull) + 1;
-    if (n > 0xffffffffull) return fail(GZFP_ERR_UNSUPPORTED, "1D field of 2^32 values or more");
-    x = (unsigned)n;
-  } else if (dims == 2) {
-    x = (unsigned)(meta & 0xffffff) + 1;
-    y = (unsigned)((meta >> 24) & 0xffffff) + 1;
-  } else if (dims == 3) {
-    x = (unsigned)(meta & 0xffff) + 1;
-    y = (unsigned)((meta >> 16) & 0xffff) + 1;
-    z = (unsigned)((meta >> 32) & 0xffff) + 1;
-  } else {
-    return fail(GZFP_ERR_UNSUPPORTED, "4D field (not part of zfp 0.5.0)");
-  }
-  uint64_t mode = h.get(pos, kModeShortBits);
-  unsigned mb;
-  if (mode <= kModeShortMax) {
-    if (mode >= 2048)
-      return fail(GZFP_ERR_UNSUPPORTED, "fixed-precision or fixed-accuracy stream (fixed rate only)");
-    mb = (unsigned)mode + 1;
-  } else {
-    if (avail_bits < kMagicBits + kMetaBits + kModeLongBits)
-      return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
-    mode |= h.get(pos, kModeLongBits - kModeShortBits) << kModeShortBits;
-    const unsigned minbits = (unsigned)((mode >> 12) & 0x7fff) + 1;
-    mb = (unsigned)((mode >> 27) & 0x7fff) + 1;
-    const unsigned maxprec = (unsigned)((mode >> 42) & 0x7f) + 1;
-    const int minexp = (int)((mode >> 49) & 0x7fff) - kMinExpBias;
-    // zfp_stream_set_rate's parameters; anything else codes blocks differently
-    if (minbits != mb || maxprec < type_precision(t) || minexp != kMinExp)
-      return fail(GZFP_ERR_UNSUPPORTED, "stream in a mode other than fixed rate");
-  }
-  if (mb < (unsigned)ebits_of(t) + 1)
-    return fail(GZFP_ERR_UNSUPPORTED, "fewer bits per block than the block header");
-  *type = t;
-  *nx = x;
-  *ny = y;
-  *nz = z;
-  *maxbits = mb;
-  *header_bits = pos;
-  return GZFP_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int gzfp_write_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
-                      void* header, size_t capacity, size_t* header_bits) {
-  clear_error();
-  HeaderWords h;
-  int st = build_header(type, nx, ny, nz, maxbits, h);
-  if (st) return st;
-  if (!header) return fail(GZFP_ERR_ARG, "null pointer");
-  const size_t bytes = (h.n + 7) / 8;
-  if (capacity < bytes) return fail(GZFP_ERR_CAPACITY, "header buffer too small");
-  memcpy(header, h.w, bytes);
-  if (header_bits) *header_bits = h.n;
-  return GZFP_OK;
-}
-
-int gzfp_read_header(const void* header, size_t bytes, int* type, unsigned* nx, unsigned* ny,
-                     unsigned* nz, unsigned* maxbits, size_t* header_bits) {
-  clear_error();
-  if (!header || !type || !nx || !ny || !nz || !maxbits || !header_bits)
-    return fail(GZFP_ERR_ARG, "null pointer");
-  HeaderWords h;
-  memcpy(h.w, header, bytes < sizeof h.w ? bytes : sizeof h.w);
-  return parse_header(h, bytes * 8, type, nx, ny, nz, maxbits, header_bits);
-}
-
-int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
-                         const void* data, void* stream, size_t capacity, size_t* out_bytes,
-                         void* cuda_stream) {
-  clear_error();
-  gzfp::Geom g;
-  int dims;
-  if (!make_geom(nx, ny, nz, g, dims)) return fail(GZFP_ERR_ARG, "bad dimensions");
-  const unsigned maxbits = gzfp_rate_to_maxbits(type, (unsigned)dims, rate);
-  if (!maxbits) return fail(GZFP_ERR_ARG, "bad type or rate");
-  HeaderWords h;
-  int st = build_header(type, nx, ny, nz, maxbits, h);
-  if (st) return st;
-  return strided_call(false, type, nx, ny, nz, 0, 0, 0, maxbits, (void*)data, (uint64_t*)stream,
-                      capacity, out_bytes, cuda_stream, h.n, h.w, (h.n + 63) / 64);
-}
-
-int gzfp_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes,
-                           void* cuda_stream) {
-  clear_error();
-  if (!stream || !data) return fail(GZFP_ERR_ARG, "null pointer");
-  HeaderWords h;
-  const size_t hb = bytes < sizeof h.w ? bytes : sizeof h.w;
-  cudaError_t e;
-  if (is_device_pointer(stream)) {
-    // the header is parsed on the host: wait for work queued before this call
-    cudaStream_t s = (cudaStream_t)cuda_stream;
-    if ((e = cudaMemcpyAsync(h.w, stream, hb, cudaMemcpyDeviceToHost, s)) ||
-        (e = cudaStreamSynchronize(s)))
-      return cuda_fail(e, "cudaMemcpyAsync(header D2H)");
-  } else {
-    memcpy(h.w, stream, hb);
-  }
-  int type;
-  unsigned nx, ny, nz, maxbits;
-  size_t header_bits;
-  int st = parse_header(h, bytes * 8, &type, &nx, &ny, &nz, &maxbits, &header_bits);
-  if (st) return st;
-  const uint64_t values = (uint64_t)nx * (ny ? ny : 1) * (nz ? nz : 1);
-  if (data_bytes < values * scalar_size(type))
-    return fail(GZFP_ERR_CAPACITY, "output buffer smaller than the field in the header");
-  return strided_call(true, type, nx, ny, nz, 0, 0, 0, maxbits, data, (uint64_t*)stream, bytes,
-                      nullptr, cuda_stream, header_bits);
-}
-
-}  // extern "C"
-
 // ------------------------------------------------------------ block access
 namespace {
 
@@ -998,29 +791,30 @@ cudaError_t decode_mode_launch(int type, int dims, const uint64_t* in, uint64_t 
 }
 
 cudaError_t index_launch(int type, int dims, const uint64_t* in, uint64_t nwords, uint64_t nblocks,
-                         const gzfp::General& mode, unsigned long long* offsets,
+                         const gzfp::General& mode, uint64_t first, unsigned long long* offsets,
                          unsigned long long* end, cudaStream_t s) {
   switch (type) {
     case GZFP_TYPE_FLOAT:
-      return gzfp::launch_index_blocks<float>(dims, in, nwords, nblocks, mode, offsets, end, s);
+      return gzfp::launch_index_blocks<float>(dims, in, nwords, nblocks, mode, first, offsets, end, s);
     case GZFP_TYPE_DOUBLE:
-      return gzfp::launch_index_blocks<double>(dims, in, nwords, nblocks, mode, offsets, end, s);
+      return gzfp::launch_index_blocks<double>(dims, in, nwords, nblocks, mode, first, offsets, end, s);
     case GZFP_TYPE_INT32:
-      return gzfp::launch_index_blocks<int32_t>(dims, in, nwords, nblocks, mode, offsets, end, s);
+      return gzfp::launch_index_blocks<int32_t>(dims, in, nwords, nblocks, mode, first, offsets, end, s);
     default:
-      return gzfp::launch_index_blocks<int64_t>(dims, in, nwords, nblocks, mode, offsets, end, s);
+      return gzfp::launch_index_blocks<int64_t>(dims, in, nwords, nblocks, mode, first, offsets, end, s);
   }
 }
 
 // Walk the blocks of a device stream into ms.offsets; *end_bit = the bit
 // after the last block.  Synchronises `s`.
 int walk_blocks(ModeSpace& ms, int type, int dims, const uint64_t* words, uint64_t nwords,
-                const gzfp::Geom& g, const gzfp::General& mode, uint64_t& end_bit, cudaStream_t s) {
+                const gzfp::Geom& g, const gzfp::General& mode, uint64_t first, uint64_t& end_bit,
+                cudaStream_t s) {
   cudaError_t e;
   if ((e = reserve(ms.offsets, ms.offsets_cap, (size_t)g.nblocks * 8)) ||
       (e = reserve(ms.sums, ms.sums_cap, 64)))
     return cuda_fail(e, "cudaMalloc(block offsets)");
-  if ((e = index_launch(type, dims, words, nwords, g.nblocks, mode,
+  if ((e = index_launch(type, dims, words, nwords, g.nblocks, mode, first,
                         (unsigned long long*)ms.offsets, (unsigned long long*)ms.sums, s)))
     return cuda_fail(e, "block walk launch");
   unsigned long long end = 0;
@@ -1075,10 +869,16 @@ size_t gzfp_mode_maximum_size(int type, unsigned nx, unsigned ny, unsigned nz,
   return (size_t)((g.nblocks * mode_block_bound(type, dims, mode) + 63) / 64 * 8);
 }
 
-int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+}  // extern "C"
+
+namespace {
+
+// A general-mode compression; with `header` (hbits bits in whole words)
+// the stream starts with it and the blocks follow directly.
+int compress_mode_impl(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
                        const void* data, void* stream, size_t capacity, size_t* out_bytes,
-                       unsigned long long* offsets, void* cuda_stream) {
-  clear_error();
+                       unsigned long long* offsets, void* cuda_stream, const uint64_t* header,
+                       unsigned hbits) {
   gzfp::Geom g;
   int dims;
   int st = check_mode(type, nx, ny, nz, mode, g, dims);
@@ -1087,14 +887,17 @@ int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gz
   cudaStream_t s = (cudaStream_t)cuda_stream;
   cudaError_t e;
   if (fixed_rate_mode(type, mode)) {
-    st = gzfp_compress_bits(type, nx, ny, nz, mode->maxbits, data, stream, capacity, out_bytes,
-                            cuda_stream);
+    st = header ? strided_call(false, type, nx, ny, nz, 0, 0, 0, mode->maxbits, (void*)data,
+                               (uint64_t*)stream, capacity, out_bytes, cuda_stream, hbits, header,
+                               (hbits + 63) / 64)
+                : gzfp_compress_bits(type, nx, ny, nz, mode->maxbits, data, stream, capacity,
+                                     out_bytes, cuda_stream);
     if (st || !offsets) return st;
     if (is_device_pointer(offsets)) {
-      if ((e = gzfp::launch_fixed_offsets(offsets, g.nblocks, mode->maxbits, s)))
+      if ((e = gzfp::launch_fixed_offsets(offsets, g.nblocks, hbits, mode->maxbits, s)))
         return cuda_fail(e, "offsets kernel launch");
     } else {
-      for (uint64_t b = 0; b < g.nblocks; b++) offsets[b] = b * mode->maxbits;
+      for (uint64_t b = 0; b < g.nblocks; b++) offsets[b] = hbits + b * mode->maxbits;
     }
     return GZFP_OK;
   }
@@ -1131,14 +934,14 @@ int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gz
   if ((e = encode_mode_launch(type, dims, din, gv, gm, (uint64_t*)ms.scratch, slot_words,
                               (uint32_t*)ms.lengths, s)))
     return cuda_fail(e, "encode kernel launch");
-  if ((e = gzfp::launch_scan_lengths((const uint32_t*)ms.lengths, g.nblocks, (uint64_t*)ms.sums,
-                                     (unsigned long long*)ms.offsets, s)))
+  if ((e = gzfp::launch_scan_lengths((const uint32_t*)ms.lengths, g.nblocks, hbits,
+                                     (uint64_t*)ms.sums, (unsigned long long*)ms.offsets, s)))
     return cuda_fail(e, "scan kernel launch");
   unsigned long long total = 0;
   if ((e = cudaMemcpyAsync(&total, (uint64_t*)ms.sums + m, 8, cudaMemcpyDeviceToHost, s)) ||
       (e = cudaStreamSynchronize(s)))
     return cuda_fail(e, "encode");
-  const size_t bytes = (size_t)((total + 63) / 64 * 8);
+  const size_t bytes = (size_t)((hbits + total + 63) / 64 * 8);
   if (out_bytes) *out_bytes = bytes;
   if (capacity < bytes) return fail(GZFP_ERR_CAPACITY, "stream buffer smaller than the compressed size");
   uint64_t* dstream = (uint64_t*)stream;
@@ -1148,6 +951,8 @@ int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gz
   }
   st = GZFP_OK;
   if ((e = cudaMemsetAsync(dstream, 0, bytes, s)) ||
+      (header && (e = cudaMemcpyAsync(dstream, header, (hbits + 63) / 64 * 8,
+                                      cudaMemcpyHostToDevice, s))) ||
       (e = gzfp::launch_place_blocks((const uint64_t*)ms.scratch, slot_words,
                                      (const uint32_t*)ms.lengths,
                                      (const unsigned long long*)ms.offsets, g.nblocks, dstream, s)))
@@ -1161,6 +966,91 @@ int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gz
   const cudaError_t es = cudaStreamSynchronize(s);  // the scratch is reused by the next call
   if (!st && es) st = cuda_fail(es, "cudaStreamSynchronize");
   return st;
+}
+
+// A general-mode decompression whose first block starts at bit `first`.
+int decompress_mode_impl(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                         const void* stream, size_t bytes, const unsigned long long* offsets,
+                         void* data, void* cuda_stream, uint64_t first) {
+  gzfp::Geom g;
+  int dims;
+  int st = check_mode(type, nx, ny, nz, mode, g, dims);
+  if (st) return st;
+  if (!stream || !data) return fail(GZFP_ERR_ARG, "null pointer");
+  if (fixed_rate_mode(type, mode))
+    return first ? strided_call(true, type, nx, ny, nz, 0, 0, 0, mode->maxbits, data,
+                                (uint64_t*)stream, bytes, nullptr, cuda_stream, first)
+                 : gzfp_decompress_bits(type, nx, ny, nz, mode->maxbits, stream, bytes, data,
+                                        cuda_stream);
+  if (g.nblocks == 0) return GZFP_OK;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  ModeSpace* msp;
+  if ((st = mode_space(msp))) return st;
+  ModeSpace& ms = *msp;
+  std::lock_guard<std::mutex> lock(ms.mu);
+  cudaError_t e;
+  const uint64_t nwords = bytes / 8;
+  const gzfp::General gm = general_of(mode);
+  const size_t field_bytes = (size_t)g.nx * g.ny * g.nz * scalar_size(type);
+  const bool dev_stream = is_device_pointer(stream), dev_data = is_device_pointer(data);
+  bool staged = !dev_stream || !dev_data;
+  const uint64_t* dw = (const uint64_t*)stream;
+  if (!dev_stream) {
+    if ((e = reserve(ms.stream, ms.stream_cap, nwords ? nwords * 8 : 8)) ||
+        (e = cudaMemcpyAsync(ms.stream, stream, nwords * 8, cudaMemcpyHostToDevice, s)))
+      return cuda_fail(e, "stream staging");
+    dw = (const uint64_t*)ms.stream;
+  }
+  const unsigned long long* doff = offsets;
+  if (!offsets) {
+    uint64_t end = 0;
+    if ((st = walk_blocks(ms, type, dims, dw, nwords, g, gm, first, end, s))) return st;
+    if (end > nwords * 64) return fail(GZFP_ERR_ARG, "stream shorter than its blocks");
+    doff = (const unsigned long long*)ms.offsets;
+  } else if (!is_device_pointer(offsets)) {
+    if ((e = reserve(ms.offsets, ms.offsets_cap, (size_t)g.nblocks * 8)) ||
+        (e = cudaMemcpyAsync(ms.offsets, offsets, (size_t)g.nblocks * 8, cudaMemcpyHostToDevice, s)))
+      return cuda_fail(e, "offsets staging");
+    doff = (const unsigned long long*)ms.offsets;
+    staged = true;
+  }
+  void* dout = data;
+  if (!dev_data) {
+    if ((e = reserve(ms.field, ms.field_cap, field_bytes))) return cuda_fail(e, "cudaMalloc(field staging)");
+    dout = ms.field;
+  }
+  gzfp::Geom gv = g;
+  gv.vec = rows_vectorizable(dout, nx, type);
+  st = GZFP_OK;
+  if ((e = decode_mode_launch(type, dims, dw, nwords, doff, gv, gm, dout, s)))
+    st = cuda_fail(e, "decode kernel launch");
+  if (!st && !dev_data && (e = cudaMemcpyAsync(data, dout, field_bytes, cudaMemcpyDeviceToHost, s)))
+    st = cuda_fail(e, "cudaMemcpyAsync(field D2H)");
+  if (staged || !offsets) {  // staging buffers and the walk's offsets are reused by the next call
+    const cudaError_t es = cudaStreamSynchronize(s);
+    if (!st && es) st = cuda_fail(es, "cudaStreamSynchronize");
+  }
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gzfp_compress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                       const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                       unsigned long long* offsets, void* cuda_stream) {
+  clear_error();
+  return compress_mode_impl(type, nx, ny, nz, mode, data, stream, capacity, out_bytes, offsets,
+                            cuda_stream, nullptr, 0);
+}
+
+int gzfp_decompress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
+                         const void* stream, size_t bytes, const unsigned long long* offsets,
+                         void* data, void* cuda_stream) {
+  clear_error();
+  return decompress_mode_impl(type, nx, ny, nz, mode, stream, bytes, offsets, data, cuda_stream,
+                              0);
 }
 
 int gzfp_index_blocks(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
@@ -1188,7 +1078,7 @@ int gzfp_index_blocks(int type, unsigned nx, unsigned ny, unsigned nz, const gzf
     dw = (const uint64_t*)ms.stream;
   }
   uint64_t end = 0;
-  if ((st = walk_blocks(ms, type, dims, dw, nwords, g, general_of(mode), end, s))) return st;
+  if ((st = walk_blocks(ms, type, dims, dw, nwords, g, general_of(mode), 0, end, s))) return st;
   if (end > nwords * 64) return fail(GZFP_ERR_ARG, "stream shorter than its blocks");
   if ((e = cudaMemcpyAsync(offsets, ms.offsets, (size_t)g.nblocks * 8,
                            is_device_pointer(offsets) ? cudaMemcpyDeviceToDevice
@@ -1198,66 +1088,270 @@ int gzfp_index_blocks(int type, unsigned nx, unsigned ny, unsigned nz, const gzf
   return GZFP_OK;
 }
 
-int gzfp_decompress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
-                         const void* stream, size_t bytes, const unsigned long long* offsets,
-                         void* data, void* cuda_stream) {
+}  // extern "C"
+
+// ------------------------------------------------------------------ headers
+// zfp 0.5.0's full header (zfp_write_header / zfp_read_header with
+// ZFP_HEADER_FULL, Z/src/zfp.c:661-719): a 32-bit magic, 52 bits of field
+// metadata (zfp_field_metadata / zfp_field_set_metadata, :158-182 and
+// :254-275) and the stream parameters in 12 or 64 bits (zfp_stream_mode /
+// zfp_stream_set_mode, :305-345 and :461-498).
+namespace {
+
+constexpr unsigned kMagicBits = 32, kMetaBits = 52, kModeShortBits = 12, kModeLongBits = 64;
+constexpr uint64_t kModeShortMax = (1u << kModeShortBits) - 2;  // ZFP_MODE_SHORT_MAX
+constexpr int kMinExp = -1074;                                    // ZFP_MIN_EXP
+constexpr unsigned kMaxBitsZfp = 4171;                            // ZFP_MAX_BITS
+constexpr int kMinExpBias = 16495;  // minexp offset of the long mode form
+constexpr unsigned kLongField = 0x8000;  // largest minbits / maxbits the long form records
+
+// up to 192 bits, LSB first in 64-bit words (the stream's own layout)
+struct HeaderWords {
+  uint64_t w[3] = {0, 0, 0};
+  unsigned n = 0;
+  void put(uint64_t v, unsigned bits) {  // bits <= 64
+    if (bits < 64) v &= (1ull << bits) - 1;
+    const unsigned i = n >> 6, o = n & 63;
+    w[i] |= v << o;
+    if (o && o + bits > 64) w[i + 1] |= v >> (64 - o);
+    n += bits;
+  }
+  uint64_t get(unsigned& pos, unsigned bits) const {  // bits <= 64
+    const unsigned i = pos >> 6, o = pos & 63;
+    uint64_t v = w[i] >> o;
+    if (o && o + bits > 64) v |= w[i + 1] << (64 - o);
+    pos += bits;
+    return bits < 64 ? v & ((1ull << bits) - 1) : v;
+  }
+};
+
+// Field sizes a header records: 48 bits of nx - 1 in 1D, 24 bits per axis
+// in 2D, 16 bits per axis in 3D (zfp_field_metadata, Z/src/zfp.c:158-182).
+bool header_sizes_fit(int dims, unsigned nx, unsigned ny, unsigned nz) {
+  if (dims == 2) return nx <= (1u << 24) && ny <= (1u << 24);
+  if (dims == 3) return nx <= (1u << 16) && ny <= (1u << 16) && nz <= (1u << 16);
+  return true;
+}
+
+// zfp_stream_mode: the 12-bit forms for fixed rate (maxbits - 1), fixed
+// precision (maxprec + 2047) and fixed accuracy (minexp + 3251), else the
+// 64-bit form holding every parameter.
+uint64_t mode_code(const gzfp_mode& m, unsigned& bits) {
+  bits = kModeShortBits;
+  if (m.minbits == m.maxbits && m.maxbits >= 1 && m.maxbits <= 2048 && m.maxprec >= 64 &&
+      m.minexp <= kMinExp)
+    return m.maxbits - 1;
+  if (m.minbits == 0 && m.maxbits >= kMaxBitsZfp && m.maxprec >= 1 && m.maxprec <= 128 &&
+      m.minexp <= kMinExp)
+    return m.maxprec + 2047;
+  if (m.minbits == 0 && m.maxbits >= kMaxBitsZfp && m.maxprec >= 64 && m.minexp >= kMinExp &&
+      m.minexp <= 843)
+    return (uint64_t)(m.minexp + 3251);
+  bits = kModeLongBits;
+  auto clamp1 = [](unsigned v, unsigned hi) { return (v < 1 ? 1 : v > hi ? hi : v) - 1; };
+  const int e = m.minexp + kMinExpBias;
+  uint64_t code = (uint64_t)(e < 0 ? 0 : e > 0x7fff ? 0x7fff : e);
+  code = (code << 7) | clamp1(m.maxprec, 0x80);
+  code = (code << 15) | clamp1(m.maxbits, kLongField);
+  code = (code << 15) | clamp1(m.minbits, kLongField);
+  return (code << 12) | 0xfff;
+}
+
+int build_header_mode(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode& m,
+                      HeaderWords& h) {
+  gzfp::Geom g;
+  int dims;
+  int st = check_mode(type, nx, ny, nz, &m, g, dims);
+  if (st) return st;
+  if (!header_sizes_fit(dims, nx, ny, nz))
+    return fail(GZFP_ERR_ARG, "field sizes beyond what a zfp header records");
+  unsigned mbits;
+  const uint64_t code = mode_code(m, mbits);
+  // the long form clamps: refuse parameters it would record differently
+  if (mbits == kModeLongBits &&
+      (m.minbits > kLongField || m.maxbits > kLongField || m.minexp + kMinExpBias < 0 ||
+       m.minexp + kMinExpBias > 0x7fff))
+    return fail(GZFP_ERR_ARG, "parameters beyond what a zfp header records");
+  h.put('z', 8);
+  h.put('f', 8);
+  h.put('p', 8);
+  h.put(5, 8);  // ZFP_VERSION >> 4 for 0.5.0
+  uint64_t meta = dims == 1   ? (uint64_t)(nx - 1)
+                  : dims == 2 ? ((uint64_t)(ny - 1) << 24) | (nx - 1)
+                              : ((((uint64_t)(nz - 1) << 16) | (ny - 1)) << 16) | (nx - 1);
+  meta = (meta << 4) | ((uint64_t)(dims - 1) << 2) | (uint64_t)(type - 1);
+  h.put(meta, kMetaBits);
+  h.put(code, mbits);
+  return GZFP_OK;
+}
+
+// Parse a header into the field and the stream parameters
+// (zfp_stream_set_mode); checks that the parameters can code a stream.
+int parse_header_mode(const HeaderWords& h, size_t avail_bits, int* type, unsigned* nx,
+                      unsigned* ny, unsigned* nz, gzfp_mode* m, size_t* header_bits) {
+  if (avail_bits < kMagicBits + kMetaBits + kModeShortBits)
+    return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
+  unsigned pos = 0;
+  if (h.get(pos, 8) != 'z' || h.get(pos, 8) != 'f' || h.get(pos, 8) != 'p' || h.get(pos, 8) != 5)
+    return fail(GZFP_ERR_ARG, "no zfp 0.5.0 header (magic mismatch)");
+  uint64_t meta = h.get(pos, kMetaBits);
+  const int t = (int)(meta & 3) + 1;
+  const int dims = (int)((meta >> 2) & 3) + 1;
+  meta >>= 4;
+  unsigned x, y = 0, z = 0;
+  if (dims == 1) {
+    const uint64_t n = (meta & 0xffffffffffffull) + 1;
+    if (n > 0xffffffffull) return fail(GZFP_ERR_UNSUPPORTED, "1D field of 2^32 values or more");
+    x = (unsigned)n;
+  } else if (dims == 2) {
+    x = (unsigned)(meta & 0xffffff) + 1;
+    y = (unsigned)((meta >> 24) & 0xffffff) + 1;
+  } else if (dims == 3) {
+    x = (unsigned)(meta & 0xffff) + 1;
+    y = (unsigned)((meta >> 16) & 0xffff) + 1;
+    z = (unsigned)((meta >> 32) & 0xffff) + 1;
+  } else {
+    return fail(GZFP_ERR_UNSUPPORTED, "4D field (not part of zfp 0.5.0)");
+  }
+  uint64_t code = h.get(pos, kModeShortBits);
+  gzfp_mode md;
+  if (code <= kModeShortMax) {
+    if (code < 2048)
+      md = gzfp_mode{(unsigned)code + 1, (unsigned)code + 1, 64, kMinExp};
+    else if (code < 2176)
+      md = gzfp_mode{0, kMaxBitsZfp, (unsigned)code - 2047, kMinExp};
+    else
+      md = gzfp_mode{0, kMaxBitsZfp, 64, (int)code - 3251};
+  } else {
+    if (avail_bits < kMagicBits + kMetaBits + kModeLongBits)
+      return fail(GZFP_ERR_ARG, "stream shorter than a zfp header");
+    code |= h.get(pos, kModeLongBits - kModeShortBits) << kModeShortBits;
+    md.minbits = (unsigned)((code >> 12) & 0x7fff) + 1;
+    md.maxbits = (unsigned)((code >> 27) & 0x7fff) + 1;
+    md.maxprec = (unsigned)((code >> 42) & 0x7f) + 1;
+    md.minexp = (int)((code >> 49) & 0x7fff) - kMinExpBias;
+  }
+  gzfp::Geom g;
+  int d;
+  if (check_mode(t, x, y, z, &md, g, d))
+    return fail(GZFP_ERR_UNSUPPORTED, "header parameters this codec cannot decode");
+  *type = t;
+  *nx = x;
+  *ny = y;
+  *nz = z;
+  *m = md;
+  *header_bits = pos;
+  return GZFP_OK;
+}
+
+// the header at the start of a host or device stream (for a device stream:
+// a copy of its first words after the work queued on `s`)
+int stream_header(const void* stream, size_t bytes, cudaStream_t s, HeaderWords& h) {
+  const size_t hb = bytes < sizeof h.w ? bytes : sizeof h.w;
+  if (is_device_pointer(stream)) {
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h.w, stream, hb, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return cuda_fail(e, "cudaMemcpyAsync(header D2H)");
+  } else {
+    memcpy(h.w, stream, hb);
+  }
+  return GZFP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gzfp_write_header_mode(int type, unsigned nx, unsigned ny, unsigned nz,
+                           const gzfp_mode* mode, void* header, size_t capacity,
+                           size_t* header_bits) {
+  clear_error();
+  if (!mode || !header) return fail(GZFP_ERR_ARG, "null pointer");
+  HeaderWords h;
+  int st = build_header_mode(type, nx, ny, nz, *mode, h);
+  if (st) return st;
+  const size_t bytes = (h.n + 7) / 8;
+  if (capacity < bytes) return fail(GZFP_ERR_CAPACITY, "header buffer too small");
+  memcpy(header, h.w, bytes);
+  if (header_bits) *header_bits = h.n;
+  return GZFP_OK;
+}
+
+int gzfp_write_header(int type, unsigned nx, unsigned ny, unsigned nz, unsigned maxbits,
+                      void* header, size_t capacity, size_t* header_bits) {
+  clear_error();
+  // the parameters zfp_stream_set_rate leaves
+  const gzfp_mode m{maxbits, maxbits, precision_bits(type), kMinExp};
+  return gzfp_write_header_mode(type, nx, ny, nz, &m, header, capacity, header_bits);
+}
+
+int gzfp_read_header_mode(const void* header, size_t bytes, int* type, unsigned* nx,
+                          unsigned* ny, unsigned* nz, gzfp_mode* mode, size_t* header_bits) {
+  clear_error();
+  if (!header || !type || !nx || !ny || !nz || !mode || !header_bits)
+    return fail(GZFP_ERR_ARG, "null pointer");
+  HeaderWords h;
+  memcpy(h.w, header, bytes < sizeof h.w ? bytes : sizeof h.w);
+  return parse_header_mode(h, bytes * 8, type, nx, ny, nz, mode, header_bits);
+}
+
+int gzfp_read_header(const void* header, size_t bytes, int* type, unsigned* nx, unsigned* ny,
+                     unsigned* nz, unsigned* maxbits, size_t* header_bits) {
+  gzfp_mode m;
+  int st = gzfp_read_header_mode(header, bytes, type, nx, ny, nz, &m, header_bits);
+  if (st) return st;
+  if (!maxbits) return fail(GZFP_ERR_ARG, "null pointer");
+  if (!fixed_rate_mode(*type, &m))
+    return fail(GZFP_ERR_UNSUPPORTED, "stream in a mode other than fixed rate (see gzfp_read_header_mode)");
+  *maxbits = m.maxbits;
+  return GZFP_OK;
+}
+
+int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
+                         const void* data, void* stream, size_t capacity, size_t* out_bytes,
+                         void* cuda_stream) {
   clear_error();
   gzfp::Geom g;
   int dims;
-  int st = check_mode(type, nx, ny, nz, mode, g, dims);
+  if (!make_geom(nx, ny, nz, g, dims)) return fail(GZFP_ERR_ARG, "bad dimensions");
+  gzfp_mode m;
+  int st = gzfp_mode_rate(type, (unsigned)dims, rate, &m);
   if (st) return st;
+  return gzfp_compress_mode_headed(type, nx, ny, nz, &m, data, stream, capacity, out_bytes,
+                                   nullptr, cuda_stream);
+}
+
+int gzfp_compress_mode_headed(int type, unsigned nx, unsigned ny, unsigned nz,
+                              const gzfp_mode* mode, const void* data, void* stream,
+                              size_t capacity, size_t* out_bytes, unsigned long long* offsets,
+                              void* cuda_stream) {
+  clear_error();
+  if (!mode) return fail(GZFP_ERR_ARG, "null mode");
+  HeaderWords h;
+  int st = build_header_mode(type, nx, ny, nz, *mode, h);
+  if (st) return st;
+  return compress_mode_impl(type, nx, ny, nz, mode, data, stream, capacity, out_bytes, offsets,
+                            cuda_stream, h.w, h.n);
+}
+
+int gzfp_decompress_headed(const void* stream, size_t bytes, void* data, size_t data_bytes,
+                           void* cuda_stream) {
+  clear_error();
   if (!stream || !data) return fail(GZFP_ERR_ARG, "null pointer");
-  if (fixed_rate_mode(type, mode))
-    return gzfp_decompress_bits(type, nx, ny, nz, mode->maxbits, stream, bytes, data, cuda_stream);
-  if (g.nblocks == 0) return GZFP_OK;
-  cudaStream_t s = (cudaStream_t)cuda_stream;
-  ModeSpace* msp;
-  if ((st = mode_space(msp))) return st;
-  ModeSpace& ms = *msp;
-  std::lock_guard<std::mutex> lock(ms.mu);
-  cudaError_t e;
-  const uint64_t nwords = bytes / 8;
-  const gzfp::General gm = general_of(mode);
-  const size_t field_bytes = (size_t)g.nx * g.ny * g.nz * scalar_size(type);
-  const bool dev_stream = is_device_pointer(stream), dev_data = is_device_pointer(data);
-  bool staged = !dev_stream || !dev_data;
-  const uint64_t* dw = (const uint64_t*)stream;
-  if (!dev_stream) {
-    if ((e = reserve(ms.stream, ms.stream_cap, nwords ? nwords * 8 : 8)) ||
-        (e = cudaMemcpyAsync(ms.stream, stream, nwords * 8, cudaMemcpyHostToDevice, s)))
-      return cuda_fail(e, "stream staging");
-    dw = (const uint64_t*)ms.stream;
-  }
-  const unsigned long long* doff = offsets;
-  if (!offsets) {
-    uint64_t end = 0;
-    if ((st = walk_blocks(ms, type, dims, dw, nwords, g, gm, end, s))) return st;
-    if (end > nwords * 64) return fail(GZFP_ERR_ARG, "stream shorter than its blocks");
-    doff = (const unsigned long long*)ms.offsets;
-  } else if (!is_device_pointer(offsets)) {
-    if ((e = reserve(ms.offsets, ms.offsets_cap, (size_t)g.nblocks * 8)) ||
-        (e = cudaMemcpyAsync(ms.offsets, offsets, (size_t)g.nblocks * 8, cudaMemcpyHostToDevice, s)))
-      return cuda_fail(e, "offsets staging");
-    doff = (const unsigned long long*)ms.offsets;
-    staged = true;
-  }
-  void* dout = data;
-  if (!dev_data) {
-    if ((e = reserve(ms.field, ms.field_cap, field_bytes))) return cuda_fail(e, "cudaMalloc(field staging)");
-    dout = ms.field;
-  }
-  gzfp::Geom gv = g;
-  gv.vec = rows_vectorizable(dout, nx, type);
-  st = GZFP_OK;
-  if ((e = decode_mode_launch(type, dims, dw, nwords, doff, gv, gm, dout, s)))
-    st = cuda_fail(e, "decode kernel launch");
-  if (!st && !dev_data && (e = cudaMemcpyAsync(data, dout, field_bytes, cudaMemcpyDeviceToHost, s)))
-    st = cuda_fail(e, "cudaMemcpyAsync(field D2H)");
-  if (staged || !offsets) {  // staging buffers and the walk's offsets are reused by the next call
-    const cudaError_t es = cudaStreamSynchronize(s);
-    if (!st && es) st = cuda_fail(es, "cudaStreamSynchronize");
-  }
-  return st;
+  HeaderWords h;
+  int st = stream_header(stream, bytes, (cudaStream_t)cuda_stream, h);
+  if (st) return st;
+  int type;
+  unsigned nx, ny, nz;
+  gzfp_mode m;
+  size_t header_bits;
+  if ((st = parse_header_mode(h, bytes * 8, &type, &nx, &ny, &nz, &m, &header_bits))) return st;
+  const uint64_t values = (uint64_t)nx * (ny ? ny : 1) * (nz ? nz : 1);
+  if (data_bytes < values * scalar_size(type))
+    return fail(GZFP_ERR_CAPACITY, "output buffer smaller than the field in the header");
+  return decompress_mode_impl(type, nx, ny, nz, &m, stream, bytes, nullptr, data, cuda_stream,
+                              header_bits);
 }
 
 }  // extern "C"

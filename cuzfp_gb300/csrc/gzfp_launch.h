@@ -54,19 +54,20 @@ cudaError_t launch_decode_mode(int dims, const uint64_t* in, uint64_t nwords,
                                const General& mode, T* out, cudaStream_t s);
 template <typename T>
 cudaError_t launch_index_blocks(int dims, const uint64_t* in, uint64_t nwords, uint64_t nblocks,
-                                const General& mode, unsigned long long* offsets,
+                                const General& mode, uint64_t first, unsigned long long* offsets,
                                 unsigned long long* end, cudaStream_t s);
-// Exclusive scan of n block lengths into start bits (sums: room for
-// ceil(n / 4096) + 1 entries; sums[ceil(n / 4096)] receives the total),
-// then the placement of every block at its start bit in a zeroed stream.
-cudaError_t launch_scan_lengths(const uint32_t* lengths, uint64_t n, uint64_t* sums,
-                                unsigned long long* offsets, cudaStream_t s);
+// Exclusive scan of n block lengths into start bits from `first` (sums:
+// room for ceil(n / 4096) + 1 entries; sums[ceil(n / 4096)] receives the
+// total length), then the placement of every block at its start bit in a
+// zeroed stream.
+cudaError_t launch_scan_lengths(const uint32_t* lengths, uint64_t n, uint64_t first,
+                                uint64_t* sums, unsigned long long* offsets, cudaStream_t s);
 uint64_t scan_sums_count(uint64_t n);
 // most bits one block can take under `mode` (gzfp_modes.cuh block_bound)
 uint32_t block_bound_host(int dims, int P, int ebits, const General& mode);
-// offsets[b] = b * maxbits: the start bits of a fixed-rate stream
-cudaError_t launch_fixed_offsets(unsigned long long* offsets, uint64_t n, uint32_t maxbits,
-                                 cudaStream_t s);
+// offsets[b] = first + b * maxbits: the start bits of a fixed-rate stream
+cudaError_t launch_fixed_offsets(unsigned long long* offsets, uint64_t n, uint64_t first,
+                                 uint32_t maxbits, cudaStream_t s);
 cudaError_t launch_place_blocks(const uint64_t* scratch, uint32_t slot_words,
                                 const uint32_t* lengths, const unsigned long long* offsets,
                                 uint64_t nblocks, uint64_t* out, cudaStream_t s);

@@ -74,16 +74,17 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
   scatter<D, T>(out, g, ix, iy, iz, raw);
 }
 
-// One thread walks the blocks of a stream: offsets[b] = start bit of block
-// b, *end = the bit after the last block.  Reads past the stream's words
-// see zeros, so a short stream ends the walk with an end past its size.
+// One thread walks the blocks of a stream from bit `first` (after a header,
+// or 0): offsets[b] = start bit of block b, *end = the bit after the last
+// block.  Reads past the stream's words see zeros, so a short stream ends
+// the walk with an end past its size.
 template <int D, typename T>
 __global__ void index_blocks_kernel(const uint64_t* __restrict__ in, uint64_t nwords,
-                                    uint64_t nblocks, General mode,
+                                    uint64_t nblocks, General mode, uint64_t first,
                                     unsigned long long* __restrict__ offsets,
                                     unsigned long long* __restrict__ end) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  uint64_t pos = 0;
+  uint64_t pos = first;
   for (uint64_t b = 0; b < nblocks; b++) {
     offsets[b] = pos;
     BitReader<DevWords> r(DevWords{nullptr, in, nwords}, pos);
@@ -146,12 +147,12 @@ cudaError_t launch_decode_mode(int dims, const uint64_t* in, uint64_t nwords,
 
 template <typename T>
 cudaError_t launch_index_blocks(int dims, const uint64_t* in, uint64_t nwords, uint64_t nblocks,
-                                const General& mode, unsigned long long* offsets,
+                                const General& mode, uint64_t first, unsigned long long* offsets,
                                 unsigned long long* end, cudaStream_t s) {
   switch (dims) {
-    case 1: index_blocks_kernel<1, T><<<1, 32, 0, s>>>(in, nwords, nblocks, mode, offsets, end); break;
-    case 2: index_blocks_kernel<2, T><<<1, 32, 0, s>>>(in, nwords, nblocks, mode, offsets, end); break;
-    case 3: index_blocks_kernel<3, T><<<1, 32, 0, s>>>(in, nwords, nblocks, mode, offsets, end); break;
+    case 1: index_blocks_kernel<1, T><<<1, 1, 0, s>>>(in, nwords, nblocks, mode, first, offsets, end); break;
+    case 2: index_blocks_kernel<2, T><<<1, 1, 0, s>>>(in, nwords, nblocks, mode, first, offsets, end); break;
+    case 3: index_blocks_kernel<3, T><<<1, 1, 0, s>>>(in, nwords, nblocks, mode, first, offsets, end); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

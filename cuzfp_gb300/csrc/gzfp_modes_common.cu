@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_sums(uint64_t* sums, uint64
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-    scan_chunks(const uint32_t* __restrict__ lengths, uint64_t n,
+    scan_chunks(const uint32_t* __restrict__ lengths, uint64_t n, uint64_t first,
                 const uint64_t* __restrict__ sums, uint64_t* __restrict__ offsets) {
   __shared__ uint64_t ws[kScanThreads / 32];
   // thread t scans its kScanPer consecutive lengths; the CTA scans the
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kScanThreads)
   }
   const uint64_t mine = v;
   cta_inclusive_scan(v, ws);
-  uint64_t pos = sums[blockIdx.x] + v - mine;
+  uint64_t pos = first + sums[blockIdx.x] + v - mine;
 #pragma unroll
   for (int j = 0; j < kScanPer; j++) {
     if (base + j < n) offsets[base + j] = pos;
@@ -126,13 +126,13 @@ uint32_t block_bound_host(int dims, int P, int ebits, const General& mode) {
 
 uint64_t scan_sums_count(uint64_t n) { return (n + kScanChunk - 1) / kScanChunk; }
 
-cudaError_t launch_scan_lengths(const uint32_t* lengths, uint64_t n, uint64_t* sums,
-                                unsigned long long* offsets, cudaStream_t s) {
+cudaError_t launch_scan_lengths(const uint32_t* lengths, uint64_t n, uint64_t first,
+                                uint64_t* sums, unsigned long long* offsets, cudaStream_t s) {
   const uint64_t m = scan_sums_count(n);
   if (m == 0) return cudaMemsetAsync(sums, 0, sizeof(uint64_t), s);
   scan_chunk_sums<<<(unsigned)m, kScanThreads, 0, s>>>(lengths, n, sums);
   scan_sums<<<1, kScanThreads, 0, s>>>(sums, m);
-  scan_chunks<<<(unsigned)m, kScanThreads, 0, s>>>(lengths, n, sums, (uint64_t*)offsets);
+  scan_chunks<<<(unsigned)m, kScanThreads, 0, s>>>(lengths, n, first, sums, (uint64_t*)offsets);
   return cudaGetLastError();
 }
 
@@ -145,15 +145,16 @@ cudaError_t launch_place_blocks(const uint64_t* scratch, uint32_t slot_words,
   return cudaGetLastError();
 }
 
-__global__ void fill_fixed_offsets(unsigned long long* offsets, uint64_t n, uint32_t maxbits) {
+__global__ void fill_fixed_offsets(unsigned long long* offsets, uint64_t n, uint64_t first,
+                                   uint32_t maxbits) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < n) offsets[b] = b * maxbits;
+  if (b < n) offsets[b] = first + b * maxbits;
 }
 
-cudaError_t launch_fixed_offsets(unsigned long long* offsets, uint64_t n, uint32_t maxbits,
-                                 cudaStream_t s) {
+cudaError_t launch_fixed_offsets(unsigned long long* offsets, uint64_t n, uint64_t first,
+                                 uint32_t maxbits, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  fill_fixed_offsets<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(offsets, n, maxbits);
+  fill_fixed_offsets<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(offsets, n, first, maxbits);
   return cudaGetLastError();
 }
 

@@ -11,7 +11,7 @@ template cudaError_t launch_decode_mode<double>(int, const uint64_t*, uint64_t,
                                             const unsigned long long*, const Geom&,
                                             const General&, double*, cudaStream_t);
 template cudaError_t launch_index_blocks<double>(int, const uint64_t*, uint64_t, uint64_t,
-                                             const General&, unsigned long long*,
+                                             const General&, uint64_t, unsigned long long*,
                                              unsigned long long*, cudaStream_t);
 
 }  // namespace gzfp

@@ -11,7 +11,7 @@ template cudaError_t launch_decode_mode<int64_t>(int, const uint64_t*, uint64_t,
                                             const unsigned long long*, const Geom&,
                                             const General&, int64_t*, cudaStream_t);
 template cudaError_t launch_index_blocks<int64_t>(int, const uint64_t*, uint64_t, uint64_t,
-                                             const General&, unsigned long long*,
+                                             const General&, uint64_t, unsigned long long*,
                                              unsigned long long*, cudaStream_t);
 
 }  // namespace gzfp

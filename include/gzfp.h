@@ -1,5 +1,5 @@
 /*
- * gzfp.h -- C ABI of the GB300 ZFP fixed-rate codec (libgzfp.so).
+ * gzfp.h -- C ABI of the GB300 ZFP codec (libgzfp.so).
  *
  * Drop-in replacement for the compress / decompress path of cuZFP
  * (src/cuZFP/cuZFP.h:9-10, implemented in src/cuZFP/cuZFP.cu:174-269): the
@@ -137,7 +137,11 @@ int gzfp_read_header(const void* header, size_t bytes, int* type, unsigned* nx, 
 
 /* Compress with a header in front, or decompress a stream that has one
    (the field's type and shape come from the header; `data_bytes` is the
-   capacity of `data`).  Pointers may be host or device memory. */
+   capacity of `data`).  Pointers may be host or device memory.
+   gzfp_decompress_headed takes streams of every mode: a header naming
+   fixed precision, fixed accuracy or other parameters (see "general
+   modes" below) is decoded in that mode, its blocks found by the serial
+   walk of gzfp_index_blocks. */
 int gzfp_compress_headed(int type, unsigned nx, unsigned ny, unsigned nz, double rate,
                          const void* data, void* stream, size_t capacity, size_t* out_bytes,
                          void* cuda_stream);
@@ -217,6 +221,21 @@ int gzfp_decompress_mode(int type, unsigned nx, unsigned ny, unsigned nz, const 
 int gzfp_index_blocks(int type, unsigned nx, unsigned ny, unsigned nz, const gzfp_mode* mode,
                       const void* stream, size_t bytes, unsigned long long* offsets,
                       void* cuda_stream);
+
+/* zfp's full header for any parameters (zfp_stream_mode's 12-bit forms
+   for fixed rate, precision and accuracy, else its 64-bit form), and the
+   header and parameters of a stream of any mode; gzfp_compress_mode_headed
+   writes the header, then the blocks (offsets count from the stream's
+   first bit). */
+int gzfp_write_header_mode(int type, unsigned nx, unsigned ny, unsigned nz,
+                           const gzfp_mode* mode, void* header, size_t capacity,
+                           size_t* header_bits);
+int gzfp_read_header_mode(const void* header, size_t bytes, int* type, unsigned* nx,
+                          unsigned* ny, unsigned* nz, gzfp_mode* mode, size_t* header_bits);
+int gzfp_compress_mode_headed(int type, unsigned nx, unsigned ny, unsigned nz,
+                              const gzfp_mode* mode, const void* data, void* stream,
+                              size_t capacity, size_t* out_bytes, unsigned long long* offsets,
+                              void* cuda_stream);
 
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and

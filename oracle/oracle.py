@@ -103,6 +103,13 @@ def port() -> ctypes.CDLL:
         lib.gzo_compress_params.restype = ctypes.c_size_t
         lib.gzo_compress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                  ctypes.c_void_p]
+        lib.gzo_compress_params_headed.restype = ctypes.c_size_t
+        lib.gzo_compress_params_headed.argtypes = _F + [ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.c_size_t]
+        lib.gzo_read_header_params.restype = ctypes.c_long
+        lib.gzo_read_header_params.argtypes = [ctypes.c_void_p, ctypes.c_size_t,
+                                               ctypes.POINTER(ctypes.c_int)] + \
+            [ctypes.POINTER(ctypes.c_uint)] * 3 + _PP
         lib.gzo_decompress_params.restype = ctypes.c_int
         lib.gzo_decompress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_size_t,
                                                    ctypes.c_void_p, ctypes.c_void_p]
@@ -170,6 +177,9 @@ def ref() -> ctypes.CDLL:
         lib.zref_decompress_params.restype = ctypes.c_int
         lib.zref_decompress_params.argtypes = _F + [ctypes.c_void_p, ctypes.c_size_t,
                                                     ctypes.c_void_p]
+        lib.zref_compress_params_headed.restype = ctypes.c_size_t
+        lib.zref_compress_params_headed.argtypes = _F + [ctypes.c_void_p, ctypes.c_void_p,
+                                                         ctypes.c_size_t]
         lib.zref_set_precision.restype = None
         lib.zref_set_precision.argtypes = [ctypes.c_int, ctypes.c_uint] + _PP
         lib.zref_set_accuracy.restype = None
@@ -558,3 +568,32 @@ def ref_decompress_params(words, shape, dtype, params: tuple) -> np.ndarray:
                                         padded.ctypes.data, padded.nbytes, out.ctypes.data):
         raise RuntimeError("reference decompress failed")
     return out
+
+
+def compress_params_headed(a: np.ndarray, params: tuple, lib=None) -> np.ndarray:
+    """The header of these parameters, then the blocks: the oracle's, or
+    with lib=ref() the reference's zfp_write_header + zfp_compress."""
+    a = np.ascontiguousarray(a)
+    nx, ny, nz = dims3(a.shape)
+    t = type_code(a.dtype)
+    cap = int(port().gzo_bound_params(t, nx, ny, nz, *params)) + 64
+    buf = np.zeros(cap // 8 + 1, np.uint64)
+    fn = port().gzo_compress_params_headed if lib is None else lib.zref_compress_params_headed
+    n = fn(t, nx, ny, nz, *params, a.ctypes.data, buf.ctypes.data, buf.nbytes)
+    if n == 0:
+        raise RuntimeError("headed compress failed")
+    return buf[: n // 8]
+
+
+def read_header_params(buf) -> dict:
+    b = np.ascontiguousarray(buf).view(np.uint8)
+    t = ctypes.c_int()
+    u = [ctypes.c_uint() for _ in range(6)]
+    e = ctypes.c_int()
+    bits = port().gzo_read_header_params(b.ctypes.data, b.nbytes, ctypes.byref(t),
+                                         *[ctypes.byref(v) for v in u], ctypes.byref(e))
+    if bits <= 0:
+        return {"bits": int(bits)}
+    nx, ny, nz, mn, mx, mp = [v.value for v in u]
+    return {"bits": int(bits), "dtype": np.dtype(_DTYPE_OF[t.value]),
+            "shape": _shape_of(nx, ny, nz), "params": (mn, mx, mp, e.value)}

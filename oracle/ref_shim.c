@@ -460,3 +460,24 @@ void zref_set_accuracy(int type, double tolerance, unsigned* minbits, unsigned* 
   stream_params(zfp, minbits, maxbits, maxprec, minexp);
   zfp_stream_close(zfp);
 }
+
+/* zfp_write_header(ZFP_HEADER_FULL) with these parameters, then
+   zfp_compress on the same bit stream (float and double fields). */
+size_t zref_compress_params_headed(int type, unsigned nx, unsigned ny, unsigned nz,
+                                   unsigned minbits, unsigned maxbits, unsigned maxprec,
+                                   int minexp, const void* data, void* buffer, size_t capacity) {
+  zfp_field* field = make_field(type, nx, ny, nz, (void*)data);
+  zfp_stream* zfp = zfp_stream_open(NULL);
+  size_t bytes = 0;
+  if (zfp_stream_set_params(zfp, minbits, maxbits, maxprec, minexp) &&
+      zfp_stream_maximum_size(zfp, field) <= capacity) {
+    bitstream* s = stream_open(buffer, capacity);
+    zfp_stream_set_bit_stream(zfp, s);
+    zfp_stream_rewind(zfp);
+    if (zfp_write_header(zfp, field, ZFP_HEADER_FULL)) bytes = zfp_compress(zfp, field);
+    stream_close(s);
+  }
+  zfp_stream_close(zfp);
+  zfp_field_free(field);
+  return bytes;
+}

@@ -736,9 +736,31 @@ int gzo_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz, long
    cannot record. */
 static unsigned header_put(wbits* w, const params* p) {
   uint64_t meta, mode;
+  unsigned mbits = 12;
   if (p->dims == 2 && (p->nx > (1u << 24) || p->ny > (1u << 24))) return 0;
   if (p->dims == 3 && (p->nx > (1u << 16) || p->ny > (1u << 16) || p->nz > (1u << 16))) return 0;
-  if (p->maxbits > 0x8000u) return 0;
+  /* zfp_stream_mode: the three 12-bit forms, else every parameter */
+  if (p->minbits == p->maxbits && p->maxbits >= 1 && p->maxbits <= 2048 && p->maxprec >= 64 &&
+      p->minexp <= GZO_MIN_EXP) {
+    mode = p->maxbits - 1u;
+  } else if (p->minbits == 0 && p->maxbits >= 4171 && p->maxprec >= 1 && p->maxprec <= 128 &&
+             p->minexp <= GZO_MIN_EXP) {
+    mode = p->maxprec + 2047u;
+  } else if (p->minbits == 0 && p->maxbits >= 4171 && p->maxprec >= 64 &&
+             p->minexp >= GZO_MIN_EXP && p->minexp <= 843) {
+    mode = (uint64_t)(p->minexp + 3251);
+  } else {
+    /* the 64-bit form would clamp these: no header records them */
+    if (p->minbits > 0x8000u || p->maxbits > 0x8000u || p->minexp + 16495 < 0 ||
+        p->minexp + 16495 > 0x7fff)
+      return 0;
+    mbits = 64;
+    mode = (uint64_t)(p->minexp + 16495);
+    mode = mode << 7 | (uint64_t)(p->maxprec - 1);
+    mode = mode << 15 | (uint64_t)(p->maxbits - 1);
+    mode = mode << 15 | (uint64_t)(p->minbits ? p->minbits - 1 : 0);
+    mode = mode << 12 | 0xfffu;
+  }
   w_put(w, 'z', 8);
   w_put(w, 'f', 8);
   w_put(w, 'p', 8);
@@ -751,17 +773,8 @@ static unsigned header_put(wbits* w, const params* p) {
     meta = (uint64_t)(p->nz - 1u) << 32 | (uint64_t)(p->ny - 1u) << 16 | (p->nx - 1u);
   meta = meta << 4 | (uint64_t)(p->dims - 1) << 2 | (uint64_t)(p->type - 1);
   w_put(w, meta, 52);
-  if (p->P >= 64 && p->maxbits <= 2048) {
-    w_put(w, p->maxbits - 1u, 12);
-    return 32 + 52 + 12;
-  }
-  mode = (uint64_t)(GZO_MIN_EXP + 16495);
-  mode = mode << 7 | (uint64_t)(p->P - 1);
-  mode = mode << 15 | (uint64_t)(p->maxbits - 1);
-  mode = mode << 15 | (uint64_t)(p->maxbits - 1);
-  mode = mode << 12 | 0xfffu;
-  w_put(w, mode, 64);
-  return 32 + 52 + 64;
+  w_put(w, mode, mbits);
+  return 32 + 52 + mbits;
 }
 
 static size_t headed_bytes(const params* p, unsigned header_bits) {
@@ -1093,4 +1106,100 @@ int gzo_decompress_params(int type, unsigned nx, unsigned ny, unsigned nz, unsig
   }
   free(padded);
   return b == nblocks && r.bit <= bytes / 8 * 64;
+}
+
+
+/* zfp_read_header's field and parameters for every mode (zfp_stream_set_mode,
+   Z/src/zfp.c:461-498).  Returns the header bits, 0 for a bad magic, a short
+   buffer or a field zfp 0.5.0 cannot hold. */
+long gzo_read_header_params(const void* stream, size_t bytes, int* type, unsigned* nx,
+                            unsigned* ny, unsigned* nz, unsigned* minbits, unsigned* maxbits,
+                            unsigned* maxprec, int* minexp) {
+  uint64_t words[3] = {0, 0, 0};
+  rbits r;
+  uint64_t meta, mode;
+  int dims;
+  long bits = 32 + 52 + 12;
+  memcpy(words, stream, bytes < sizeof words ? bytes : sizeof words);
+  if (bytes * 8 < (size_t)bits) return 0;
+  r.words = words;
+  r.bit = 0;
+  if (r_get(&r, 8) != 'z' || r_get(&r, 8) != 'f' || r_get(&r, 8) != 'p' || r_get(&r, 8) != 0x05)
+    return 0;
+  meta = r_get(&r, 52);
+  *type = (int)(meta & 3) + 1;
+  dims = (int)(meta >> 2 & 3) + 1;
+  meta >>= 4;
+  *ny = *nz = 0;
+  if (dims == 1) {
+    if ((meta & 0xffffffffffffull) >= 0xffffffffull) return 0;
+    *nx = (unsigned)(meta & 0xffffffffffffull) + 1u;
+  } else if (dims == 2) {
+    *nx = (unsigned)(meta & 0xffffff) + 1u;
+    *ny = (unsigned)(meta >> 24 & 0xffffff) + 1u;
+  } else if (dims == 3) {
+    *nx = (unsigned)(meta & 0xffff) + 1u;
+    *ny = (unsigned)(meta >> 16 & 0xffff) + 1u;
+    *nz = (unsigned)(meta >> 32 & 0xffff) + 1u;
+  } else {
+    return 0;
+  }
+  mode = r_get(&r, 12);
+  if (mode < 2048) {
+    *minbits = *maxbits = (unsigned)mode + 1u;
+    *maxprec = 64;
+    *minexp = GZO_MIN_EXP;
+  } else if (mode < 2176) {
+    *minbits = 0;
+    *maxbits = 4171;
+    *maxprec = (unsigned)mode - 2047u;
+    *minexp = GZO_MIN_EXP;
+  } else if (mode < 4095) {
+    *minbits = 0;
+    *maxbits = 4171;
+    *maxprec = 64;
+    *minexp = (int)mode - 3251;
+  } else {
+    bits = 32 + 52 + 64;
+    if (bytes * 8 < (size_t)bits) return 0;
+    mode += r_get(&r, 52) << 12;
+    *minbits = (unsigned)(mode >> 12 & 0x7fff) + 1u;
+    *maxbits = (unsigned)(mode >> 27 & 0x7fff) + 1u;
+    *maxprec = (unsigned)(mode >> 42 & 0x7f) + 1u;
+    *minexp = (int)(mode >> 49 & 0x7fff) - 16495;
+  }
+  return bits;
+}
+
+/* The header of these parameters, then the blocks (zfp_write_header, then
+   zfp_compress with them).  Returns the stream size in bytes, 0 on a bad
+   argument, parameters no header records, or a short buffer. */
+size_t gzo_compress_params_headed(int type, unsigned nx, unsigned ny, unsigned nz,
+                                  unsigned minbits, unsigned maxbits, unsigned maxprec,
+                                  int minexp, const void* data, void* stream, size_t capacity) {
+  params p;
+  uint64_t scratch[3];
+  wbits w;
+  unsigned hb;
+  uint64_t b, nblocks, pos;
+  double blk[64];
+  if (!setup_params(&p, type, nx, ny, nz, minbits, maxbits, maxprec, minexp)) return 0;
+  w_init(&w, scratch, 0);
+  hb = header_put(&w, &p);
+  if (!hb) return 0;
+  if (capacity < gzo_bound_params(type, nx, ny, nz, minbits, maxbits, maxprec, minexp) + 24)
+    return 0;
+  w_init(&w, (uint64_t*)stream, 0);
+  header_put(&w, &p);
+  nblocks = (uint64_t)p.bx * p.by * p.bz;
+  for (b = 0; b < nblocks; b++) {
+    unsigned bx = (unsigned)(b % p.bx);
+    unsigned by = (unsigned)((b / p.bx) % p.by);
+    unsigned bz = (unsigned)(b / ((uint64_t)p.bx * p.by));
+    gather(&p, data, bx, by, bz, blk);
+    encode_block(&w, &p, blk);
+  }
+  pos = (uint64_t)w.pos * 64 + w.fill;
+  w_flush(&w);
+  return (size_t)((pos + 63) / 64 * 8);
 }

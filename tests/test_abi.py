@@ -222,3 +222,31 @@ def test_mode_argument_errors(gz):
     assert gz.mode_maximum_size(3, 8, 8, 8, gz.Mode(0, 8, 32, -1074)) == 0  # under the block header
     with pytest.raises(gz.GzfpError):
         gz.mode_accuracy(4, float("nan"))
+
+
+def test_header_mode_write_read(gz, orc):
+    """gzfp_write_header_mode writes the oracle's header bits for every mode
+    form, and gzfp_read_header_mode reads back the parameters zfp would."""
+    n = 0
+    for t, dt in ((3, np.float32), (4, np.float64), (1, np.int32), (2, np.int64)):
+        for shape in ((203,), (9, 13), (5, 6, 7)):
+            nx, ny, nz = orc.dims3(shape)
+            modes = [gz.mode_precision(t, p) for p in (3, 24, 64)]
+            modes += [gz.mode_accuracy(t, tol) for tol in (1e-8, 0.5)]
+            modes += [gz.Mode(100, 300, 40, -30), gz.Mode(200, 200, 64, -1074),
+                      gz.Mode(0, 4171, 16, -20), gz.mode_rate(t, len(shape), 9.0)]
+            for m in modes:
+                if m.maxbits < {3: 9, 4: 12}.get(t, 1):
+                    continue
+                raw, bits = gz.write_header_mode(t, nx, ny, nz, m)
+                a = np.zeros(shape, dt)
+                s = orc.compress_params_headed(a, m.as_tuple())
+                sb = np.unpackbits(s.view(np.uint8), bitorder="little")[:bits]
+                hb = np.unpackbits(np.frombuffer(raw, np.uint8), bitorder="little")[:bits]
+                assert np.array_equal(hb, sb), (t, shape, m.as_tuple())
+                h = gz.read_header_mode(raw)
+                ho = orc.read_header_params(s)
+                assert h["bits"] == bits == ho["bits"] and h["shape"] == shape
+                assert h["mode"].as_tuple() == ho["params"], (m.as_tuple(), ho)
+                n += 1
+    assert n > 80

@@ -117,3 +117,30 @@ def test_mode_errors(gz, cuda):
     with pytest.raises(gz.GzfpError) as e:  # stream cut short: the walk runs past it
         gz.decompress_mode(w[: w.numel() // 2], x.shape, x.dtype, m)
     assert e.value.status == gz.GZFP_ERR_ARG
+
+
+@pytest.mark.parametrize("dt", list(TYPES))
+def test_headed_modes(gz, orc, cuda, dt):
+    """A header of the mode, then the blocks: the oracle's stream (itself
+    pinned to zfp_write_header + zfp_compress); gzfp_decompress_headed
+    decodes it from the header alone."""
+    import torch
+    rng = np.random.default_rng(123)
+    t = TYPES[dt]
+    for shape in ((203,), (37, 29), (9, 10, 11)):
+        a = _field(rng, dt, shape)
+        for m in (gz.mode_precision(t, 20), gz.mode_accuracy(t, 1e-4), gz.Mode(100, 300, 40, -30),
+                  gz.mode_rate(t, len(shape), 10.0)):
+            s = orc.compress_params_headed(a, m.as_tuple())
+            x = torch.from_numpy(a).to(cuda)
+            w, offs = gz.compress_mode_headed(x, m, with_offsets=True)
+            torch.cuda.synchronize()
+            assert np.array_equal(w.cpu().numpy().view(np.uint64), s), (shape, m.as_tuple())
+            h = gz.read_header_mode(w)
+            assert int(offs[0]) == h["bits"]
+            d = gz.decompress_headed(w)
+            torch.cuda.synchronize()
+            exp = orc.decompress_params(orc.compress_params(a, m.as_tuple()), shape, a.dtype,
+                                        m.as_tuple())
+            assert np.array_equal(d.cpu().numpy(), exp), (shape, m.as_tuple())
+            assert np.array_equal(gz.decompress_headed(s), exp)  # host stream

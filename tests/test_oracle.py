@@ -451,3 +451,20 @@ def test_general_params_golden(orc):
         assert np.array_equal(s, c["stream"]), c["name"]
         assert np.array_equal(orc.decompress_params(c["stream"], a.shape, a.dtype, c["params"]),
                               c["output"]), c["name"]
+
+
+def test_general_headers_match_reference(ref):
+    """Headers of every mode -- the 12-bit fixed-precision and
+    fixed-accuracy forms and the 64-bit form -- followed by the blocks, as
+    zfp_write_header + zfp_compress write them; zfp_read_header's parameters
+    read back."""
+    rng = np.random.default_rng(131)
+    for dt in (np.float32, np.float64):
+        for shape in ((37,), (9, 13), (5, 6, 7)):
+            a = np.cumsum(rng.standard_normal(shape), axis=-1).astype(dt)
+            for pr in _mode_list(ref, dt):
+                s = ref.compress_params_headed(a, pr)
+                assert np.array_equal(s, ref.compress_params_headed(a, pr, lib=ref.ref())), pr
+                h, r = ref.read_header_params(s), ref.ref_read_header(s)
+                assert h["bits"] == r["bits"] and h["shape"] == shape
+                assert h["params"] == (r["minbits"], r["maxbits"], r["maxprec"], r["minexp"])
