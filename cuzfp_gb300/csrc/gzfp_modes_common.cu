@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(kThreads)
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b >= nblocks) return;
   const uint32_t len = lengths[b];
+  if (len == 0) return;  // every block takes at least one bit; nothing to place
   const uint64_t pos = offsets[b], end = pos + len;
   const uint64_t* src = scratch + b * slot_words;
   const uint32_t sh = (uint32_t)(pos & 63);
