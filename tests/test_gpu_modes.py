@@ -144,3 +144,27 @@ def test_headed_modes(gz, orc, cuda, dt):
                                         m.as_tuple())
             assert np.array_equal(d.cpu().numpy(), exp), (shape, m.as_tuple())
             assert np.array_equal(gz.decompress_headed(s), exp)  # host stream
+
+
+def test_random_params(gz, orc, cuda):
+    """Random stream parameters and shapes, every scalar type: the GPU's
+    streams, block start bits and decoded arrays are the oracle's."""
+    import torch
+    from tests.test_oracle import _random_params
+    rng = np.random.default_rng(142)
+    for k in range(80):
+        dt = ("float32", "float64", "int32", "int64")[k % 4]
+        d = 1 + int(rng.integers(0, 3))
+        shape = tuple(int(v) for v in rng.integers(1, 30, d))
+        a = _field(rng, dt, shape)
+        pr = _random_params(rng, np.dtype(dt).type)
+        m = gz.Mode(*pr)
+        s, so = orc.compress_params(a, pr, with_offsets=True)
+        x = torch.from_numpy(a).to(cuda)
+        w, offs = gz.compress_mode(x, m, with_offsets=True)
+        torch.cuda.synchronize()
+        assert np.array_equal(w.cpu().numpy().view(np.uint64), s), (dt, shape, pr)
+        assert np.array_equal(offs.cpu().numpy().view(np.uint64), so), (dt, shape, pr)
+        d_gpu = gz.decompress_mode(w, shape, x.dtype, m, offsets=offs)
+        torch.cuda.synchronize()
+        assert np.array_equal(d_gpu.cpu().numpy(), orc.decompress_params(s, shape, a.dtype, pr))

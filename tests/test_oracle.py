@@ -468,3 +468,31 @@ def test_general_headers_match_reference(ref):
                 h, r = ref.read_header_params(s), ref.ref_read_header(s)
                 assert h["bits"] == r["bits"] and h["shape"] == shape
                 assert h["params"] == (r["minbits"], r["maxbits"], r["maxprec"], r["minexp"])
+
+
+def _random_params(rng, dt):
+    lo = {np.float32: 9, np.float64: 12}.get(dt, 1)
+    minbits = int(rng.choice([0, 0, int(rng.integers(1, 700))]))
+    maxbits = int(max(lo, minbits, int(rng.integers(lo, 4500))))
+    return (minbits, maxbits, int(rng.integers(1, 65)), int(rng.integers(-1100, 60)))
+
+
+def test_random_params_match_reference(ref):
+    """Random stream parameters (any minbits, maxbits, maxprec, minexp that
+    zfp_stream_set_params accepts) on random fields: the oracle's streams
+    are the reference's."""
+    rng = np.random.default_rng(141)
+    for k in range(120):
+        dt = (np.float32, np.float64, np.int32, np.int64)[k % 4]
+        d = 1 + int(rng.integers(0, 3))
+        if ref.is_int(dt):
+            shape = tuple(4 * int(v) for v in rng.integers(1, 6, d))
+        else:
+            shape = tuple(int(v) for v in rng.integers(1, 23, d))
+        a = np.cumsum(rng.standard_normal(shape) * 10.0 ** rng.integers(-5, 5), axis=-1)
+        a = (a * 1000).astype(dt) if ref.is_int(dt) else a.astype(dt)
+        pr = _random_params(rng, dt)
+        s = ref.compress_params(a, pr)
+        assert np.array_equal(s, ref.ref_compress_params(a, pr)), (dt, shape, pr)
+        assert np.array_equal(ref.decompress_params(s, shape, dt, pr),
+                              ref.ref_decompress_params(s, shape, dt, pr)), (dt, shape, pr)
