@@ -208,9 +208,39 @@ def stream_set_rate(zfp: zfp_stream, rate: float, type: zfp_type, dims: int) -> 
     return bits / float(1 << (2 * dims))
 
 
+def zfp_stream_set_precision(zfp: zfp_stream, precision: int, type: zfp_type) -> int:
+    """zfp's fixed-precision mode (zfp-0.5.0/src/zfp.c:432-441)."""
+    m = mode_precision(type, precision)
+    zfp.minbits, zfp.maxbits, zfp.maxprec, zfp.minexp = m.as_tuple()
+    return m.maxprec
+
+
+def zfp_stream_set_accuracy(zfp: zfp_stream, tolerance: float, type: zfp_type) -> float:
+    """zfp's fixed-accuracy mode (zfp-0.5.0/src/zfp.c:443-458)."""
+    m = mode_accuracy(type, tolerance)
+    zfp.minbits, zfp.maxbits, zfp.maxprec, zfp.minexp = m.as_tuple()
+    return 2.0 ** m.minexp if tolerance > 0 else 0.0
+
+
+def _fixed_rate(zfp: zfp_stream, t: zfp_type) -> bool:
+    """The parameters of fixed-rate coding (the fixed-rate path's)."""
+    ints = zfp_type(t) in (zfp_type.int32, zfp_type.int64)
+    prec = 32 if zfp_type(t) in (zfp_type.float, zfp_type.int32) else 64
+    return (zfp.minbits == zfp.maxbits and zfp.maxprec >= prec
+            and (ints or zfp.minexp == ZFP_MIN_EXP))
+
+
+def _mode_of(zfp: zfp_stream):
+    return Mode(zfp.minbits, zfp.maxbits, zfp.maxprec, zfp.minexp)
+
+
 def zfp_stream_maximum_size(zfp: zfp_stream, f: zfp_field) -> int:
-    """Worst-case buffer bytes (zfp_structs.h:222-251)."""
-    return int(_lib.gzfp_maximum_size(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits))
+    """Worst-case buffer bytes (zfp_structs.h:222-251), header allowance
+    included, for every mode."""
+    if _fixed_rate(zfp, f.type):
+        return int(_lib.gzfp_maximum_size(int(f.type), f.nx, f.ny, f.nz, zfp.maxbits))
+    n = mode_maximum_size(f.type, f.nx, f.ny, f.nz, _mode_of(zfp))
+    return n + 24 if n else 0
 
 
 def stream_size(type: zfp_type, nx: int, ny: int, nz: int, maxbits: int) -> int:
@@ -270,9 +300,9 @@ def _cuda_stream_handle(cuda_stream: Any) -> int:
     return int(cuda_stream.cuda_stream)  # torch.cuda.Stream
 
 
-def _check_fixed_rate(zfp: zfp_stream, f: zfp_field) -> None:
-    if zfp.minbits != zfp.maxbits:
-        raise GzfpError(GZFP_ERR_UNSUPPORTED, "only fixed-rate streams (minbits == maxbits)")
+def _check_strided_mode(zfp: zfp_stream, f: zfp_field, strides) -> None:
+    if strides and not _fixed_rate(zfp, f.type):
+        raise GzfpError(GZFP_ERR_UNSUPPORTED, "strided fields take the fixed-rate path only")
 
 
 def compress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> int:
@@ -281,10 +311,25 @@ def compress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> int:
     Mirrors cuZFP::compress (src/cuZFP/cuZFP.cu:174-210).  With device
     buffers the work is queued on ``cuda_stream`` (default: the legacy
     default stream) and the call returns at once; with a host buffer it
-    returns when the result is in host memory.
+    returns when the result is in host memory.  Parameters other than fixed
+    rate (zfp_stream_set_precision / _accuracy) take zfp's general mode,
+    which returns when the stream is complete.
     """
-    _check_fixed_rate(zfp, f)
     strides = _field_strides(f)
+    _check_strided_mode(zfp, f, strides)
+    if not _fixed_rate(zfp, f.type):
+        src, _ = _addr_and_size(f.data)
+        dst, cap = _addr_and_size(zfp.stream)
+        if zfp.capacity is not None:
+            cap = zfp.capacity
+        if cap is None:
+            cap = zfp_stream_maximum_size(zfp, f)
+        out = _SZ(0)
+        m = _mode_of(zfp)
+        _check(_lib.gzfp_compress_mode(int(f.type), f.nx, f.ny, f.nz, ctypes.byref(m), src, dst,
+                                       cap, ctypes.byref(out), None,
+                                       _cuda_stream_handle(cuda_stream)), "compress")
+        return int(out.value)
     src = _field_addr(f.data) if strides else _addr_and_size(f.data)[0]
     dst, cap = _addr_and_size(zfp.stream)
     if zfp.capacity is not None:
@@ -305,9 +350,21 @@ def compress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> int:
 
 def decompress(zfp: zfp_stream, f: zfp_field, cuda_stream: Any = None) -> None:
     """Decompress ``zfp.stream`` into ``f.data`` (cuZFP::decompress,
-    src/cuZFP/cuZFP.cu:212-269)."""
-    _check_fixed_rate(zfp, f)
+    src/cuZFP/cuZFP.cu:212-269); in zfp's general mode the blocks are found
+    by walking them (see decompress_mode for decoding from known offsets)."""
     strides = _field_strides(f)
+    _check_strided_mode(zfp, f, strides)
+    if not _fixed_rate(zfp, f.type):
+        src, size = _addr_and_size(zfp.stream)
+        if zfp.capacity is not None:
+            size = zfp.capacity
+        if size is None:
+            size = zfp_stream_maximum_size(zfp, f)
+        m = _mode_of(zfp)
+        _check(_lib.gzfp_decompress_mode(int(f.type), f.nx, f.ny, f.nz, ctypes.byref(m), src,
+                                         size, None, _addr_and_size(f.data)[0],
+                                         _cuda_stream_handle(cuda_stream)), "decompress")
+        return
     src, size = _addr_and_size(zfp.stream)
     dst = _field_addr(f.data) if strides else _addr_and_size(f.data)[0]
     if zfp.capacity is not None:
@@ -950,5 +1007,5 @@ __all__ = [
     "compress_headed", "decompress_headed", "decode_blocks", "encode_blocks", "Mode",
     "mode_rate", "mode_precision", "mode_accuracy", "mode_maximum_size", "compress_mode",
     "decompress_mode", "index_blocks", "read_header_mode", "write_header_mode",
-    "compress_mode_headed",
+    "compress_mode_headed", "zfp_stream_set_precision", "zfp_stream_set_accuracy",
 ]

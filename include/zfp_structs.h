@@ -13,6 +13,7 @@
 #define GZFP_ZFP_STRUCTS_H
 
 #include <climits>
+#include <cmath>
 #include <cstddef>
 #include <cstdlib>
 
@@ -65,6 +66,31 @@ static inline double stream_set_rate(zfp_stream* zfp, double rate, zfp_type type
   zfp->maxprec = ZFP_MAX_PREC;
   zfp->minexp = ZFP_MIN_EXP;
   return (double)bits / (double)(1u << (2 * dims));
+}
+
+/* zfp's fixed-precision and fixed-accuracy settings (zfp 0.5.0,
+   zfp_stream_set_precision / zfp_stream_set_accuracy, src/zfp.c:432-458);
+   not in cuZFP, which is fixed-rate only.  Return the precision, or the
+   tolerance actually used. */
+static inline unsigned int zfp_stream_set_precision(zfp_stream* zfp, unsigned int precision,
+                                                    zfp_type type) {
+  gzfp_mode m;
+  if (gzfp_mode_precision((int)type, precision, &m) != GZFP_OK) return 0;
+  zfp->minbits = m.minbits;
+  zfp->maxbits = m.maxbits;
+  zfp->maxprec = m.maxprec;
+  zfp->minexp = m.minexp;
+  return m.maxprec;
+}
+
+static inline double zfp_stream_set_accuracy(zfp_stream* zfp, double tolerance, zfp_type type) {
+  gzfp_mode m;
+  if (gzfp_mode_accuracy((int)type, tolerance, &m) != GZFP_OK) return 0.0;
+  zfp->minbits = m.minbits;
+  zfp->maxbits = m.maxbits;
+  zfp->maxprec = m.maxprec;
+  zfp->minexp = m.minexp;
+  return tolerance > 0 ? std::ldexp(1.0, m.minexp) : 0.0;
 }
 
 static inline zfp_field* zfp_field_alloc() {

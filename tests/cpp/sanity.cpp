@@ -3,7 +3,8 @@
 // Mirrors the checks of cuZFP's own gtest smoke tests: exact integer round
 // trips at rate 8 for 1D (128 values), 2D (4x4) and 3D (16x8x4) float
 // fields (src/tests/t_sanity_check_{1,2,3}.cpp) and the same 3D case with a
-// device-resident stream (src/tests/t_cuda_mem.cu), plus a strided field.  Built and run by
+// device-resident stream (src/tests/t_cuda_mem.cu), plus a strided field and
+// zfp's fixed-accuracy mode.  Built and run by
 // tests/test_cpp_dropin.py on a GPU machine; prints "ok" on success.
 #include <cuda_runtime.h>
 
@@ -99,6 +100,35 @@ int main() {
     zfp_field_free(fc);
     zfp_field_free(gs);
     zfp_field_free(gc);
+  }
+  // zfp's fixed-accuracy mode through the same calls: the stream of
+  // gzfp_compress_mode, decoded within the tolerance
+  {
+    const unsigned nx = 16, ny = 8, nz = 4, n = nx * ny * nz;
+    std::vector<double> in(n), out(n, -1.0);
+    for (unsigned i = 0; i < n; i++) in[i] = 0.01 * i + 0.5 * (i % 5);
+    zfp_field* f = zfp_field_3d(in.data(), zfp_type_double, nx, ny, nz);
+    zfp_stream zfp;
+    zfp_stream_set_accuracy(&zfp, 1e-4, zfp_type_double);
+    std::vector<unsigned char> buf(zfp_stream_maximum_size(&zfp, f)), ref(buf.size());
+    zfp.stream = (Word*)buf.data();
+    const size_t bytes = compress(&zfp, f);
+    gzfp_mode m{zfp.minbits, zfp.maxbits, zfp.maxprec, zfp.minexp};
+    size_t rbytes = 0;
+    if (!bytes || gzfp_compress_mode(GZFP_TYPE_DOUBLE, nx, ny, nz, &m, in.data(), ref.data(),
+                                     ref.size(), &rbytes, nullptr, nullptr) != GZFP_OK ||
+        rbytes != bytes || std::memcmp(buf.data(), ref.data(), bytes))
+      fails++;
+    zfp_field* g = zfp_field_3d(out.data(), zfp_type_double, nx, ny, nz);
+    decompress(&zfp, g);
+    if (last_status() != GZFP_OK) fails++;
+    for (unsigned i = 0; i < n; i++)
+      if (out[i] - in[i] > 1e-4 || in[i] - out[i] > 1e-4) {
+        fails++;
+        break;
+      }
+    zfp_field_free(f);
+    zfp_field_free(g);
   }
   std::printf(fails ? "FAILED %d\n" : "ok\n", fails);
   return fails ? 1 : 0;

@@ -102,10 +102,15 @@ def test_python_mirror_errors(gz):
     gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 3)
     assert zfp.maxbits == zfp.minbits == 512
     f = gz.zfp_field_3d(None, gz.zfp_type.float, 4, 4, 4)
-    zfp.minbits = 0  # not fixed rate: the only mode of this path
+    zfp.minbits = 0  # not fixed rate: zfp's general mode, but no data
+    with pytest.raises(gz.GzfpError) as e:
+        gz.compress(zfp, f)
+    assert e.value.status == gz.GZFP_ERR_ARG
+    f.sx = 2  # strided fields take the fixed-rate path only
     with pytest.raises(gz.GzfpError) as e:
         gz.compress(zfp, f)
     assert e.value.status == gz.GZFP_ERR_UNSUPPORTED
+    f.sx = 0
     gz.stream_set_rate(zfp, 8.0, gz.zfp_type.float, 3)
     f.sx = 2
     with pytest.raises(gz.GzfpError) as e:  # strided, but no data

@@ -168,3 +168,30 @@ def test_random_params(gz, orc, cuda):
         d_gpu = gz.decompress_mode(w, shape, x.dtype, m, offsets=offs)
         torch.cuda.synchronize()
         assert np.array_equal(d_gpu.cpu().numpy(), orc.decompress_params(s, shape, a.dtype, pr))
+
+
+def test_mirror_compress_in_general_mode(gz, orc, cuda):
+    """The cuZFP-style compress / decompress with zfp_stream_set_accuracy or
+    _precision take the general mode: compress_mode's stream, decoded by
+    walking its blocks."""
+    import torch
+    rng = np.random.default_rng(124)
+    a = _field(rng, "float32", (24, 20, 36))
+    x = torch.from_numpy(a).to(cuda)
+    for setter, v in ((gz.zfp_stream_set_accuracy, 1e-3), (gz.zfp_stream_set_precision, 18)):
+        zfp = gz.zfp_stream()
+        setter(zfp, v, gz.zfp_type.float)
+        f = gz.zfp_field_3d(x, gz.zfp_type.float, 36, 20, 24)
+        cap = gz.zfp_stream_maximum_size(zfp, f)
+        zfp.stream = torch.zeros(cap // 8, dtype=torch.int64, device=cuda)
+        n = gz.compress(zfp, f)
+        exp = orc.compress_params(a, (zfp.minbits, zfp.maxbits, zfp.maxprec, zfp.minexp))
+        assert n == exp.nbytes
+        assert np.array_equal(zfp.stream[: n // 8].cpu().numpy().view(np.uint64), exp)
+        out = torch.empty_like(x)
+        gz.decompress(zfp, gz.zfp_field_3d(out, gz.zfp_type.float, 36, 20, 24))
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(),
+                              orc.decompress_params(exp, a.shape, a.dtype,
+                                                    (zfp.minbits, zfp.maxbits, zfp.maxprec,
+                                                     zfp.minexp)))
