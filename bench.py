@@ -52,11 +52,12 @@ def parse():
                    help="cube edge of the field (smaller cases for profiling)")
     p.add_argument("--rate", type=float, default=16.0)
     p.add_argument("--workload", default="plain3d",
-                   choices=["plain3d", "batched", "serving", "accuracy"],
+                   choices=["plain3d", "batched", "serving", "accuracy", "edges"],
                    help="plain3d: the 1 GiB 3D float64 field (default); batched: 512 mixed "
                         "3D arrays in one persistent launch vs 512 plain launches; serving: "
                         "Poisson request arrivals through the request server; accuracy: the "
-                        "plain3d field in zfp's fixed-accuracy mode")
+                        "plain3d field in zfp's fixed-accuracy mode; edges: the 1D and 2D "
+                        "fields with partial edge blocks at rates 4, 12 and 24")
     p.add_argument("--tolerance", type=float, default=1e-6,
                    help="accuracy workload: absolute error tolerance")
     p.add_argument("--arrays", type=int, default=512, help="batched workload: array count")
@@ -507,6 +508,88 @@ def run_serving(args, rank, world, local):
     print(json.dumps(res_line), flush=True)
 
 
+def run_edges(args, rank, world, local):
+    """The 1D and 2D fields whose last blocks are partial: 1D float32 of
+    2^28 - 3 values (random walk), 2D float32 16381 x 16383 and float64
+    8191 x 8190 (8 sinusoids, |k| up to 64), each at 4, 12 and 24 bits per
+    value, compress and decompress kernels timed with CUDA events."""
+    import torch
+
+    import cuzfp_gb300 as gz
+    from cuzfp_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    peak, peak_kind = peaks()
+    cases, tot_bytes, tot_ms = [], 0, 0.0
+    fields = [("1d_f32_walk", lambda: synth.random_walk_device((1 << 28) - 3, seed=2 + rank,
+                                                            dtype=torch.float32, device=dev)),
+              ("2d_f32_16381x16383", lambda: synth.sinusoids_device(
+                  (16383, 16381), 8, 64, seed=3 + rank, dtype=torch.float32, device=dev)),
+              ("2d_f64_8191x8190", lambda: synth.sinusoids_device(
+                  (8190, 8191), 8, 64, seed=4 + rank, dtype=torch.float64, device=dev))]
+    with ClockSampler(local) as clk:
+        for name, make in fields:
+            x = make()
+            nbytes = x.numel() * x.element_size()
+            for rate in (4.0, 12.0, 24.0):
+                words = gz.compress_tensor(x, rate)
+                out = torch.empty_like(x)
+                sbytes = words.numel() * 8
+                for _ in range(max(args.warmup, 3)):
+                    gz.compress_tensor(x, rate, out=words, cuda_stream=stream)
+                    gz.decompress_tensor(words, x.shape, x.dtype, rate, out=out, cuda_stream=stream)
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+                torch.cuda.synchronize()
+                if world > 1:
+                    torch.distributed.barrier()
+                with torch.cuda.stream(stream):
+                    for i in range(args.steps):
+                        ev[3 * i].record(stream)
+                        gz.compress_tensor(x, rate, out=words, cuda_stream=stream)
+                        ev[3 * i + 1].record(stream)
+                        gz.decompress_tensor(words, x.shape, x.dtype, rate, out=out,
+                                             cuda_stream=stream)
+                        ev[3 * i + 2].record(stream)
+                stream.synchronize()
+                enc = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
+                dec = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
+                enc = max_over_ranks(enc, world, dev)
+                dec = max_over_ranks(dec, world, dev)
+                alg = nbytes + sbytes
+                cases.append({"field": name, "rate": rate, "encode_ms": round(enc, 4),
+                              "decode_ms": round(dec, 4),
+                              "gbs": round(2 * nbytes / ((enc + dec) * 1e-3) / 1e9, 2),
+                              "encode_frac": round(alg / (enc * 1e-3) / 1e9 / peak, 4),
+                              "decode_frac": round(alg / (dec * 1e-3) / 1e9 / peak, 4)})
+                tot_bytes += 2 * nbytes
+                tot_ms += enc + dec
+                del words, out
+            del x
+            torch.cuda.empty_cache()
+    if rank != 0:
+        return
+    worst = max(cases, key=lambda c: c["encode_ms"] + c["decode_ms"])
+    res = {
+        "metric": "zfp fixed-rate compress+decompress throughput, 1D/2D fields with partial edge blocks",
+        "value": round(tot_bytes * world / (tot_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(tot_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "edges_1d_f32_2d_f32_2d_f64_rates_4_12_24",
+                   "l2": "inputs larger than L2 (0.5-1 GiB fields)",
+                   "parallelism": f"replicas x{world}"},
+        "cases": cases,
+        "roofline": {"bound": "hbm", "kernel": f"slowest case {worst['field']} rate {worst['rate']}",
+                     "frac": min(worst["encode_frac"], worst["decode_frac"]), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "traffic": None},
+        "gpu_launches": 2 * args.steps * len(cases),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(res), flush=True)
+
+
 def run_accuracy(args, rank, world, local):
     """The plain3d field in zfp's fixed-accuracy mode: variable-length blocks,
     compressed on the device with their start bits and decompressed from
@@ -623,6 +706,9 @@ def run(args, rank, world, local):
         return
     if args.workload == "accuracy":
         run_accuracy(args, rank, world, local)
+        return
+    if args.workload == "edges":
+        run_edges(args, rank, world, local)
         return
     import numpy as np
     import torch

@@ -68,6 +68,21 @@ GZ_HD uint32_t clz64(uint64_t x) {
 #endif
 }
 
+GZ_HD uint32_t clz32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__clz((int)x);
+#else
+  return x ? (uint32_t)__builtin_clz(x) : 32u;
+#endif
+}
+GZ_HD uint32_t popcount32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__popc(x);
+#else
+  return (uint32_t)__builtin_popcount(x);
+#endif
+}
+
 GZ_HD uint32_t umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
 GZ_HD uint32_t lo32(uint64_t v) { return (uint32_t)v; }
 GZ_HD uint32_t hi32(uint64_t v) { return (uint32_t)(v >> 32); }
@@ -442,6 +457,53 @@ GZ_HD uint64_t rank_spread(uint64_t z) {
   return S;
 }
 
+// Rank spread of a plane of at most 16 bits: below 2^31.
+GZ_HD uint32_t rank_spread32(uint32_t z) {
+  const uint32_t z1 = z & (z - 1);
+  uint32_t z2 = z1 & (z1 - 1);
+  uint32_t S = z + z1 + (z2 << 1);
+  for (uint32_t j = 2; z2; j++) {
+    z2 &= z2 - 1;
+    S += z2 << j;
+  }
+  return S;
+}
+
+// code_planes for blocks of at most 16 values (1D and 2D): a plane has at
+// most 16 bits and its whole code -- verbatim bits, then group tests -- at
+// most 16 + 33 bits, so it is built in 32-bit arithmetic and written in one
+// piece.  Same bits as the general form below.
+template <int BS, class W, class PlaneFn>
+GZ_HD int code_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, W& w,
+                            PlaneFn&& plane) {
+  static_assert(BS <= 16, "at most 16 values per block");
+  for (; k >= k_low && bits; k--) {
+    const uint32_t x = (uint32_t)plane(k);
+    const uint32_t bl = 32 - clz32(x);      // bit length of the plane
+    const bool full = n == (uint32_t)BS;
+    const bool any = bl > n;                // a one above the frontier
+    if (any && bl >= (uint32_t)BS) {        // a one in the last position is implied
+      encode_plane<BS>(x, n, bits, w);
+      continue;
+    }
+    const uint32_t xh = full ? 0u : x >> n;
+    const uint32_t hb = bl - 1 - n;
+    const uint32_t m = popcount32(xh);
+    const uint32_t S = rank_spread32(xh);
+    const uint64_t grp =
+        any ? (1 | ((uint64_t)S << 1) | ((uint64_t)(S - (1u << ((hb + m - 1) & 31))) << 2)) : 0;
+    const uint32_t hlen = full ? (uint32_t)BS : n;
+    const uint32_t head = full ? x : x & ((1u << n) - 1);
+    const uint32_t glen = full ? 0 : any ? hb + m + 2 : 1;
+    n = any ? bl : n;
+    const uint32_t len = hlen + glen;
+    const uint32_t l = len < bits ? len : bits;
+    w.put(((uint64_t)head | (grp << hlen)) & lowmask64(l), l);
+    bits -= l;
+  }
+  return k;
+}
+
 // Code planes k, k-1, ... down to k_low while budget remains; plane(k)
 // yields plane k.  Returns the index of the next plane.  A plane's code is
 // written as two pieces -- its n verbatim bits, then its group tests (at
@@ -452,6 +514,7 @@ GZ_HD uint64_t rank_spread(uint64_t z) {
 // truncates its code, as the bit-serial coder does.
 template <int BS, class W, class PlaneFn>
 GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, PlaneFn&& plane) {
+  if constexpr (BS <= 16) return code_planes_small<BS>(k, k_low, n, bits, w, plane);
   // The frontier after a plane is max(n, bit length of the plane), so the
   // chain from one plane to the next is a single max; the rest of a plane's
   // code depends on n but not on the previous plane's code.
@@ -474,12 +537,72 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
     const uint64_t head = full ? x : x & ((1ull << sh) - 1);
     const uint32_t glen = full ? 0 : any ? hb + m + 2 : 1;
     n = any ? bl : n;
-    uint32_t l = hlen < bits ? hlen : bits;
-    w.put(head & lowmask64(l), l);
-    bits -= l;
-    l = glen < bits ? glen : bits;
-    w.put(grp & lowmask64(l), l);
-    bits -= l;
+    if (hlen + glen <= 64) {  // both pieces in one word (most planes)
+      const uint32_t len = hlen + glen;
+      const uint64_t code = head | (glen ? grp << (hlen & 63) : 0);
+      const uint32_t l = len < bits ? len : bits;
+      w.put(code & lowmask64(l), l);
+      bits -= l;
+    } else {
+      uint32_t l = hlen < bits ? hlen : bits;
+      w.put(head & lowmask64(l), l);
+      bits -= l;
+      l = glen < bits ? glen : bits;
+      w.put(grp & lowmask64(l), l);
+      bits -= l;
+    }
+  }
+  return k;
+}
+
+// uncode_planes for blocks of at most 16 values: the verbatim bits and the
+// group tests of a plane (at most 16 + 33 bits) come from one 64-bit window.
+// Same bits as the general form below.
+template <int BS, class R, class StoreFn>
+GZ_HD int uncode_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
+                              StoreFn&& store) {
+  static_assert(BS <= 16, "at most 16 values per block");
+  for (; k >= k_low && bits; k--) {
+    const bool full = n == (uint32_t)BS;
+    const uint32_t hlen = full ? (uint32_t)BS : n;
+    if (hlen > bits) {  // the budget ends inside the verbatim bits
+      store(k, decode_plane<BS>(n, bits, r));
+      continue;
+    }
+    const uint64_t w = r.peek64();
+    uint32_t x = (uint32_t)w & ((1u << hlen) - 1);
+    if (full || bits == hlen) {
+      r.skip(hlen);
+      bits -= hlen;
+      store(k, x);
+      continue;
+    }
+    const bool test = (w >> hlen) & 1;
+    uint64_t g = (w >> hlen) >> 1;
+    uint32_t used = hlen + 1, pos = n;  // bits of the window taken so far
+    bool ok = true;
+    bool more = test;
+    while (more && ok) {  // runs once per one of the plane
+      const uint32_t t = ctz64(g);
+      ok = pos + t < (uint32_t)BS - 1 && used + t + 2 <= 64 && used + t + 2 <= bits;
+      if (ok) {
+        x |= 1u << (pos + t);
+        more = (g >> (t + 1)) & 1;
+        g = (g >> (t + 1)) >> 1;
+        used += t + 2;
+        pos += t + 1;
+      }
+    }
+    if (ok) {
+      r.skip(used);
+      bits -= used;
+      n = test ? pos : n;
+      store(k, x);
+    } else {
+      r.skip(hlen);
+      bits -= hlen;
+      store(k, decode_group<BS>(x, n, bits, r));  // group tests not consumed yet
+    }
   }
   return k;
 }
@@ -492,6 +615,7 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
 // the general routine decodes the group tests.
 template <int BS, class R, class StoreFn>
 GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
+  if constexpr (BS <= 16) return uncode_planes_small<BS>(k, k_low, n, bits, r, store);
   for (; k >= k_low && bits; k--) {
     const bool full = n == (uint32_t)BS;
     const uint32_t hlen = full ? (uint32_t)BS : n;
