@@ -659,6 +659,147 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
   return k;
 }
 
+// ------------------------------------------------------ 4-value blocks
+// In a 1D block of smooth data the first coefficient is often the only
+// significant one for many planes: each such plane is that coefficient's
+// bit and a 0 test bit, and a run of them is the coefficient's bit segment
+// (plane k first) spread to every other bit.  Runs at frontier 0 (all-zero
+// planes, one 0 bit each) and 1 are coded and decoded whole; the other
+// planes go one at a time through the small-block coder.
+
+// bit i of x (below 2^32) to bit 2i
+GZ_HD uint64_t spread2(uint64_t x) {
+  x &= 0xffffffffull;
+  x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+  x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+  x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  return (x | (x << 1)) & 0x5555555555555555ull;
+}
+// inverse: bit 2i of x to bit i (odd bits ignored)
+GZ_HD uint64_t compact2(uint64_t x) {
+  x &= 0x5555555555555555ull;
+  x = (x | (x >> 1)) & 0x3333333333333333ull;
+  x = (x | (x >> 2)) & 0x0f0f0f0f0f0f0f0full;
+  x = (x | (x >> 4)) & 0x00ff00ff00ff00ffull;
+  x = (x | (x >> 8)) & 0x0000ffff0000ffffull;
+  return (x | (x >> 16)) & 0x00000000ffffffffull;
+}
+GZ_HD uint32_t brev_u(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __brev(x);
+#else
+  x = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+  x = ((x >> 2) & 0x33333333u) | ((x & 0x33333333u) << 2);
+  x = ((x >> 4) & 0x0f0f0f0fu) | ((x & 0x0f0f0f0fu) << 4);
+  x = ((x >> 8) & 0x00ff00ffu) | ((x & 0x00ff00ffu) << 8);
+  return (x >> 16) | (x << 16);
+#endif
+}
+GZ_HD uint64_t brev_u(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __brevll(x);
+#else
+  return ((uint64_t)brev_u((uint32_t)x) << 32) | brev_u((uint32_t)(x >> 32));
+#endif
+}
+
+// plane k of four coefficients
+template <typename UInt>
+GZ_HD uint64_t plane4(const UInt* u, int k) {
+  return (uint64_t)(((u[0] >> k) & 1u) | (((u[1] >> k) & 1u) << 1) | (((u[2] >> k) & 1u) << 2) |
+                    (((u[3] >> k) & 1u) << 3));
+}
+
+// Code the planes of a 4-value block from plane k down to k_low
+// (coefficients u, frontier n, budget bits): the same bits as
+// code_planes<4>.
+template <typename UInt, class W>
+GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w) {
+  constexpr int P = 8 * sizeof(UInt);
+  while (k >= k_low && bits) {
+    if (n >= 2) {  // the rest plane by plane
+      code_planes_small<4>(k, k_low, n, bits, w, [&](int kk) { return plane4(u, kk); });
+      return;
+    }
+    // the highest plane at or below k with a one at a position >= n (no
+    // such one sits above k, or n would be larger)
+    const UInt hi = (n <= 0 ? u[0] : 0) | (n <= 1 ? u[1] : 0) | (n <= 2 ? u[2] : 0) |
+                    (n <= 3 ? u[3] : 0);
+    const int kstop = hi ? P - 1 - (int)(sizeof(UInt) == 8 ? clz64((uint64_t)hi)
+                                                           : clz32((uint32_t)hi))
+                         : -1;
+    const int lo = kstop > k_low - 1 ? kstop : k_low - 1;
+    if (k > lo) {  // planes k .. lo + 1: a run (n is 0 or 1)
+      const uint32_t gw = n + 1;
+      const uint32_t cmax = 64 / gw;
+      uint32_t r = (uint32_t)(k - lo);
+      while (r && bits) {
+        const uint32_t c = r < cmax ? r : cmax;
+        const uint64_t seg = (uint64_t)(brev_u(u[0]) >> (P - 1 - k)) & lowmask64(c);
+        const uint64_t code = n ? spread2(seg) : 0;
+        const uint32_t len = c * gw;
+        const uint32_t l = len < bits ? len : bits;
+        w.put(code & lowmask64(l), l);
+        bits -= l;
+        k -= (int)c;
+        r -= c;
+      }
+      continue;  // k == lo, or the budget is spent
+    }
+    // plane k brings a new coefficient
+    k = code_planes_small<4>(k, k, n, bits, w, [&](int kk) { return plane4(u, kk); });
+  }
+}
+
+// Decode the planes of a 4-value block from plane k down to k_low into the
+// coefficients u (zeroed by the caller): the same bits as uncode_planes<4>.
+template <typename UInt, class R>
+GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r) {
+  constexpr int P = 8 * sizeof(UInt);
+  auto deposit = [&](int kk, uint64_t x) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) u[i] |= (UInt)((x >> i) & 1u) << kk;
+  };
+  // with a budget this small the runs are too short to pay for themselves
+  if (bits < 32) {
+    uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
+    return;
+  }
+  while (k >= k_low && bits) {
+    if (n >= 2) {  // the rest plane by plane
+      uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
+      return;
+    }
+    const uint32_t gw = n + 1;
+    // whole planes that fit the window, the budget and the planes left
+    uint32_t c = 64 / gw;
+    if ((uint32_t)(k - k_low + 1) < c) c = (uint32_t)(k - k_low + 1);
+    if (bits / gw < c) c = bits / gw;
+    uint32_t rr = 0;
+    uint64_t win = 0;
+    if (c) {  // the run ends at the first test bit that is 1
+      win = r.peek64();
+      const uint64_t tests = (n ? 0xaaaaaaaaaaaaaaaaull : ~0ull) & lowmask64(c * gw);
+      const uint64_t hit = win & tests;
+      rr = hit ? (uint32_t)popcount64(tests & lowmask64(ctz64(hit))) : c;
+    }
+    if (rr) {  // rr planes of verbatim bits and 0 tests
+      if (n) {
+        // bit j of seg is bit k - j of the coefficient
+        const uint64_t seg = compact2(win) & lowmask64(rr);
+        u[0] |= brev_u((UInt)seg) >> (P - 1 - k);
+      }
+      r.skip(rr * gw);
+      bits -= rr * gw;
+      k -= (int)rr;
+      continue;
+    }
+    // plane k brings a new coefficient, or the budget ends inside it
+    k = uncode_planes_small<4>(k, k, n, bits, r, deposit);
+  }
+}
+
 // --------------------------------------------------------- float <-> bits
 
 GZ_HD float bits_f32(uint32_t b) {
@@ -1024,6 +1165,8 @@ GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mo
   } else if constexpr (BS == 64) {
     planes_to_store<0>(u, ps);
     code_planes<BS>(k, kmin, n, bits, w, [&](int kk) { return ps.get(kk); });
+  } else if constexpr (D == 1) {
+    code_planes_1d(u, k, kmin, n, bits, w);
   } else {
     PL pl;
 #pragma unroll
@@ -1112,6 +1255,10 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
       k = uncode_planes<BS>(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
       store_to_coeffs<0>(ps, 0, k, top, u);
     }
+  } else if constexpr (D == 1) {
+#pragma unroll
+    for (int i = 0; i < BS; i++) u[i] = 0;
+    uncode_planes_1d(u, k, kmin, n, bits, r);
   } else {
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, 0);
