@@ -711,32 +711,31 @@ GZ_HD uint64_t plane4(const UInt* u, int k) {
                     (((u[3] >> k) & 1u) << 3));
 }
 
-// Code the planes of a 4-value block from plane k down to k_low
-// (coefficients u, frontier n, budget bits): the same bits as
-// code_planes<4>.
-template <typename UInt, class W>
-GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w) {
+// Code planes k, k-1, ... of a block of at most 16 values while the
+// frontier is 0 or 1, in runs: u0 is the first coefficient, above0 / above1
+// the OR of the coefficients at positions >= 0 / >= 1 (a plane brings a new
+// coefficient at the highest set bit among those at or above the
+// frontier), plane(k) a plane for the planes that bring one.  Returns the
+// next plane; the same bits as code_planes<BS>.
+template <int BS, typename UInt, class W, class PlaneFn>
+GZ_HD int code_runs01(UInt u0, UInt above0, UInt above1, int k, int k_low, uint32_t& n,
+                      uint32_t& bits, W& w, PlaneFn&& plane) {
   constexpr int P = 8 * sizeof(UInt);
-  while (k >= k_low && bits) {
-    if (n >= 2) {  // the rest plane by plane
-      code_planes_small<4>(k, k_low, n, bits, w, [&](int kk) { return plane4(u, kk); });
-      return;
-    }
+  while (k >= k_low && bits && n <= 1) {
     // the highest plane at or below k with a one at a position >= n (no
     // such one sits above k, or n would be larger)
-    const UInt hi = (n <= 0 ? u[0] : 0) | (n <= 1 ? u[1] : 0) | (n <= 2 ? u[2] : 0) |
-                    (n <= 3 ? u[3] : 0);
+    const UInt hi = n ? above1 : above0;
     const int kstop = hi ? P - 1 - (int)(sizeof(UInt) == 8 ? clz64((uint64_t)hi)
                                                            : clz32((uint32_t)hi))
                          : -1;
     const int lo = kstop > k_low - 1 ? kstop : k_low - 1;
-    if (k > lo) {  // planes k .. lo + 1: a run (n is 0 or 1)
+    if (k > lo) {  // planes k .. lo + 1: a run
       const uint32_t gw = n + 1;
       const uint32_t cmax = 64 / gw;
       uint32_t r = (uint32_t)(k - lo);
       while (r && bits) {
         const uint32_t c = r < cmax ? r : cmax;
-        const uint64_t seg = (uint64_t)(brev_u(u[0]) >> (P - 1 - k)) & lowmask64(c);
+        const uint64_t seg = (uint64_t)(brev_u(u0) >> (P - 1 - k)) & lowmask64(c);
         const uint64_t code = n ? spread2(seg) : 0;
         const uint32_t len = c * gw;
         const uint32_t l = len < bits ? len : bits;
@@ -748,29 +747,22 @@ GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t
       continue;  // k == lo, or the budget is spent
     }
     // plane k brings a new coefficient
-    k = code_planes_small<4>(k, k, n, bits, w, [&](int kk) { return plane4(u, kk); });
+    k = code_planes_small<BS>(k, k, n, bits, w, plane);
   }
+  return k;
 }
 
-// Decode the planes of a 4-value block from plane k down to k_low into the
-// coefficients u (zeroed by the caller): the same bits as uncode_planes<4>.
-template <typename UInt, class R>
-GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r) {
+// Decode planes k, k-1, ... of a block of at most 16 values while the
+// frontier is 0 or 1: runs add their bits of the first coefficient to u0,
+// the planes that bring a new coefficient go to store(k, x).  Returns the
+// next plane; the same bits as uncode_planes<BS>.
+template <int BS, typename UInt, class R, class StoreFn>
+GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
+                        StoreFn&& store) {
   constexpr int P = 8 * sizeof(UInt);
-  auto deposit = [&](int kk, uint64_t x) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) u[i] |= (UInt)((x >> i) & 1u) << kk;
-  };
   // with a budget this small the runs are too short to pay for themselves
-  if (bits < 32) {
-    uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
-    return;
-  }
-  while (k >= k_low && bits) {
-    if (n >= 2) {  // the rest plane by plane
-      uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
-      return;
-    }
+  if (bits < 32) return k;
+  while (k >= k_low && bits && n <= 1) {
     const uint32_t gw = n + 1;
     // whole planes that fit the window, the budget and the planes left
     uint32_t c = 64 / gw;
@@ -788,7 +780,7 @@ GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bi
       if (n) {
         // bit j of seg is bit k - j of the coefficient
         const uint64_t seg = compact2(win) & lowmask64(rr);
-        u[0] |= brev_u((UInt)seg) >> (P - 1 - k);
+        u0 |= brev_u((UInt)seg) >> (P - 1 - k);
       }
       r.skip(rr * gw);
       bits -= rr * gw;
@@ -796,8 +788,28 @@ GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bi
       continue;
     }
     // plane k brings a new coefficient, or the budget ends inside it
-    k = uncode_planes_small<4>(k, k, n, bits, r, deposit);
+    k = uncode_planes_small<BS>(k, k, n, bits, r, store);
   }
+  return k;
+}
+
+// 4-value blocks: the runs, then the rest plane by plane.
+template <typename UInt, class W>
+GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w) {
+  auto plane = [&](int kk) { return plane4(u, kk); };
+  const UInt above1 = u[1] | u[2] | u[3];
+  k = code_runs01<4>(u[0], (UInt)(u[0] | above1), above1, k, k_low, n, bits, w, plane);
+  if (k >= k_low && bits) code_planes_small<4>(k, k_low, n, bits, w, plane);
+}
+
+template <typename UInt, class R>
+GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r) {
+  auto deposit = [&](int kk, uint64_t x) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) u[i] |= (UInt)((x >> i) & 1u) << kk;
+  };
+  k = uncode_runs01<4>(u[0], k, k_low, n, bits, r, deposit);
+  if (k >= k_low && bits) uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
 }
 
 // --------------------------------------------------------- float <-> bits
@@ -1176,11 +1188,20 @@ GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mo
     }
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, pl.tw[i]);
-    code_planes<BS>(k, kmin, n, bits, w, [&](int kp) {
+    auto plane = [&](int kp) {
       const int G = kp >> 5, kk = kp & 31, r = kk % PL::N, g = kk / PL::N;
       const uint32_t word = (uint32_t)ps.get(G * BS + r);
       return (uint64_t)((word >> (g * PL::N)) & ((1u << PL::N) - 1));
-    });
+    };
+    // runs while the first coefficient alone is significant (for 2D blocks
+    // of 64-bit values they measured slower than plane by plane)
+    if constexpr (BS <= 16 && P == 32) {
+      UInt above1 = 0;
+#pragma unroll
+      for (int i = 1; i < BS; i++) above1 |= u[i];
+      k = code_runs01<BS>(u[0], (UInt)(u[0] | above1), above1, k, kmin, n, bits, w, plane);
+    }
+    if (k >= kmin && bits) code_planes<BS>(k, kmin, n, bits, w, plane);
   }
   if constexpr (!Mode::kGeneral) {
     w.zeros(bits);  // pad to exactly maxbits
@@ -1262,16 +1283,20 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
   } else {
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, 0);
-    uncode_planes<BS>(k, kmin, n, bits, r, [&](int kp, uint64_t x) {
+    auto store = [&](int kp, uint64_t x) {
       const int G = kp >> 5, kk = kp & 31, rr = kk % PL::N, g = kk / PL::N;
       ps.put(G * BS + rr, ps.get(G * BS + rr) | (x << (g * PL::N)));
-    });
+    };
+    UInt u0 = 0;  // the runs' bits of the first coefficient
+    if constexpr (BS <= 16 && P == 32) k = uncode_runs01<BS>(u0, k, kmin, n, bits, r, store);
+    if (k >= kmin && bits) uncode_planes<BS>(k, kmin, n, bits, r, store);
     PL pl;
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) pl.tw[i] = (uint32_t)ps.get(i);
 #pragma unroll
     for (int G = 0; G < P / 32; G++) pl.transpose(G);
     pl.store(u);
+    u[0] |= u0;
   }
 
   Int q[BS];
