@@ -473,11 +473,12 @@ GZ_HD uint32_t rank_spread32(uint32_t z) {
 // most 16 bits and its whole code -- verbatim bits, then group tests -- at
 // most 16 + 33 bits, so it is built in 32-bit arithmetic and written in one
 // piece.  Same bits as the general form below.
-template <int BS, class W, class PlaneFn>
+template <int BS, bool STOP_FULL = false, class W, class PlaneFn>
 GZ_HD int code_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, W& w,
                             PlaneFn&& plane) {
   static_assert(BS <= 16, "at most 16 values per block");
-  for (; k >= k_low && bits; k--) {
+  // STOP_FULL: return as soon as every coefficient is significant
+  for (; k >= k_low && bits && !(STOP_FULL && n == (uint32_t)BS); k--) {
     const uint32_t x = (uint32_t)plane(k);
     const uint32_t bl = 32 - clz32(x);      // bit length of the plane
     const bool full = n == (uint32_t)BS;
@@ -558,11 +559,11 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
 // uncode_planes for blocks of at most 16 values: the verbatim bits and the
 // group tests of a plane (at most 16 + 33 bits) come from one 64-bit window.
 // Same bits as the general form below.
-template <int BS, class R, class StoreFn>
+template <int BS, bool STOP_FULL = false, class R, class StoreFn>
 GZ_HD int uncode_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
                               StoreFn&& store) {
   static_assert(BS <= 16, "at most 16 values per block");
-  for (; k >= k_low && bits; k--) {
+  for (; k >= k_low && bits && !(STOP_FULL && n == (uint32_t)BS); k--) {
     const bool full = n == (uint32_t)BS;
     const uint32_t hlen = full ? (uint32_t)BS : n;
     if (hlen > bits) {  // the budget ends inside the verbatim bits
@@ -675,6 +676,22 @@ GZ_HD uint64_t spread2(uint64_t x) {
   x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
   x = (x | (x << 2)) & 0x3333333333333333ull;
   return (x | (x << 1)) & 0x5555555555555555ull;
+}
+// bit i of x (below 2^16) to bit 4i
+GZ_HD uint64_t spread4(uint64_t x) {
+  x &= 0xffffull;
+  x = (x | (x << 24)) & 0x000000ff000000ffull;
+  x = (x | (x << 12)) & 0x000f000f000f000full;
+  x = (x | (x << 6)) & 0x0303030303030303ull;
+  return (x | (x << 3)) & 0x1111111111111111ull;
+}
+// inverse: bit 4i of x to bit i (other bits ignored)
+GZ_HD uint64_t compact4(uint64_t x) {
+  x &= 0x1111111111111111ull;
+  x = (x | (x >> 3)) & 0x0303030303030303ull;
+  x = (x | (x >> 6)) & 0x000f000f000f000full;
+  x = (x | (x >> 12)) & 0x000000ff000000ffull;
+  return (x | (x >> 24)) & 0x000000000000ffffull;
 }
 // inverse: bit 2i of x to bit i (odd bits ignored)
 GZ_HD uint64_t compact2(uint64_t x) {
@@ -793,23 +810,65 @@ GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits,
   return k;
 }
 
-// 4-value blocks: the runs, then the rest plane by plane.
+// 4-value blocks: runs at frontier 0 and 1, planes one at a time until all
+// four coefficients are significant, then runs of 4-bit planes (the four
+// bit segments interleaved, 16 planes a word).
 template <typename UInt, class W>
 GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w) {
+  constexpr int P = 8 * sizeof(UInt);
   auto plane = [&](int kk) { return plane4(u, kk); };
   const UInt above1 = u[1] | u[2] | u[3];
+  // (budgets under 64 bits seldom reach the all-significant planes: those
+  // blocks stay plane by plane, which measured faster for them)
+  const bool full_runs = bits >= 64;
   k = code_runs01<4>(u[0], (UInt)(u[0] | above1), above1, k, k_low, n, bits, w, plane);
-  if (k >= k_low && bits) code_planes_small<4>(k, k_low, n, bits, w, plane);
+  if (!full_runs) {
+    if (k >= k_low && bits) code_planes_small<4>(k, k_low, n, bits, w, plane);
+    return;
+  }
+  if (k >= k_low && bits) k = code_planes_small<4, true>(k, k_low, n, bits, w, plane);
+  while (k >= k_low && bits) {  // n == 4
+    const uint32_t c = (uint32_t)(k - k_low + 1) < 16 ? (uint32_t)(k - k_low + 1) : 16;
+    uint64_t code = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+      code |= spread4((uint64_t)(brev_u(u[i]) >> (P - 1 - k)) & lowmask64(c)) << i;
+    const uint32_t l = 4 * c < bits ? 4 * c : bits;
+    w.put(code & lowmask64(l), l);
+    bits -= l;
+    k -= (int)c;
+  }
 }
 
 template <typename UInt, class R>
 GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r) {
+  constexpr int P = 8 * sizeof(UInt);
   auto deposit = [&](int kk, uint64_t x) {
 #pragma unroll
     for (int i = 0; i < 4; i++) u[i] |= (UInt)((x >> i) & 1u) << kk;
   };
+  const bool full_runs = bits >= 64;  // as in code_planes_1d
   k = uncode_runs01<4>(u[0], k, k_low, n, bits, r, deposit);
-  if (k >= k_low && bits) uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
+  if (!full_runs) {
+    if (k >= k_low && bits) uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
+    return;
+  }
+  if (k >= k_low && bits) k = uncode_planes_small<4, true>(k, k_low, n, bits, r, deposit);
+  while (k >= k_low && bits) {  // n == 4: whole 4-bit planes, then the last partial one
+    uint32_t c = (uint32_t)(k - k_low + 1) < 16 ? (uint32_t)(k - k_low + 1) : 16;
+    if (bits / 4 < c) c = bits / 4;
+    if (!c) {
+      uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
+      return;
+    }
+    const uint64_t win = r.peek64();
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+      u[i] |= brev_u((UInt)(compact4(win >> i) & lowmask64(c))) >> (P - 1 - k);
+    r.skip(4 * c);
+    bits -= 4 * c;
+    k -= (int)c;
+  }
 }
 
 // --------------------------------------------------------- float <-> bits
