@@ -43,6 +43,7 @@ int bcuda(cudaError_t e, const char* what) {
 }
 
 constexpr int kMaxBatchItems = 65535;
+constexpr int kMaxCtasPerSm = 16;  // the largest gzfp_batch_config::ctas_per_sm
 
 }  // namespace
 
@@ -51,15 +52,8 @@ namespace bhost {
 
 bool valid_config(const gzfp_batch_config& c) {
   return (c.threads == 64 || c.threads == 128 || c.threads == 256) && c.ctas_per_sm >= 1 &&
-         c.ctas_per_sm <= 16 && (c.blocks_per_thread == 1 || c.blocks_per_thread == 2 ||
+         c.ctas_per_sm <= kMaxCtasPerSm && (c.blocks_per_thread == 1 || c.blocks_per_thread == 2 ||
                                  c.blocks_per_thread == 4);
-}
-
-int occupancy(int threads, bool decode, uint32_t staged_w) {
-  // the largest over the kinds: a shape's CTAs per SM are capped per kind
-  int best = 0;
-  for (int k = 0; k < kBatchKinds; k++) best = std::max(best, batch_occupancy(threads, decode, k, staged_w));
-  return best;
 }
 
 int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
@@ -188,7 +182,6 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
 
 namespace {
 
-using gzfp::bhost::occupancy;
 using gzfp::bhost::Prepared;
 using gzfp::bhost::valid_config;
 using gzfp::bhost::WorkList;
@@ -335,9 +328,20 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
     for (int i = 0; i < count; i++)
       if (items[i].maxbits % 64 == 0 && items[i].maxbits / 64 <= gzfp::kBatchMaxStagedWords)
         sw = std::max(sw, items[i].maxbits / 64);
+  // the kinds present: their occupancy bounds the CTAs per SM worth trying
+  bool present[gzfp::kBatchKinds] = {};
+  if (items)
+    for (int i = 0; i < count; i++)
+      if (gzfp::batch_type_ok(items[i].type)) {
+        const int dims = items[i].nz ? 3 : items[i].ny ? 2 : 1;
+        present[gzfp::batch_kind_index(gzfp::batch_kind(items[i].type, dims))] = true;
+      }
   // every candidate is timed as it is meant to run: a graph replay
   for (int nt : threads) {
-    const int occ = std::max(1, occupancy(nt, decompress != 0, sw));
+    int occ = 1;
+    for (int k = 0; k < gzfp::kBatchKinds; k++)
+      if (present[k]) occ = std::max(occ, gzfp::batch_occupancy(nt, decompress != 0, k, sw));
+    occ = std::min(occ, kMaxCtasPerSm);
     for (int per_sm = 1; per_sm <= occ && !st; per_sm++) {
       for (int bpt : bpts) {
         for (int ahead = 0; ahead < 2 && !st; ahead++) {

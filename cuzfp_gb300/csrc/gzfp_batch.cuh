@@ -95,10 +95,10 @@ struct BatchMinBlocks {
   static constexpr int value = v < 1 ? 1 : v;
 };
 
-// plane-store slots per thread: as the plain encoder, 32 when decoding
+// plane-store slots per thread: as the plain kernels
 template <bool DECODE, int D, typename T>
 struct BatchSlots {
-  static constexpr int value = DECODE ? 32 : ((D == 3 && sizeof(T) == 8) ? 64 : 32);
+  static constexpr int value = DECODE ? decode_slots<D, T>() : store_slots<D, T>();
 };
 
 // Persistent kernel for one kind: chunks [lo, hi) of the work list.  NT

@@ -37,10 +37,6 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
 
 bool valid_config(const gzfp_batch_config& c);
 
-// Resident CTAs per SM of the batch kernels at `threads` per CTA (the
-// largest over the kinds).
-int occupancy(int threads, bool decode, uint32_t staged_w);
-
 // Device work list of one batch in flight: descriptors, chunk table and
 // one claim counter per kind, a pinned host copy of the descriptors, and an event
 // recorded after the batch's kernel so that the next user of the list can

@@ -105,7 +105,7 @@ cudaError_t launch_decode_blocks_t(const uint64_t* in, uint64_t nwords,
                                    uint64_t count, uint32_t maxbits, T* tiles, cudaStream_t s) {
   if (count == 0) return cudaSuccess;
   const dim3 grid((unsigned)((count + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(32, false, 0);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0);
   auto k = decode_blocks_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;

@@ -97,11 +97,19 @@ struct MinBlocks {
   static constexpr int value = (D == 3 && sizeof(T) == 8) ? 3 : 4;
 };
 
-// plane-store slots per thread: 64 for 4^3 double blocks (two 32-plane
-// halves' worth), 32 otherwise
+// Plane-store slots per thread, as many as the block codec touches, so that
+// shared memory does not cap the CTAs per SM below what registers allow:
+// 4^3 blocks of 64-bit values encode through two 32-plane halves (64 slots)
+// and decode one half at a time (32); other 4^3 blocks use 32; 2D blocks
+// hold their transposed words (16 per 32 bits of value); 1D blocks keep
+// their planes in registers (none).
 template <int D, typename T>
-constexpr int store_slots() {
-  return (D == 3 && sizeof(T) == 8) ? 64 : 32;
+__host__ __device__ constexpr int store_slots() {
+  return D == 1 ? 0 : D == 2 ? 16 * (int)(sizeof(T) / 4) : (sizeof(T) == 8 ? 64 : 32);
+}
+template <int D, typename T>
+__host__ __device__ constexpr int decode_slots() {
+  return D == 3 ? 32 : store_slots<D, T>();
 }
 
 template <int D, typename T>
@@ -127,7 +135,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (STAGED) {
     const uint32_t W = maxbits >> 6;
-    uint64_t* buf = smem + 32 * kThreads;
+    uint64_t* buf = smem + decode_slots<D, T>() * kThreads;
     const uint64_t b0 = b - (threadIdx.x & 31);
     if (b0 < g.nblocks) {
       const uint64_t left = g.nblocks - b0;
@@ -166,7 +174,7 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords && g.base == 0;
-  const size_t sm = smem_bytes(32, staged, maxbits >> 6);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), staged, maxbits >> 6);
   constexpr int MB = MinBlocks<D, T>::value;
   auto k = !staged ? decode_kernel<D, T, false, MB>
            : (MB < 4 && sm <= kSmemFor4) ? decode_kernel<D, T, true, 4>

@@ -113,7 +113,7 @@ cudaError_t launch_decode_mode_t(const uint64_t* in, uint64_t nwords,
                                  const General& mode, T* out, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(32, false, 0);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0);
   auto k = decode_mode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
