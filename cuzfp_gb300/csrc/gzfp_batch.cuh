@@ -48,6 +48,7 @@ inline int batch_kind_index(uint32_t kind) {
 template <int NT>
 struct BatchPlanes {
   uint64_t* p;
+  const Plane4Tables* t4;  // the CTA's plane tables (1D kinds)
   __device__ __forceinline__ uint64_t get(int i) const { return p[i * NT]; }
   __device__ __forceinline__ void put(int i, uint64_t v) { p[i * NT] = v; }
 };
@@ -113,8 +114,9 @@ __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
   extern __shared__ uint64_t smem[];
   __shared__ unsigned long long s_claim;
   __shared__ BatchDesc s_desc;  // the claimed chunk's array, read field by field
-  BatchPlanes<NT> ps{smem + threadIdx.x};
-  uint64_t* sbuf = smem + BatchSlots<DECODE, D, T>::value * NT;
+  const Plane4Tables* t4 = stage_tables<D, NT>(smem);
+  BatchPlanes<NT> ps{smem + table_words<D>() + threadIdx.x, t4};
+  uint64_t* sbuf = smem + table_words<D>() + BatchSlots<DECODE, D, T>::value * NT;
   if (threadIdx.x == 0) s_claim = lo + atomicAdd(counter, 1ull);
   __syncthreads();
   for (;;) {
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
 // decoding the staged word buffer (staged_w words per block at pitch NT + 1)
 template <int NT, bool DECODE, int D, typename T>
 size_t batch_smem_bytes(uint32_t staged_w) {
-  return (size_t)NT * BatchSlots<DECODE, D, T>::value * 8 +
+  return ((size_t)NT * BatchSlots<DECODE, D, T>::value + (size_t)table_words<D>()) * 8 +
          (DECODE ? (size_t)staged_w * (NT + 1) * 8 : 0);
 }
 

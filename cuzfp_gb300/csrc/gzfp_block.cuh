@@ -25,8 +25,10 @@
 
 #if defined(__CUDACC__)
 #define GZ_HD __host__ __device__ __forceinline__
+#define GZ_CX __host__ __device__ constexpr
 #else
 #define GZ_HD inline
+#define GZ_CX constexpr
 #endif
 
 namespace gzfp {
@@ -660,13 +662,14 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
   return k;
 }
 
-// ------------------------------------------------------ 4-value blocks
-// In a 1D block of smooth data the first coefficient is often the only
+// ------------------------------------------------- runs at frontier 0 and 1
+// In a block of smooth data the first coefficient is often the only
 // significant one for many planes: each such plane is that coefficient's
 // bit and a 0 test bit, and a run of them is the coefficient's bit segment
 // (plane k first) spread to every other bit.  Runs at frontier 0 (all-zero
 // planes, one 0 bit each) and 1 are coded and decoded whole; the other
-// planes go one at a time through the small-block coder.
+// planes go one at a time through the small-block coder.  (Used for 2D
+// blocks of 32-bit values; 4-value blocks use the plane tables below.)
 
 // bit i of x (below 2^32) to bit 2i
 GZ_HD uint64_t spread2(uint64_t x) {
@@ -676,22 +679,6 @@ GZ_HD uint64_t spread2(uint64_t x) {
   x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
   x = (x | (x << 2)) & 0x3333333333333333ull;
   return (x | (x << 1)) & 0x5555555555555555ull;
-}
-// bit i of x (below 2^16) to bit 4i
-GZ_HD uint64_t spread4(uint64_t x) {
-  x &= 0xffffull;
-  x = (x | (x << 24)) & 0x000000ff000000ffull;
-  x = (x | (x << 12)) & 0x000f000f000f000full;
-  x = (x | (x << 6)) & 0x0303030303030303ull;
-  return (x | (x << 3)) & 0x1111111111111111ull;
-}
-// inverse: bit 4i of x to bit i (other bits ignored)
-GZ_HD uint64_t compact4(uint64_t x) {
-  x &= 0x1111111111111111ull;
-  x = (x | (x >> 3)) & 0x0303030303030303ull;
-  x = (x | (x >> 6)) & 0x000f000f000f000full;
-  x = (x | (x >> 12)) & 0x000000ff000000ffull;
-  return (x | (x >> 24)) & 0x000000000000ffffull;
 }
 // inverse: bit 2i of x to bit i (odd bits ignored)
 GZ_HD uint64_t compact2(uint64_t x) {
@@ -721,12 +708,6 @@ GZ_HD uint64_t brev_u(uint64_t x) {
 #endif
 }
 
-// plane k of four coefficients
-template <typename UInt>
-GZ_HD uint64_t plane4(const UInt* u, int k) {
-  return (uint64_t)(((u[0] >> k) & 1u) | (((u[1] >> k) & 1u) << 1) | (((u[2] >> k) & 1u) << 2) |
-                    (((u[3] >> k) & 1u) << 3));
-}
 
 // Code planes k, k-1, ... of a block of at most 16 values while the
 // frontier is 0 or 1, in runs: u0 is the first coefficient, above0 / above1
@@ -810,65 +791,189 @@ GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits,
   return k;
 }
 
-// 4-value blocks: runs at frontier 0 and 1, planes one at a time until all
-// four coefficients are significant, then runs of 4-bit planes (the four
-// bit segments interleaved, 16 planes a word).
-template <typename UInt, class W>
-GZ_HD void code_planes_1d(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w) {
-  constexpr int P = 8 * sizeof(UInt);
-  auto plane = [&](int kk) { return plane4(u, kk); };
-  const UInt above1 = u[1] | u[2] | u[3];
-  // (budgets under 64 bits seldom reach the all-significant planes: those
-  // blocks stay plane by plane, which measured faster for them)
-  const bool full_runs = bits >= 64;
-  k = code_runs01<4>(u[0], (UInt)(u[0] | above1), above1, k, k_low, n, bits, w, plane);
-  if (!full_runs) {
-    if (k >= k_low && bits) code_planes_small<4>(k, k_low, n, bits, w, plane);
-    return;
+// ------------------------------------------------------ 4-value blocks
+// A plane of a 4-value block has 4 bits, and with the frontier n (0..4)
+// they alone determine the plane's code in encode_ints
+// (Z/src/template/encode.c:122-151): n verbatim bits, then the group tests,
+// at most 7 bits in all.  Decoding a plane (decode_ints, Z/src/template/
+// decode.c:73-105) reads at most 7 bits and depends only on n, those bits
+// and how many of them the budget still allows.  So both directions are
+// table lookups with no data-dependent branch: the encoder codes two planes
+// per lookup, the decoder one.  A budget that ends inside a plane cuts the
+// encoder's output there, as the bit-serial coder stops there; for the
+// decoder the budget is part of the index, and zfp's rule that a run cut
+// off by the budget still deposits a one is in the table.
+
+struct Plane4Tables {
+  // planes k and k - 1: index n * 256 + x_k + 16 * x_{k-1}; entry = both
+  // codes (14 bits, plane k's first) | plane k's code length << 14 | both
+  // lengths << 17 | frontier after plane k << 21 | after both << 24
+  uint32_t enc2[5 * 256];
+  // one plane, with r = min(7, bits left) >= 1: index n * 256 + (r == 7 ?
+  // 128 + the next 7 bits : 2^r + the next r bits); entry = the plane's 4
+  // bits | bits read << 4 | frontier after << 7
+  uint16_t dec[5 * 256];
+};
+
+struct Code4 {
+  uint32_t code, len, n;
+};
+
+// encode_ints for one plane x (4 bits) at frontier n, with no budget limit
+GZ_CX Code4 plane4_code(uint32_t x, uint32_t n) {
+  uint32_t code = x & ((1u << n) - 1), len = n, m = n, xs = x >> n;
+  while (m < 4) {  // group tests
+    const uint32_t t = xs != 0;
+    code |= t << len++;
+    if (!t) break;
+    while (m < 3) {  // up to the next one; a one in the last position is implied
+      const uint32_t b = xs & 1u;
+      code |= b << len++;
+      if (b) break;
+      xs >>= 1;
+      m++;
+    }
+    xs >>= 1;
+    m++;
   }
-  if (k >= k_low && bits) k = code_planes_small<4, true>(k, k_low, n, bits, w, plane);
-  while (k >= k_low && bits) {  // n == 4
-    const uint32_t c = (uint32_t)(k - k_low + 1) < 16 ? (uint32_t)(k - k_low + 1) : 16;
-    uint64_t code = 0;
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-      code |= spread4((uint64_t)(brev_u(u[i]) >> (P - 1 - k)) & lowmask64(c)) << i;
-    const uint32_t l = 4 * c < bits ? 4 * c : bits;
-    w.put(code & lowmask64(l), l);
+  return Code4{code, len, m};
+}
+
+// decode_ints for one plane at frontier n from the r-bit budget v (bit 0
+// first): the plane's bits, the bits read, the new frontier
+GZ_CX Code4 plane4_decode(uint32_t v, uint32_t r, uint32_t n) {
+  const uint32_t m = n < r ? n : r;
+  uint32_t x = v & ((1u << m) - 1), pos = m, b = r - m;
+  while (n < 4 && b) {
+    b--;
+    if (!((v >> pos++) & 1u)) break;  // group test 0: no one left
+    while (n < 3 && b) {
+      b--;
+      if ((v >> pos++) & 1u) break;
+      n++;
+    }
+    x += 1u << n;  // also when the budget ended the run
+    n++;
+  }
+  return Code4{x, pos, n};
+}
+
+GZ_CX Plane4Tables make_plane4_tables() {
+  Plane4Tables t{};
+  for (uint32_t n = 0; n <= 4; n++) {
+    for (uint32_t i = 0; i < 256; i++) {
+      const Code4 a = plane4_code(i & 15u, n);
+      const Code4 c = plane4_code(i >> 4, a.n);
+      t.enc2[n * 256 + i] = (a.code | (c.code << a.len)) | (a.len << 14) |
+                            ((a.len + c.len) << 17) | (a.n << 21) | (c.n << 24);
+    }
+    for (uint32_t r = 1; r <= 7; r++)
+      for (uint32_t v = 0; v < (1u << r); v++) {
+        const Code4 d = plane4_decode(v, r, n);
+        t.dec[n * 256 + (r == 7 ? 128 + v : (1u << r) + v)] =
+            (uint16_t)(d.code | (d.len << 4) | (d.n << 7));
+      }
+  }
+  return t;
+}
+
+#if defined(__CUDACC__)
+// device copy, built by the compiler; kernels stage it in shared memory
+__device__ const __align__(16) Plane4Tables kPlane4Tables = make_plane4_tables();
+#endif
+
+// host copy (host builds and tests)
+inline const Plane4Tables* plane4_tables_host() {
+  static const Plane4Tables t = make_plane4_tables();
+  return &t;
+}
+
+// Planes k, k-1, ... down to k_low of a 4-value block while budget
+// remains, from the tables.  k starts at P - 1.  The 4x4 bit tiles of each
+// 32-bit slice of the coefficients are transposed, so word i holds planes
+// 32G + 4c + i at bits 4c..4c+3; the words are shifted up a tile at a time
+// and two planes make one table index.
+template <typename UInt, class W>
+GZ_HD void code_planes_4(const UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, W& w,
+                         const Plane4Tables& t) {
+  constexpr int NS = (int)sizeof(UInt) / 4;  // 32-bit slices
+  auto pair = [&](uint32_t xb) {  // planes k, k - 1 (xb = x_k | x_{k-1} << 4)
+    if (k < k_low || !bits) return;
+    const uint32_t e = t.enc2[n * 256 + xb];
+    const bool two = k - 1 >= k_low;
+    const uint32_t len = two ? (e >> 17) & 15u : (e >> 14) & 7u;
+    n = two ? (e >> 24) & 7u : (e >> 21) & 7u;
+    const uint32_t l = len < bits ? len : bits;
+    w.put(e & ((1u << l) - 1), l);
     bits -= l;
-    k -= (int)c;
+    k -= 2;
+  };
+#pragma unroll
+  for (int G = NS - 1; G >= 0; G--) {
+    uint32_t tw[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) tw[i] = (uint32_t)((uint64_t)u[i] >> (32 * G));
+    transpose_tiles<4>(tw);
+#pragma unroll 1
+    for (int c = 7; c >= 0 && k >= k_low && bits; c--) {
+      pair((tw[3] >> 28) | ((tw[2] >> 24) & 0xf0u));
+      pair((tw[1] >> 28) | ((tw[0] >> 24) & 0xf0u));
+#pragma unroll
+      for (int i = 0; i < 4; i++) tw[i] <<= 4;
+    }
   }
 }
 
+// Decode planes k = P - 1, ... down to k_low of a 4-value block while
+// budget remains, from the tables, into u (zero on entry).  The stream is
+// read through a 64-bit window refilled when fewer than 7 bits are left in
+// it; the planes are shifted into the transposed words of code_planes_4.
 template <typename UInt, class R>
-GZ_HD void uncode_planes_1d(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r) {
-  constexpr int P = 8 * sizeof(UInt);
-  auto deposit = [&](int kk, uint64_t x) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) u[i] |= (UInt)((x >> i) & 1u) << kk;
-  };
-  const bool full_runs = bits >= 64;  // as in code_planes_1d
-  k = uncode_runs01<4>(u[0], k, k_low, n, bits, r, deposit);
-  if (!full_runs) {
-    if (k >= k_low && bits) uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
-    return;
-  }
-  if (k >= k_low && bits) k = uncode_planes_small<4, true>(k, k_low, n, bits, r, deposit);
-  while (k >= k_low && bits) {  // n == 4: whole 4-bit planes, then the last partial one
-    uint32_t c = (uint32_t)(k - k_low + 1) < 16 ? (uint32_t)(k - k_low + 1) : 16;
-    if (bits / 4 < c) c = bits / 4;
-    if (!c) {
-      uncode_planes_small<4>(k, k_low, n, bits, r, deposit);
-      return;
+GZ_HD void uncode_planes_4(UInt* u, int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
+                           const Plane4Tables& t) {
+  constexpr int NS = (int)sizeof(UInt) / 4;
+  uint64_t win = r.peek64();
+  uint32_t avail = 64, taken = 0;  // bits of win not yet used; used since the last skip
+  auto one = [&]() -> uint32_t {   // plane k
+    if (k < k_low || !bits) return 0u;
+    if (avail < 7) {
+      r.skip(taken);
+      taken = 0;
+      win = r.peek64();
+      avail = 64;
     }
-    const uint64_t win = r.peek64();
+    const uint32_t v = (uint32_t)win & 127u;
+    const uint32_t idx = bits >= 7 ? 128u + v : (1u << bits) + (v & ((1u << bits) - 1));
+    const uint32_t e = t.dec[n * 256 + idx];
+    const uint32_t used = (e >> 4) & 7u;
+    n = e >> 7;
+    win >>= used;
+    avail -= used;
+    taken += used;
+    bits -= used;
+    k--;
+    return e & 15u;
+  };
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-      u[i] |= brev_u((UInt)(compact4(win >> i) & lowmask64(c))) >> (P - 1 - k);
-    r.skip(4 * c);
-    bits -= 4 * c;
-    k -= (int)c;
+  for (int G = NS - 1; G >= 0; G--) {
+    uint32_t tw[4] = {0, 0, 0, 0};
+    int c = 7;
+#pragma unroll 1
+    for (; c >= 0 && k >= k_low && bits; c--) {
+      const uint32_t x3 = one(), x2 = one(), x1 = one(), x0 = one();
+      tw[3] = (tw[3] << 4) | x3;
+      tw[2] = (tw[2] << 4) | x2;
+      tw[1] = (tw[1] << 4) | x1;
+      tw[0] = (tw[0] << 4) | x0;
+    }
+    const uint32_t sh = 4u * (uint32_t)(c + 1);  // tiles not reached are zero
+#pragma unroll
+    for (int i = 0; i < 4; i++) tw[i] = sh < 32 ? tw[i] << sh : 0u;
+    transpose_tiles<4>(tw);
+#pragma unroll
+    for (int i = 0; i < 4; i++) u[i] |= (UInt)((uint64_t)tw[i] << (32 * G));
   }
+  r.skip(taken);
 }
 
 // --------------------------------------------------------- float <-> bits
@@ -1237,7 +1342,7 @@ GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mo
     planes_to_store<0>(u, ps);
     code_planes<BS>(k, kmin, n, bits, w, [&](int kk) { return ps.get(kk); });
   } else if constexpr (D == 1) {
-    code_planes_1d(u, k, kmin, n, bits, w);
+    code_planes_4(u, k, kmin, n, bits, w, *ps.t4);
   } else {
     PL pl;
 #pragma unroll
@@ -1338,7 +1443,7 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
   } else if constexpr (D == 1) {
 #pragma unroll
     for (int i = 0; i < BS; i++) u[i] = 0;
-    uncode_planes_1d(u, k, kmin, n, bits, r);
+    uncode_planes_4(u, k, kmin, n, bits, r, *ps.t4);
   } else {
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) ps.put(i, 0);
@@ -1409,6 +1514,7 @@ GZ_HD uint32_t block_bits(R& r, const General& mode) {
 // Plane store backed by a plain array (host builds and tests).
 struct LocalPlanes {
   uint64_t v[64];
+  const Plane4Tables* t4 = plane4_tables_host();
   GZ_HD uint64_t get(int i) const { return v[i]; }
   GZ_HD void put(int i, uint64_t x) { v[i] = x; }
 };

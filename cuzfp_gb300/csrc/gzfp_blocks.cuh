@@ -57,7 +57,8 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
                          const uint8_t* __restrict__ shape, uint64_t count, uint32_t maxbits,
                          uint64_t* __restrict__ out, uint64_t nwords, uint32_t vec) {
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (i >= count) return;
   const uint64_t slot = index[i];
@@ -75,7 +76,8 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
                          const uint8_t* __restrict__ shape, uint64_t count, uint32_t maxbits,
                          T* __restrict__ tiles, uint32_t vec) {
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (i >= count) return;
   const uint64_t slot = index[i];
@@ -90,7 +92,7 @@ cudaError_t launch_encode_blocks_t(const T* tiles, const unsigned long long* ind
                                    uint64_t* out, uint64_t nwords, cudaStream_t s) {
   if (count == 0) return cudaSuccess;
   const dim3 grid((unsigned)((count + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0);
+  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0, table_words<D>());
   auto k = encode_blocks_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -105,7 +107,7 @@ cudaError_t launch_decode_blocks_t(const uint64_t* in, uint64_t nwords,
                                    uint64_t count, uint32_t maxbits, T* tiles, cudaStream_t s) {
   if (count == 0) return cudaSuccess;
   const dim3 grid((unsigned)((count + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0, table_words<D>());
   auto k = decode_blocks_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;

@@ -25,18 +25,41 @@ constexpr int kStride = kThreads + 1;    // staged word buffer row pitch (words)
 constexpr uint32_t kMaxStagedWords = 64; // staged decode up to 4096-bit blocks
 // dynamic shared memory of a CTA: the plane store (32 or 64 slots of 8
 // bytes per thread) and, for staged decode, the word buffer
-inline size_t smem_bytes(int slots, bool staged, uint32_t words_per_block) {
-  size_t b = (size_t)slots * kThreads * 8;
+inline size_t smem_bytes(int slots, bool staged, uint32_t words_per_block, int tables = 0) {
+  size_t b = ((size_t)slots * kThreads + (size_t)tables) * 8;
   if (staged) b += (size_t)words_per_block * kStride * 8;
   return b;
 }
 
-// per-thread plane store in shared memory, slot i at planes[i * kThreads]
+// per-thread plane store in shared memory, slot i at planes[i * kThreads];
+// t4: the CTA's copy of the 4-value plane tables (1D kernels only)
 struct SmemPlanes {
   uint64_t* p;
+  const Plane4Tables* t4;
   __device__ __forceinline__ uint64_t get(int i) const { return p[i * kThreads]; }
   __device__ __forceinline__ void put(int i, uint64_t v) { p[i * kThreads] = v; }
 };
+
+// 4-value blocks code through the plane tables, which each CTA copies into
+// the start of its shared memory (7.5 KB); other blocks use none.
+template <int D>
+__host__ __device__ constexpr int table_words() {
+  return D == 1 ? (int)(sizeof(Plane4Tables) / 8) : 0;
+}
+
+// Copy the plane tables into shared memory and return them (null for
+// D > 1).  Every thread of the CTA must call it before any thread returns.
+template <int D, int NT>
+__device__ __forceinline__ const Plane4Tables* stage_tables(uint64_t* smem) {
+  if constexpr (D != 1) {
+    return nullptr;
+  } else {
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(&kPlane4Tables);
+    for (int i = threadIdx.x; i < table_words<1>(); i += NT) smem[i] = src[i];
+    __syncthreads();
+    return reinterpret_cast<const Plane4Tables*>(smem);
+  }
+}
 
 // Global stream words.  `merge` ORs a word that neighbouring zfp blocks share
 // (only when maxbits is not a multiple of 64; the stream is zeroed first).
@@ -117,7 +140,8 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
     encode_kernel(const T* __restrict__ in, Geom g, uint32_t maxbits, uint64_t* __restrict__ out,
                   uint64_t nwords) {
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b < g.nblocks)
     encode_one<D, T>(in, g, b, maxbits, DevWords{out, nullptr, nwords}, ps);
@@ -131,11 +155,12 @@ __global__ void __launch_bounds__(kThreads, MINB)
     decode_kernel(const uint64_t* __restrict__ in, uint64_t nwords, Geom g, uint32_t maxbits,
                   T* __restrict__ out) {
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (STAGED) {
     const uint32_t W = maxbits >> 6;
-    uint64_t* buf = smem + decode_slots<D, T>() * kThreads;
+    uint64_t* buf = smem + table_words<D>() + decode_slots<D, T>() * kThreads;
     const uint64_t b0 = b - (threadIdx.x & 31);
     if (b0 < g.nblocks) {
       const uint64_t left = g.nblocks - b0;
@@ -156,7 +181,7 @@ cudaError_t launch_encode_t(const T* in, const Geom& g, uint32_t maxbits, uint64
                             uint64_t nwords, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0);
+  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0, table_words<D>());
   auto k = encode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -174,7 +199,7 @@ cudaError_t launch_decode_t(const uint64_t* in, uint64_t nwords, const Geom& g, 
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
   const bool staged = maxbits % 64 == 0 && (maxbits >> 6) <= kMaxStagedWords && g.base == 0;
-  const size_t sm = smem_bytes(decode_slots<D, T>(), staged, maxbits >> 6);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), staged, maxbits >> 6, table_words<D>());
   constexpr int MB = MinBlocks<D, T>::value;
   auto k = !staged ? decode_kernel<D, T, false, MB>
            : (MB < 4 && sm <= kSmemFor4) ? decode_kernel<D, T, true, 4>

@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b >= g.nblocks) return;
   uint32_t ix, iy, iz;
@@ -63,7 +64,8 @@ __global__ void __launch_bounds__(kThreads, (MinBlocks<D, T>::value))
   typedef typename FT<T>::UInt UInt;
   constexpr int BS = 1 << (2 * D);
   extern __shared__ uint64_t smem[];
-  SmemPlanes ps{smem + threadIdx.x};
+  const Plane4Tables* t4 = stage_tables<D, kThreads>(smem);
+  SmemPlanes ps{smem + table_words<D>() + threadIdx.x, t4};
   const uint64_t b = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
   if (b >= g.nblocks) return;
   uint32_t ix, iy, iz;
@@ -99,7 +101,7 @@ cudaError_t launch_encode_mode_t(const T* in, const Geom& g, const General& mode
                                  cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0);
+  const size_t sm = smem_bytes(store_slots<D, T>(), false, 0, table_words<D>());
   auto k = encode_mode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -113,7 +115,7 @@ cudaError_t launch_decode_mode_t(const uint64_t* in, uint64_t nwords,
                                  const General& mode, T* out, cudaStream_t s) {
   if (g.nblocks == 0) return cudaSuccess;
   const dim3 grid((unsigned)((g.nblocks + kThreads - 1) / kThreads));
-  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0);
+  const size_t sm = smem_bytes(decode_slots<D, T>(), false, 0, table_words<D>());
   auto k = decode_mode_kernel<D, T>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
