@@ -60,6 +60,10 @@ def parse():
                         "fields with partial edge blocks at rates 4, 12 and 24")
     p.add_argument("--tolerance", type=float, default=1e-6,
                    help="accuracy workload: absolute error tolerance")
+    p.add_argument("--edges-fields", default="1d_f32_walk,2d_f32_16381x16383,2d_f64_8191x8190",
+                   help="edges workload: the fields to run (for profiling one of them)")
+    p.add_argument("--edges-scale", type=float, default=1.0,
+                   help="edges workload: values per field x this (for small profiling cases)")
     p.add_argument("--arrays", type=int, default=512, help="batched workload: array count")
     p.add_argument("--requests", type=int, default=20000, help="serving workload: requests")
     p.add_argument("--inflight", type=int, default=3, help="serving workload: batches in flight")
@@ -523,12 +527,19 @@ def run_edges(args, rank, world, local):
     stream = torch.cuda.Stream(device=dev)
     peak, peak_kind = peaks()
     cases, tot_bytes, tot_ms = [], 0, 0.0
-    fields = [("1d_f32_walk", lambda: synth.random_walk_device((1 << 28) - 3, seed=2 + rank,
-                                                            dtype=torch.float32, device=dev)),
+    sc = args.edges_scale
+    side = lambda n: max(1, int(round(n * sc ** 0.5)))  # noqa: E731
+    fields = [("1d_f32_walk", lambda: synth.random_walk_device(
+                  max(1, int((1 << 28) * sc) - 3), seed=2 + rank, dtype=torch.float32,
+                  device=dev)),
               ("2d_f32_16381x16383", lambda: synth.sinusoids_device(
-                  (16383, 16381), 8, 64, seed=3 + rank, dtype=torch.float32, device=dev)),
+                  (side(16383), side(16381)), 8, 64, seed=3 + rank, dtype=torch.float32,
+                  device=dev)),
               ("2d_f64_8191x8190", lambda: synth.sinusoids_device(
-                  (8190, 8191), 8, 64, seed=4 + rank, dtype=torch.float64, device=dev))]
+                  (side(8190), side(8191)), 8, 64, seed=4 + rank, dtype=torch.float64,
+                  device=dev))]
+    keep = set(args.edges_fields.split(","))
+    fields = [f for f in fields if f[0] in keep]
     with ClockSampler(local) as clk:
         for name, make in fields:
             x = make()
@@ -578,7 +589,9 @@ def run_edges(args, rank, world, local):
         "ms_per_step": round(tot_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": "edges_1d_f32_2d_f32_2d_f64_rates_4_12_24",
-                   "l2": "inputs larger than L2 (0.5-1 GiB fields)",
+                   "fields": [f[0] for f in fields], "scale": sc,
+                   "l2": "inputs larger than L2 (0.5-1 GiB fields)" if sc >= 1 else
+                         f"fields scaled by {sc}",
                    "parallelism": f"replicas x{world}"},
         "cases": cases,
         "roofline": {"bound": "hbm", "kernel": f"slowest case {worst['field']} rate {worst['rate']}",
