@@ -98,6 +98,34 @@ def test_arbitrary_streams(gz, orc, cuda):
                                  orc.decompress(w, shape, dt, rate)), (shape, dt, rate)
 
 
+def test_1d_plane_tables(gz, orc, cuda):
+    """1D blocks code and decode through the 4-value plane tables: every
+    length remainder, all four scalar types, budgets from 2 to 256 bits per
+    block (word-aligned or not), and random words decoded at each budget."""
+    rng = np.random.default_rng(4646)
+    rates = (0.5, 1, 2.25, 3, 4, 7, 8, 12, 13.5, 16, 24, 31, 32, 48, 64)
+    for i, rate in enumerate(rates):
+        for dt in (np.float32, np.float64, np.int32, np.int64):
+            n = int(rng.integers(1, 3000)) + i % 4
+            if np.dtype(dt).kind == "f":
+                a = (np.cumsum(rng.standard_normal(n)) * 10.0 ** rng.integers(-20, 20)).astype(dt)
+            else:
+                bits = 8 * np.dtype(dt).itemsize
+                a = np.clip(np.cumsum(rng.integers(-1000, 1000, n)), -(2 ** (bits - 3)),
+                            2 ** (bits - 3)).astype(dt)
+            if orc.stream_bytes(a.shape, a.dtype, rate) == 0:
+                continue
+            s = orc.compress(a, rate)
+            assert np.array_equal(gpu_compress(gz, a, rate, cuda), s), (n, dt, rate)
+            assert same_bits(gpu_decompress(gz, s, a.shape, a.dtype, rate, cuda),
+                             orc.decompress(s, a.shape, a.dtype, rate)), (n, dt, rate)
+            if np.dtype(dt).kind == "f":
+                w = rng.integers(0, 2 ** 63, s.size, dtype=np.int64).astype(np.uint64)
+                w = (w << np.uint64(1)) | rng.integers(0, 2, s.size).astype(np.uint64)
+                assert same_bits(gpu_decompress(gz, w, a.shape, a.dtype, rate, cuda),
+                                 orc.decompress(w, a.shape, a.dtype, rate)), ("random", n, dt, rate)
+
+
 def test_golden_small(gz, cuda):
     for c in golden_io.load_all():
         a = c["input"]
