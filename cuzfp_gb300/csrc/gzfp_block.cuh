@@ -558,14 +558,71 @@ GZ_HD int code_planes(int k, int k_low, uint32_t& n, uint32_t& bits, W& w, Plane
   return k;
 }
 
+// The group tests of one plane from a 64-bit window w of the stream, of
+// which `used` bits (the plane's verbatim bits) are taken, with `bits` the
+// budget from the window's start and `pos` the frontier: decode_ints'
+// loops (Z/src/template/decode.c:88-99) one new coefficient at a time,
+// including the budget ending inside a run (a one is still deposited where
+// it ends) and the implied one in the last position.  Ones go into x;
+// `used` and `pos` advance.  Returns false, with nothing final, when the
+// group runs past the window; the caller then decodes it from the stream.
+// Every plane, the last one in the budget included, takes this one path,
+// so the lanes of a warp do not split at their blocks' last planes.
+template <int BS, typename X>
+GZ_HD bool group_in_window(uint64_t w, uint32_t bits, uint32_t& used, uint32_t& pos, X& x) {
+  if (pos >= (uint32_t)BS || used >= bits) return true;  // no group tests
+  bool more = (w >> used) & 1;  // the first test bit (used < 64 here)
+  used++;
+  uint64_t g = shr64(w, used);
+  while (more) {
+    const uint32_t t = ctz64(g);  // zeros before the next one in the window
+    const uint32_t rem = bits - used, lim = (uint32_t)BS - 1 - pos;
+    uint32_t z = t < rem ? t : rem;
+    z = z < lim ? z : lim;  // zeros read before the run ends
+    if (used + z + 2 > 64) return false;
+    const uint32_t c = z + ((z == t && t < rem && t < lim) ? 1u : 0u);  // with the one, if read
+    x |= (X)1 << (pos + z);
+    g >>= c;
+    used += c;
+    pos += z + 1;
+    more = false;
+    if (pos < (uint32_t)BS && used < bits) {  // the next test bit
+      more = g & 1;
+      g >>= 1;
+      used++;
+    }
+  }
+  return true;
+}
+
 // uncode_planes for blocks of at most 16 values: the verbatim bits and the
 // group tests of a plane (at most 16 + 33 bits) come from one 64-bit window.
-// Same bits as the general form below.
-template <int BS, bool STOP_FULL = false, class R, class StoreFn>
+// Same bits as the general form below.  UNIFIED: every plane, the one the
+// budget ends in included, goes through group_in_window, so a warp's lanes
+// do not split at their blocks' last planes (faster for 2D blocks of 32-bit
+// values; for 64-bit values and 4^3 blocks the split form measured faster).
+template <int BS, bool STOP_FULL = false, bool UNIFIED = false, class R, class StoreFn>
 GZ_HD int uncode_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
                               StoreFn&& store) {
   static_assert(BS <= 16, "at most 16 values per block");
   for (; k >= k_low && bits && !(STOP_FULL && n == (uint32_t)BS); k--) {
+    if constexpr (UNIFIED) {
+      const uint32_t h = n < bits ? n : bits;  // verbatim bits (n == BS once all are significant)
+      const uint64_t w = r.peek64();
+      const uint32_t x0 = (uint32_t)w & ((1u << h) - 1);
+      uint32_t x = x0, used = h, pos = n;
+      if (group_in_window<BS>(w, bits, used, pos, x)) {
+        r.skip(used);
+        bits -= used;
+        n = pos;
+        store(k, x);
+      } else {
+        r.skip(h);
+        bits -= h;
+        store(k, decode_group<BS>(x0, n, bits, r));
+      }
+      continue;
+    }
     const bool full = n == (uint32_t)BS;
     const uint32_t hlen = full ? (uint32_t)BS : n;
     if (hlen > bits) {  // the budget ends inside the verbatim bits
@@ -616,9 +673,10 @@ GZ_HD int uncode_planes_small(int k, int k_low, uint32_t& n, uint32_t& bits, R& 
 // when they lie inside it and the budget, with no one implied by the last
 // position.  Otherwise (the plane the budget ends in, and rarely others)
 // the general routine decodes the group tests.
-template <int BS, class R, class StoreFn>
+template <int BS, bool UNIFIED = false, class R, class StoreFn>
 GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
-  if constexpr (BS <= 16) return uncode_planes_small<BS>(k, k_low, n, bits, r, store);
+  if constexpr (BS <= 16)
+    return uncode_planes_small<BS, false, UNIFIED>(k, k_low, n, bits, r, store);
   for (; k >= k_low && bits; k--) {
     const bool full = n == (uint32_t)BS;
     const uint32_t hlen = full ? (uint32_t)BS : n;
@@ -754,7 +812,7 @@ GZ_HD int code_runs01(UInt u0, UInt above0, UInt above1, int k, int k_low, uint3
 // frontier is 0 or 1: runs add their bits of the first coefficient to u0,
 // the planes that bring a new coefficient go to store(k, x).  Returns the
 // next plane; the same bits as uncode_planes<BS>.
-template <int BS, typename UInt, class R, class StoreFn>
+template <int BS, bool UNIFIED = false, typename UInt, class R, class StoreFn>
 GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits, R& r,
                         StoreFn&& store) {
   constexpr int P = 8 * sizeof(UInt);
@@ -786,7 +844,7 @@ GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits,
       continue;
     }
     // plane k brings a new coefficient, or the budget ends inside it
-    k = uncode_planes_small<BS>(k, k, n, bits, r, store);
+    k = uncode_planes_small<BS, false, UNIFIED>(k, k, n, bits, r, store);
   }
   return k;
 }
@@ -1452,8 +1510,9 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
       ps.put(G * BS + rr, ps.get(G * BS + rr) | (x << (g * PL::N)));
     };
     UInt u0 = 0;  // the runs' bits of the first coefficient
-    if constexpr (BS <= 16 && P == 32) k = uncode_runs01<BS>(u0, k, kmin, n, bits, r, store);
-    if (k >= kmin && bits) uncode_planes<BS>(k, kmin, n, bits, r, store);
+    if constexpr (BS <= 16 && P == 32)
+      k = uncode_runs01<BS, true>(u0, k, kmin, n, bits, r, store);
+    if (k >= kmin && bits) uncode_planes<BS, P == 32>(k, kmin, n, bits, r, store);
     PL pl;
 #pragma unroll
     for (int i = 0; i < PL::NW; i++) pl.tw[i] = (uint32_t)ps.get(i);
