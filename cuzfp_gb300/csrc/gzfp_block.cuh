@@ -800,9 +800,10 @@ GZ_HD int code_runs01(UInt u0, UInt above0, UInt above1, int k, int k_low, uint3
         k -= (int)c;
         r -= c;
       }
-      continue;  // k == lo, or the budget is spent
     }
-    // plane k brings a new coefficient
+    // then, in the same step (so that a warp's lanes stay together), plane
+    // k = kstop, which brings a new coefficient
+    if (k < k_low || !bits) break;
     k = code_planes_small<BS>(k, k, n, bits, w, plane);
   }
   return k;
@@ -841,9 +842,10 @@ GZ_HD int uncode_runs01(UInt& u0, int k, int k_low, uint32_t& n, uint32_t& bits,
       r.skip(rr * gw);
       bits -= rr * gw;
       k -= (int)rr;
-      continue;
     }
-    // plane k brings a new coefficient, or the budget ends inside it
+    // then, in the same step, one plane one at a time: one that brings a
+    // new coefficient, the budget's last, or a plane past the window
+    if (k < k_low || !bits) break;
     k = uncode_planes_small<BS, false, UNIFIED>(k, k, n, bits, r, store);
   }
   return k;
