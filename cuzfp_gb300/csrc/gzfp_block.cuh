@@ -727,7 +727,7 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
 // (plane k first) spread to every other bit.  Runs at frontier 0 (all-zero
 // planes, one 0 bit each) and 1 are coded and decoded whole; the other
 // planes go one at a time through the small-block coder.  (Used for 2D
-// blocks of 32-bit values; 4-value blocks use the plane tables below.)
+// blocks; 4-value blocks use the plane tables below.)
 
 // bit i of x (below 2^32) to bit 2i
 GZ_HD uint64_t spread2(uint64_t x) {
@@ -1417,9 +1417,8 @@ GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mo
       const uint32_t word = (uint32_t)ps.get(G * BS + r);
       return (uint64_t)((word >> (g * PL::N)) & ((1u << PL::N) - 1));
     };
-    // runs while the first coefficient alone is significant (for 2D blocks
-    // of 64-bit values they measured slower than plane by plane)
-    if constexpr (BS <= 16 && P == 32) {
+    // runs while the first coefficient alone is significant
+    if constexpr (BS <= 16) {
       UInt above1 = 0;
 #pragma unroll
       for (int i = 1; i < BS; i++) above1 |= u[i];
@@ -1512,8 +1511,8 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
       ps.put(G * BS + rr, ps.get(G * BS + rr) | (x << (g * PL::N)));
     };
     UInt u0 = 0;  // the runs' bits of the first coefficient
-    if constexpr (BS <= 16 && P == 32)
-      k = uncode_runs01<BS, true>(u0, k, kmin, n, bits, r, store);
+    if constexpr (BS <= 16)
+      k = uncode_runs01<BS, P == 32>(u0, k, kmin, n, bits, r, store);
     if (k >= kmin && bits) uncode_planes<BS, P == 32>(k, kmin, n, bits, r, store);
     PL pl;
 #pragma unroll
