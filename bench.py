@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -166,8 +167,32 @@ class ClockSampler:
 
 # --------------------------------------------------------------- CPU side
 
+def load_synth():
+    """cuzfp_gb300/synth.py loaded by path.  Importing it through the package
+    would run the package's __init__, which loads the CUDA codec; the CPU
+    reference arm must not load it."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "gzfp_synth", os.path.join(ROOT, "cuzfp_gb300", "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def plain_config(maxbits: int, sbytes: int, world: int) -> dict:
+    """The `config` of the plain 3D workload, the same on both arms."""
+    return {"workload": WORKLOAD, "shape": list(SHAPE), "rate": RATE, "maxbits": maxbits,
+            "stream_bytes": sbytes,
+            "l2": ("inputs larger than L2" if SHAPE[0] * SHAPE[1] * SHAPE[2] * 8 > 129e6
+                   else "field smaller than L2 (a profiling size)") +
+                  f" ({(SHAPE[0] * SHAPE[1] * SHAPE[2] * 8) >> 20} MiB field, "
+                  f"{sbytes >> 20} MiB stream)",
+            "parallelism": f"replicas x{world}"}
+
 def cpu_measure(field_np, rate: float, threads: int, reps: int = 1):
-    """Oracle (CPU restatement of zfp 0.5.0) compress+decompress throughput."""
+    """Oracle (CPU restatement of zfp 0.5.0) compress+decompress throughput:
+    (GB/s both ways, compress GB/s, decompress GB/s, the stream, the
+    decompressed array)."""
     from oracle import oracle
     nbytes = field_np.nbytes
     best = None
@@ -175,41 +200,43 @@ def cpu_measure(field_np, rate: float, threads: int, reps: int = 1):
         t0 = time.perf_counter()
         s = oracle.compress(field_np, rate, threads)
         t1 = time.perf_counter()
-        oracle.decompress(s, field_np.shape, field_np.dtype, rate, threads)
+        d = oracle.decompress(s, field_np.shape, field_np.dtype, rate, threads)
         t2 = time.perf_counter()
         gbs = 2 * nbytes / (t2 - t0) / 1e9
         if best is None or gbs > best[0]:
             best = (gbs, nbytes / (t1 - t0) / 1e9, nbytes / (t2 - t1) / 1e9)
-    return best
+    return best + (s, d)
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the oracle port of zfp 0.5.0 on all host cores."""
+    """--impl reference: zfp 0.5.0's CPU path (the oracle port, pinned bit for
+    bit to the reference's own zfp build) on all host cores, one step = the
+    whole field compressed and decompressed."""
     import numpy as np
     if rank != 0:
         return
     from oracle import oracle
-    from cuzfp_gb300 import synth
-    oracle.port()
+    synth = load_synth()
+    lib = oracle.port()
     threads = os.cpu_count() or 1
-    planes = 128  # 128 x 512 x 512 doubles = 256 MiB of the 1 GiB field per step
-    field = synth.sinusoids((planes, SHAPE[1], SHAPE[2]), 16, 32, seed=0, dtype=np.float64)
+    field = synth.sinusoids(SHAPE, 16, 32, seed=0, dtype=np.float64)
+    maxbits = int(lib.gzo_maxbits(oracle.DOUBLE, 3, RATE))
+    sbytes = int(lib.gzo_stream_bytes(oracle.DOUBLE, SHAPE[2], SHAPE[1], SHAPE[0], RATE))
     for _ in range(max(args.warmup, 0)):
         cpu_measure(field, RATE, threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s = oracle.compress(field, RATE, threads)
-        oracle.decompress(s, field.shape, field.dtype, RATE, threads)
+        st = oracle.compress(field, RATE, threads)
+        oracle.decompress(st, field.shape, field.dtype, RATE, threads)
     dt = time.perf_counter() - t0
     value = 2 * field.nbytes * args.steps / dt / 1e9
-    sample = f"first {planes} of 512 z-planes (256 MiB) of the field per step"
+    sample = f"the whole {field.nbytes >> 20} MiB field, compress+decompress, every step"
     out = {
         "impl": "reference", "metric": "zfp fixed-rate compress+decompress throughput",
         "value": round(value, 4), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "rate": RATE,
-                                        "l2": "inputs larger than L2"},
+        "data": "synthetic", "config": plain_config(maxbits, sbytes, args.gpus),
         "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -776,8 +803,19 @@ def run(args, rank, world, local):
     ms_per_step = total_ms / args.steps
     value = 2 * nbytes * world / (ms_per_step * 1e-3) / 1e9
 
-    # correctness spot check of this run's buffers against the oracle on one
-    # block-aligned brick (cheap; the full parity suite lives in tests/)
+    # rate-distortion of the decoded field against the original, for
+    # information (the zfp tool's statistics, zfp-0.5.0/utils/zfp.c:29-57)
+    err = (out - field).abs()
+    erms = float(torch.sqrt((err * err).mean()))
+    frange = float(field.max() - field.min())
+    distortion = {"maxe": float(err.max()), "rmse": erms,
+                  "nrmse": erms / frange if frange > 0 else 0.0,
+                  "psnr": 20 * math.log10(frange / (2 * erms)) if erms > 0 and frange > 0
+                  else float("inf")}
+    del err
+    dev_stream = words.cpu().numpy().view(np.uint64)
+    dev_out = out.cpu().numpy()
+
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -824,24 +862,33 @@ def run(args, rank, world, local):
     except Exception:
         traffic = None
     cpu = None
+    parity = {"checked": False}
     if not args.no_cpu:
         from oracle import oracle
         oracle.port()
         host = field.cpu().numpy()
         threads = os.cpu_count() or 1
-        gbs, c_gbs, d_gbs = cpu_measure(host, RATE, threads, reps=2)
+        gbs, c_gbs, d_gbs, ref_s, ref_d = cpu_measure(host, RATE, threads, reps=2)
         cpu = {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"the whole {nbytes >> 20} MiB field, compress+decompress, best of 2",
                "compress_gbs": round(c_gbs, 4), "decompress_gbs": round(d_gbs, 4)}
+        # the CPU leg coded the very field the GPU coded: compare the whole
+        # stream and the whole decoded array bit for bit, for the timed
+        # device-buffer run and for the host-buffer (e2e) run
+        parity = {"checked": True, "compared": "whole field",
+                  "stream": bool(np.array_equal(dev_stream, ref_s)),
+                  "output": bool(np.array_equal(dev_out.view(np.uint64), ref_d.view(np.uint64)))}
+        if e2e is not None:
+            parity["e2e_stream"] = bool(np.array_equal(h_stream.numpy().view(np.uint64), ref_s))
+            parity["e2e_output"] = bool(np.array_equal(h_out.numpy().view(np.uint64),
+                                                       ref_d.view(np.uint64)))
+        del ref_s, ref_d, host
     res = {
         "metric": "zfp fixed-rate compress+decompress throughput",
         "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "rate": RATE,
-                   "maxbits": zfp.maxbits, "stream_bytes": sbytes,
-                   "l2": "inputs larger than L2 (1 GiB field, 256 MiB stream)",
-                   "parallelism": f"replicas x{world}"},
+        "config": plain_config(zfp.maxbits, sbytes, world),
         "compress_gbs": round(nbytes / (enc_ms * 1e-3) / 1e9, 3),
         "decompress_gbs": round(nbytes / (dec_ms * 1e-3) / 1e9, 3),
         "kernels": {"encode": {"ms": round(enc_ms, 4), "alg_gbs": round(enc_gbs, 2),
@@ -855,6 +902,8 @@ def run(args, rank, world, local):
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "parity": parity,
+        "rate_distortion": distortion,
     }
     print(json.dumps(res), flush=True)
 

@@ -21,7 +21,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libzfp_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libzfpref.so")
 FIELDS_LIB = os.path.join(HERE, "_ref", "libzfpfields.so")
-REF_TREE = os.environ.get("GZFP_REFERENCE_ROOT", "/root/reference")
+# the cuZFP checkout: GZFP_REFERENCE_ROOT, else a checkout named `reference`
+# beside this repository
+REF_TREE = os.environ.get("GZFP_REFERENCE_ROOT",
+                          os.path.abspath(os.path.join(HERE, "..", "..", "reference")))
 
 INT32, INT64, FLOAT, DOUBLE = 1, 2, 3, 4  # zfp_type (Z/inc/zfp.h:107-113)
 
