@@ -316,6 +316,30 @@ GZ_HD void decode_one(T* out, const Geom& g, uint64_t b, uint32_t maxbits, Words
   uint32_t ix, iy, iz;
   block_coords(g, b, ix, iy, iz);
   BitReader<Words> r(words, g.base + b * (uint64_t)maxbits);
+  if constexpr (D == 3 && !FT<T>::INT && sizeof(T) == 8) {
+    // 4^3 double blocks hand over their values one z slice at a time, so
+    // that the inverse transform does not keep all 64 values live (the
+    // register budget of the 4-CTA decoder spills otherwise)
+    const uint32_t cx = valid_count(g.nx, ix), cy = valid_count(g.ny, iy),
+                   cz = valid_count(g.nz, iz);
+    const int64_t sx = g.sx, sy = g.sy, sz = g.sz;
+    UInt* base = (UInt*)out + 4 * (ix * sx + iy * sy + iz * sz);
+    const bool vec = g.vec && cx == 4 && cy == 4 && cz == 4;
+    decode_block_mode<3, T, true>(r, FixedRate{maxbits}, nullptr, ps, [&](int z, const UInt* rs) {
+      if (vec) {
+#pragma unroll
+        for (int y = 0; y < 4; y++) store_row((T*)base + y * sy + z * sz, rs + 4 * y);
+      } else {
+#pragma unroll
+        for (int y = 0; y < 4; y++)
+#pragma unroll
+          for (int x = 0; x < 4; x++)
+            if ((uint32_t)x < cx && (uint32_t)y < cy && (uint32_t)z < cz)
+              base[x * sx + y * sy + z * sz] = rs[4 * y + x];
+      }
+    });
+    return;
+  }
   UInt raw[BS];
   decode_block<D, T>(r, maxbits, raw, ps);
   scatter<D, T>(out, g, ix, iy, iz, raw);

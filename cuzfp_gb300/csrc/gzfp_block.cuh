@@ -720,6 +720,54 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
   return k;
 }
 
+// Planes k, ... down to k_low of a 4^3 block while budget remains, decoded
+// as one flat sequence of steps, each of which reads one token: a plane's
+// verbatim bits with its first group test, or one run of a group (its
+// zeros, the one -- read, implied by the last position, or placed where the
+// budget ends, as decode_ints places it (Z/src/template/decode.c:88-99) --
+// and the test after it).  A warp's lanes step through tokens, not planes,
+// so a plane with many new ones in one lane does not hold the others at
+// that plane.  Same bits as uncode_planes<64>.
+template <class R, class StoreFn>
+GZ_HD int uncode_flat64(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
+  uint64_t x = 0;
+  uint32_t pos = n;
+  bool grp = false;
+  // a group test of 1 that spends the budget still places a one (a run cut
+  // off after no zeros), so a pending group runs even with no bits left
+  while (k >= k_low && (bits || grp)) {
+    const uint64_t w = r.peek64();
+    uint32_t c;
+    if (!grp) {  // verbatim bits, cut by the budget
+      const uint32_t h = umin(n, bits);  // n <= 64
+      x = w & lowmask64(h);
+      c = h;
+      pos = n;
+    } else {  // zeros up to the next one, the last position or the budget's end
+      const uint32_t t = ctz64(w);
+      const uint32_t lim = umin(63 - pos, bits);
+      const bool read = t < lim;
+      const uint32_t z = read ? t : lim;
+      c = read ? t + 1 : lim;
+      x |= 1ull << (pos + z);
+      pos += z + 1;
+    }
+    const uint32_t rest = bits - c;
+    const bool has_test = pos < 64 && rest > 0;  // c < 64 here
+    const bool test = has_test && ((w >> c) & 1);
+    c += has_test ? 1u : 0u;
+    bits = rest - (has_test ? 1u : 0u);
+    r.skip(c);
+    grp = test;
+    if (!test) {  // the plane is complete
+      store(k, x);
+      k--;
+      n = pos;
+    }
+  }
+  return k;
+}
+
 // ------------------------------------------------- runs at frontier 0 and 1
 // In a block of smooth data the first coefficient is often the only
 // significant one for many planes: each such plane is that coefficient's
@@ -1446,8 +1494,17 @@ GZ_HD void encode_block(const typename FT<T>::UInt* raw, uint32_t maxbits, W& w,
 // bit patterns (Z/src/template/decode.c:137-165).  Returns the bits the
 // block takes in the stream (fixed rate: maxbits; the reader is not moved
 // past a block's padding).
-template <int D, typename T, class Mode, class R, class PS>
-GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* raw, PS& ps) {
+struct NoSlice {
+  template <typename U>
+  GZ_HD void operator()(int, const U*) const {}
+};
+
+// SLICED (4^3 floating-point blocks): the values of z slice z go to
+// slice(z, 16 values) as soon as they are final, and raw is not written.
+template <int D, typename T, bool SLICED = false, class Mode, class R, class PS,
+          class SliceFn = NoSlice>
+GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* raw, PS& ps,
+                                 SliceFn&& slice = SliceFn{}) {
   typedef FT<T> F;
   typedef typename F::UInt UInt;
   typedef typename F::Int Int;
@@ -1463,8 +1520,16 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
   } else {
     const uint64_t head = r.peek64();
     if (!(head & 1)) {
+      if constexpr (D == 3 && SLICED) {
+        UInt zs[16];
 #pragma unroll
-      for (int i = 0; i < BS; i++) raw[i] = 0;
+        for (int i = 0; i < 16; i++) zs[i] = 0;
+#pragma unroll
+        for (int z = 0; z < 4; z++) slice(z, zs);
+      } else {
+#pragma unroll
+        for (int i = 0; i < BS; i++) raw[i] = 0;
+      }
       return mode.min_bits() > 1 ? mode.min_bits() : 1;
     }
     r.skip(F::EBITS + 1);
@@ -1486,17 +1551,17 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
       // top-half planes into the store, folded into the coefficients before
       // the bottom half reuses the store
       const int top = k;
-      k = uncode_planes<BS>(k, kmin > 32 ? kmin : 32, n, bits, r,
-                            [&](int kk, uint64_t x) { ps.put(kk - 32, x); });
+      k = uncode_flat64(k, kmin > 32 ? kmin : 32, n, bits, r,
+                        [&](int kk, uint64_t x) { ps.put(kk - 32, x); });
       store_to_coeffs<1>(ps, 0, k - 32, top - 32, u);
       if (k >= kmin && bits) {
         const int top0 = k;
-        k = uncode_planes<BS>(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
+        k = uncode_flat64(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
         store_to_coeffs<0>(ps, 0, k, top0, u);
       }
     } else {
       const int top = k;
-      k = uncode_planes<BS>(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
+      k = uncode_flat64(k, kmin, n, bits, r, [&](int kk, uint64_t x) { ps.put(kk, x); });
       store_to_coeffs<0>(ps, 0, k, top, u);
     }
   } else if constexpr (D == 1) {
@@ -1526,6 +1591,25 @@ GZ_HD uint32_t decode_block_mode(R& r, const Mode& mode, typename FT<T>::UInt* r
   Int q[BS];
 #pragma unroll
   for (int i = 0; i < BS; i++) q[Perm<D>::at(i)] = (Int)((u[i] ^ (UInt)F::NB) - (UInt)F::NB);
+  if constexpr (D == 3 && !F::INT && SLICED) {
+    // inverse lifts along z, then each z slice to the end (y, x, values,
+    // sink) before the next, so that a finished slice's values are dead
+#pragma unroll
+    for (int l = 0; l < 16; l++) inv_lift(q[l], q[l + 16], q[l + 32], q[l + 48]);
+#pragma unroll
+    for (int z = 0; z < 4; z++) {
+      Int* qs = q + 16 * z;
+#pragma unroll
+      for (int x = 0; x < 4; x++) inv_lift(qs[x], qs[x + 4], qs[x + 8], qs[x + 12]);
+#pragma unroll
+      for (int y = 0; y < 4; y++) inv_lift(qs[4 * y], qs[4 * y + 1], qs[4 * y + 2], qs[4 * y + 3]);
+      UInt rs[16];
+      dequantize(qs, rs, 16, emax);
+      slice(z, rs);
+    }
+    const uint32_t used = (maxbits - budget) + (budget - bits);
+    return used < mode.min_bits() ? mode.min_bits() : used;
+  }
   inv_xform<D>(q);
   if constexpr (F::INT) {
 #pragma unroll
