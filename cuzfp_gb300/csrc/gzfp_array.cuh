@@ -212,7 +212,7 @@ GZ_HD void scatter(T* out, const Geom& g, uint32_t ix, uint32_t iy, uint32_t iz,
 // Words that another block also touches (the first and last word when the
 // block does not start / end on a word boundary) go through `Words::merge`,
 // every other word through `Words::store`.
-template <class Words>
+template <class Words, bool ALIGNED = false>
 struct BitWriter {
   Words words;
   uint64_t wi;      // index of the word being filled
@@ -230,7 +230,7 @@ struct BitWriter {
     last = (end & 63) ? (end >> 6) : ~0ull;
   }
   GZ_HD void emit() {
-    if (wi == first || wi == last)
+    if (!ALIGNED && (wi == first || wi == last))
       words.merge(wi, acc);
     else
       words.store(wi, acc);
@@ -275,7 +275,14 @@ struct BitReader {
     w0 = words.load(wi);
     w1 = words.load(wi + 1);
   }
-  GZ_HD uint64_t peek64() const { return (w0 >> off) | ((w1 << 1) << (63 - off)); }
+  GZ_HD uint64_t peek64() const {
+    // the 64 bits from `off` of (w1:w0): one funnel shift per result word
+    const uint32_t a0 = lo32(w0), a1 = hi32(w0), a2 = lo32(w1), a3 = hi32(w1);
+    const bool ge = off >= 32;
+    const uint32_t s = off & 31;
+    const uint32_t b0 = ge ? a1 : a0, b1 = ge ? a2 : a1, b2 = ge ? a3 : a2;
+    return ((uint64_t)fshr(b1, b2, s) << 32) | fshr(b0, b1, s);
+  }
   GZ_HD void skip(uint32_t n) {  // n <= 64
     off += n;
     if (off >= 64) {
@@ -295,7 +302,7 @@ struct BitReader {
 
 // ------------------------------------------------------- per-block drivers
 
-template <int D, typename T, class Words, class PS>
+template <int D, typename T, bool ALIGNED = false, class Words, class PS>
 GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, Words words,
                       PS& ps) {
   typedef typename FT<T>::UInt UInt;
@@ -304,7 +311,7 @@ GZ_HD void encode_one(const T* in, const Geom& g, uint64_t b, uint32_t maxbits, 
   block_coords(g, b, ix, iy, iz);
   UInt raw[BS];
   gather<D, T>(in, g, ix, iy, iz, raw);
-  BitWriter<Words> w(words, g.base + b * (uint64_t)maxbits, maxbits);
+  BitWriter<Words, ALIGNED> w(words, g.base + b * (uint64_t)maxbits, maxbits);
   encode_block<D, T>(raw, maxbits, w, ps);
   w.finish();
 }

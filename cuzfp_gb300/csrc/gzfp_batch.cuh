@@ -71,6 +71,9 @@ __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, Batc
         warp_copy<false, NT + 1>(sbuf + (threadIdx.x & ~31u), (uint64_t*)d.in + b0 * W, W,
                                  left < 32 ? (uint32_t)left : 32);
       }
+      // zero rows after the slot: the staged bit reader loads two words
+#pragma unroll
+      for (uint32_t j = 0; j < kPadRows; j++) sbuf[(W + j) * (NT + 1) + threadIdx.x] = 0;
       __syncwarp();
       if (b < d.g.nblocks)
         decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
@@ -138,11 +141,12 @@ __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
 }
 
 // shared memory of a batch CTA of one kind: the plane store, and for
-// decoding the staged word buffer (staged_w words per block at pitch NT + 1)
+// decoding the staged word buffer (staged_w words per block and the zero
+// rows after them, at pitch NT + 1)
 template <int NT, bool DECODE, int D, typename T>
 size_t batch_smem_bytes(uint32_t staged_w) {
   return ((size_t)NT * BatchSlots<DECODE, D, T>::value + (size_t)table_words<D>()) * 8 +
-         (DECODE ? (size_t)staged_w * (NT + 1) * 8 : 0);
+         (DECODE && staged_w ? (size_t)(staged_w + kPadRows) * (NT + 1) * 8 : 0);
 }
 
 template <int NT, bool DECODE, int D, typename T>

@@ -450,11 +450,14 @@ GZ_HD uint64_t decode_plane(uint32_t& n, uint32_t& bits, R& r) {
 // cost two clears and three adds; more ones loop.
 GZ_HD uint64_t rank_spread(uint64_t z) {
   const uint64_t z1 = z & (z - 1);
-  uint64_t z2 = z1 & (z1 - 1);
-  uint64_t S = z + z1 + (z2 << 1);
-  for (uint32_t j = 2; z2; j++) {
-    z2 &= z2 - 1;
-    S += z2 << j;
+  const uint64_t z2 = z1 & (z1 - 1);
+  const uint64_t z3 = z2 & (z2 - 1);
+  const uint64_t z4 = z3 & (z3 - 1);
+  uint64_t z5 = z4 & (z4 - 1);
+  uint64_t S = z + z1 + (z2 << 1) + (z3 << 2) + (z4 << 3) + (z5 << 4);
+  for (uint32_t j = 5; z5; j++) {
+    z5 &= z5 - 1;
+    S += z5 << j;
   }
   return S;
 }
@@ -728,39 +731,54 @@ GZ_HD int uncode_planes(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, Sto
 // and the test after it).  A warp's lanes step through tokens, not planes,
 // so a plane with many new ones in one lane does not hold the others at
 // that plane.  Same bits as uncode_planes<64>.
+// 32-bit helpers for the token loop: the low/high words of 64-bit values,
+// so that shifts by a variable amount are one funnel shift per word
+GZ_HD uint32_t fshr(uint32_t lo, uint32_t hi, uint32_t s) {  // (hi:lo) >> s, s < 32
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_r(lo, hi, s);
+#else
+  return s ? (lo >> s) | (hi << (32 - s)) : lo;
+#endif
+}
+
 template <class R, class StoreFn>
 GZ_HD int uncode_flat64(int k, int k_low, uint32_t& n, uint32_t& bits, R& r, StoreFn&& store) {
-  uint64_t x = 0;
+  uint32_t xl = 0, xh = 0;  // the plane being built
   uint32_t pos = n;
   bool grp = false;
-  // a group test of 1 that spends the budget still places a one (a run cut
-  // off after no zeros), so a pending group runs even with no bits left
   while (k >= k_low && (bits || grp)) {
-    const uint64_t w = r.peek64();
+    const uint64_t w64 = r.peek64();
+    const uint32_t wl = lo32(w64), wh = hi32(w64);
     uint32_t c;
     if (!grp) {  // verbatim bits, cut by the budget
       const uint32_t h = umin(n, bits);  // n <= 64
-      x = w & lowmask64(h);
+      // low h bits of w
+      xl = h >= 32 ? wl : wl & ((1u << h) - 1u);
+      xh = h >= 64 ? wh : h > 32 ? wh & ((1u << (h - 32)) - 1u) : 0u;
       c = h;
       pos = n;
     } else {  // zeros up to the next one, the last position or the budget's end
-      const uint32_t t = ctz64(w);
+      const uint32_t t = wl ? ctz32(wl) : 32 + ctz32(wh);
       const uint32_t lim = umin(63 - pos, bits);
       const bool read = t < lim;
       const uint32_t z = read ? t : lim;
       c = read ? t + 1 : lim;
-      x |= 1ull << (pos + z);
-      pos += z + 1;
+      const uint32_t p = pos + z;
+      const uint32_t b = 1u << (p & 31);
+      xl |= p < 32 ? b : 0u;
+      xh |= p < 32 ? 0u : b;
+      pos = p + 1;
     }
     const uint32_t rest = bits - c;
     const bool has_test = pos < 64 && rest > 0;  // c < 64 here
-    const bool test = has_test && ((w >> c) & 1);
+    const uint32_t tw = c < 32 ? wl : wh;
+    const bool test = has_test && ((tw >> (c & 31)) & 1u);
     c += has_test ? 1u : 0u;
     bits = rest - (has_test ? 1u : 0u);
     r.skip(c);
     grp = test;
     if (!test) {  // the plane is complete
-      store(k, x);
+      store(k, ((uint64_t)xh << 32) | xl);
       k--;
       n = pos;
     }
@@ -1429,20 +1447,14 @@ GZ_HD uint32_t encode_block_mode(const typename FT<T>::UInt* raw, const Mode& mo
   uint32_t n = 0;
   int k = P - 1;
   if constexpr (BS == 64 && P == 64) {
+    // the low halves wait in registers while the top 32 planes are coded
+    uint32_t lo[64];
 #pragma unroll
-    for (int i = 0; i < 32; i++)
-      ps.put(32 + i, (uint64_t)(uint32_t)u[2 * i] | ((uint64_t)u[2 * i + 1] << 32));
+    for (int i = 0; i < 64; i++) lo[i] = (uint32_t)u[i];
     planes_to_store<1>(u, ps);
     k = code_planes<BS>(k, kmin > 32 ? kmin : 32, n, bits, w,
                         [&](int kk) { return ps.get(kk - 32); });
     if (k >= kmin && bits) {
-      uint32_t lo[64];
-#pragma unroll
-      for (int i = 0; i < 32; i++) {
-        const uint64_t v = ps.get(32 + i);
-        lo[2 * i] = (uint32_t)v;
-        lo[2 * i + 1] = (uint32_t)(v >> 32);
-      }
       planes_to_store<0>(lo, ps);
       code_planes<BS>(k, kmin, n, bits, w, [&](int kk) { return ps.get(kk); });
     }
