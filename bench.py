@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--impl", default="gzfp", choices=["gzfp", "reference"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-batched", action="store_true",
+                   help="plain3d: leave out the batched workload's summary")
     p.add_argument("--edge", type=int, default=512,
                    help="cube edge of the field (smaller cases for profiling)")
     p.add_argument("--rate", type=float, default=16.0)
@@ -261,9 +263,10 @@ def batched_arrays(n_arrays: int, seed: int = 0):
     return specs
 
 
-def run_batched(args, rank, world, local):
+def run_batched(args, rank, world, local, emit=True):
     """512 mixed arrays: one graph-captured persistent launch per direction
-    against 512 plain launches per direction (same stream, device buffers)."""
+    against 512 plain launches per direction (same stream, device buffers).
+    Prints the result line when `emit`, and returns it (on rank 0)."""
     import torch
 
     import cuzfp_gb300 as gz
@@ -379,7 +382,9 @@ def run_batched(args, rank, world, local):
         "gpu_launches": 2 * (1 + len({dt for _, dt, _, _ in specs})) * args.steps,
         "clocks": clk.summary(),
     }
-    print(json.dumps(res), flush=True)
+    if emit:
+        print(json.dumps(res), flush=True)
+    return res
 
 
 # ------------------------------------------------------------ serving loop
@@ -848,6 +853,23 @@ def run(args, rank, world, local):
                "ms_per_step": round(e_ms, 3),
                "h2d_bytes_per_step": nbytes + sbytes, "d2h_bytes_per_step": sbytes + nbytes}
 
+    # the batched workload's summary (512 mixed arrays, graph-captured
+    # persistent launches against plain launches), so that one run records it
+    batched = None
+    if not args.no_batched:
+        bargs = argparse.Namespace(**vars(args))
+        bargs.steps, bargs.warmup = 5, 3
+        b = run_batched(bargs, rank, world, local, emit=False)
+        if b is not None:
+            batched = {"workload": b["config"]["workload"], "ms_per_step": b["ms_per_step"],
+                       "arrays_per_s": b["value"], "batched_gbs": b["batched_gbs"],
+                       "plain_ms_per_step": b["plain"]["ms_per_step"],
+                       "speedup_vs_plain": b["speedup_vs_plain"],
+                       "bit_identical": b["bit_identical"], "steps": bargs.steps,
+                       "compress_config": b["config"]["compress_config"],
+                       "decompress_config": b["config"]["decompress_config"]}
+        torch.cuda.empty_cache()
+
     if rank != 0:
         return
     peak, peak_kind = peaks()
@@ -904,6 +926,7 @@ def run(args, rank, world, local):
         "cpu_baseline": cpu,
         "parity": parity,
         "rate_distortion": distortion,
+        "batched": batched,
     }
     print(json.dumps(res), flush=True)
 
