@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true",
                    help="plain3d: leave out the batched workload's summary")
+    p.add_argument("--no-serving", action="store_true",
+                   help="plain3d: leave out the serving workload's summary")
     p.add_argument("--edge", type=int, default=512,
                    help="cube edge of the field (smaller cases for profiling)")
     p.add_argument("--rate", type=float, default=16.0)
@@ -403,9 +405,11 @@ def serving_requests(n: int, seed: int = 0):
              float(rates[i])) for i in range(n)]
 
 
-def run_serving(args, rank, world, local):
+def run_serving(args, rank, world, local, emit=True):
     """Poisson arrivals at 70% of the plain path's capacity through the
-    request server, against serial plain calls on the same requests."""
+    request server (device-queue mode, and the slot mode beside it), against
+    serial plain calls on the same requests.  Prints the result line when
+    `emit`, and returns it (on rank 0)."""
     import numpy as np
     import torch
 
@@ -496,25 +500,31 @@ def run_serving(args, rank, world, local):
                                             shape=(e, e, e), dtype=dts[dt], copy_to=cp))
         return out
 
+    # the device-queue server (one persistent kernel drains published
+    # requests) and, beside it, the slot server (a batch per free slot)
+    qcfg = gz.default_serve_config()
+    qcfg.budget_bytes = 40 << 30
+    qcfg.max_batch = args.max_batch
+    qcfg.device_queue = 1
     cfg = gz.default_serve_config()
     cfg.budget_bytes = 40 << 30
     cfg.max_inflight = args.inflight
     cfg.max_batch = args.max_batch
     with ClockSampler(local) as clk:
-        res, stats = gz.serve(requests(arrivals), cfg)
+        res, stats = gz.serve(requests(arrivals), qcfg)
     lat = np.array([r.completed - arrivals[i] for i, r in enumerate(res)])
     ok = all(r.status == 0 for r in res)
     # saturation: every request queued at time zero
-    sres, sstats = gz.serve(requests(np.zeros(n)), cfg)
+    sres, sstats = gz.serve(requests(np.zeros(n)), qcfg)
     torch.cuda.synchronize()
+    bit_q = ok and all(_same_bits(expect[i], check[i]) for i in sample)
+    res_s, stats_s = gz.serve(requests(arrivals), cfg)
+    lat_s = np.array([r.completed - arrivals[i] for i, r in enumerate(res_s)])
+    ssres, ssstats = gz.serve(requests(np.zeros(n)), cfg)
+    torch.cuda.synchronize()
+    ok = ok and all(r.status == 0 for r in res_s)
 
-    def same(a, b):
-        if a.dtype in (torch.float32, torch.float64):
-            it = torch.int32 if a.dtype == torch.float32 else torch.int64
-            return torch.equal(a.view(it), b.view(it))
-        return torch.equal(a, b)
-
-    bit_identical = ok and all(same(expect[i], check[i]) for i in sample)
+    bit_identical = bit_q and ok and all(_same_bits(expect[i], check[i]) for i in sample)
     if rank != 0:
         return
     p50, p99 = np.percentile(lat, 50), np.percentile(lat, 99)
@@ -528,7 +538,7 @@ def run_serving(args, rank, world, local):
                    "uncompressed_bytes": float(nbytes.sum()),
                    "l2": "inputs larger than L2 (a 384^3 field per dtype, ~2 GB of streams "
                          "per second of arrivals)",
-                   "server": {"max_batch": cfg.max_batch, "max_inflight": cfg.max_inflight}},
+                   "server": "device queue (one persistent kernel drains published requests)"},
         "latency_ms": {"p50": round(p50 * 1e3, 4), "p99": round(p99 * 1e3, 4),
                        "mean": round(float(lat.mean()) * 1e3, 4)},
         "plain_serial_latency_ms": {"p50": round(np.percentile(lat_plain, 50) * 1e3, 4),
@@ -538,10 +548,27 @@ def run_serving(args, rank, world, local):
         "plain_serial_gbs": round(plain_gbs, 2),
         "saturated_vs_plain": round(nbytes.sum() / sstats.wall / 1e9 / plain_gbs, 3),
         "stats": stats.as_dict(), "saturated_stats": sstats.as_dict(),
+        "slots": {"max_batch": cfg.max_batch, "max_inflight": cfg.max_inflight,
+                  "latency_ms": {"p50": round(np.percentile(lat_s, 50) * 1e3, 4),
+                                 "p99": round(np.percentile(lat_s, 99) * 1e3, 4)},
+                  "saturated_gbs": round(nbytes.sum() / ssstats.wall / 1e9, 2),
+                  "stats": stats_s.as_dict()},
         "bit_identical_sample": bool(bit_identical), "checked": len(sample),
         "gpu_launches": int(stats.kernels), "clocks": clk.summary(),
     }
+    if not emit:
+        return res_line
     print(json.dumps(res_line), flush=True)
+    return res_line
+
+
+def _same_bits(a, b):
+    """Two tensors equal bit for bit."""
+    import torch
+    if a.dtype in (torch.float32, torch.float64):
+        it = torch.int32 if a.dtype == torch.float32 else torch.int64
+        return torch.equal(a.view(it), b.view(it))
+    return torch.equal(a, b)
 
 
 def run_edges(args, rank, world, local):
@@ -869,6 +896,20 @@ def run(args, rank, world, local):
                        "compress_config": b["config"]["compress_config"],
                        "decompress_config": b["config"]["decompress_config"]}
         torch.cuda.empty_cache()
+    # the serving workload's summary (Poisson arrivals at 70% of plain-path
+    # capacity through the device-queue server)
+    serving = None
+    if not args.no_serving:
+        s = run_serving(argparse.Namespace(**vars(args)), rank, world, local, emit=False)
+        if s is not None:
+            serving = {"workload": s["config"]["workload"], "server": s["config"]["server"],
+                       "latency_ms": s["latency_ms"],
+                       "plain_serial_latency_ms": s["plain_serial_latency_ms"],
+                       "slots_latency_ms": s["slots"]["latency_ms"],
+                       "served_gbs": s["served_gbs"], "saturated_vs_plain": s["saturated_vs_plain"],
+                       "mean_inflight": round(s["stats"]["mean_inflight"], 3),
+                       "bit_identical_sample": s["bit_identical_sample"]}
+        torch.cuda.empty_cache()
 
     if rank != 0:
         return
@@ -927,6 +968,7 @@ def run(args, rank, world, local):
         "parity": parity,
         "rate_distortion": distortion,
         "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(res), flush=True)
 

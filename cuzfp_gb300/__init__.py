@@ -937,18 +937,25 @@ class ServeRequest(ctypes.Structure):
 
 
 class ServeResult(ctypes.Structure):
+    """gzfp_serve_result: host times of admission and completion; in the
+    device-queue mode also the device-clock span of the request's chunks."""
     _fields_ = [("admitted", ctypes.c_double), ("completed", ctypes.c_double),
-                ("output_bytes", _SZ), ("batch", _I), ("status", _I)]
+                ("output_bytes", _SZ), ("batch", _I), ("status", _I),
+                ("device_start", ctypes.c_double), ("device_end", ctypes.c_double)]
 
 
 class ServeConfig(ctypes.Structure):
+    """gzfp_serve_config: device_queue = 1 selects the device-queue mode
+    (3D float / double requests), idle_exit_us its kernel's wait limit."""
     _fields_ = [("budget_bytes", _SZ), ("max_batch", _I), ("max_inflight", _I),
-                ("compress_cfg", BatchConfig), ("decompress_cfg", BatchConfig)]
+                ("compress_cfg", BatchConfig), ("decompress_cfg", BatchConfig),
+                ("device_queue", _I), ("idle_exit_us", _U)]
 
 
 class ServeStats(ctypes.Structure):
     _fields_ = [("wall", ctypes.c_double), ("batches", _I), ("mean_batch", ctypes.c_double),
-                ("peak_bytes", _SZ), ("busy", ctypes.c_double), ("kernels", _I)]
+                ("peak_bytes", _SZ), ("busy", ctypes.c_double), ("kernels", _I),
+                ("mean_inflight", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {f: (float(getattr(self, f)) if t is ctypes.c_double else int(getattr(self, f)))

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "gzfp_batch_host.h"
+#include "gzfp_serve_host.h"
 
 namespace {
 
@@ -38,58 +39,10 @@ int scuda(cudaError_t e, const char* what) {
   return GZFP_ERR_CUDA;
 }
 
-constexpr size_t kAlign = 256;
+using gzfp::serve::Arena;
+using gzfp::serve::kAlign;
+using gzfp::serve::output_bytes;
 constexpr int kMaxInflight = 8;
-
-// First-fit allocator over one device arena; free ranges keyed by offset
-// and merged with their neighbours on release.
-class Arena {
- public:
-  explicit Arena(size_t size) : size_(size) { free_[0] = size; }
-  // offset of `bytes` (rounded up to kAlign), or SIZE_MAX if nothing fits
-  size_t alloc(size_t bytes) {
-    bytes = (bytes + kAlign - 1) / kAlign * kAlign;
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second < bytes) continue;
-      const size_t off = it->first, rest = it->second - bytes;
-      free_.erase(it);
-      if (rest) free_[off + bytes] = rest;
-      used_ += bytes;
-      peak_ = std::max(peak_, used_);
-      return off;
-    }
-    return SIZE_MAX;
-  }
-  void release(size_t off, size_t bytes) {
-    bytes = (bytes + kAlign - 1) / kAlign * kAlign;
-    used_ -= bytes;
-    auto it = free_.emplace(off, bytes).first;
-    auto next = std::next(it);
-    if (next != free_.end() && it->first + it->second == next->first) {
-      it->second += next->second;
-      free_.erase(next);
-    }
-    if (it != free_.begin()) {
-      auto prev = std::prev(it);
-      if (prev->first + prev->second == it->first) {
-        prev->second += it->second;
-        free_.erase(it);
-      }
-    }
-  }
-  size_t peak() const { return peak_; }
-
- private:
-  size_t size_, used_ = 0, peak_ = 0;
-  std::map<size_t, size_t> free_;
-};
-
-size_t output_bytes(const gzfp_serve_request& r) {
-  const unsigned ny = r.ny ? r.ny : 1, nz = r.nz ? r.nz : 1;
-  if (r.op == GZFP_SERVE_COMPRESS)
-    return gzfp_stream_size(r.type, r.nx, r.ny, r.nz, r.maxbits);
-  return (size_t)r.nx * ny * nz * gzfp::batch_scalar_size(r.type);
-}
 
 struct Slot {
   cudaStream_t s = nullptr;
@@ -106,6 +59,13 @@ using Clock = std::chrono::steady_clock;
 
 }  // namespace
 
+namespace gzfp {
+namespace serve {
+int serve_fail(int status, const char* msg) { return sfail(status, msg); }
+int serve_cuda(cudaError_t e, const char* what) { return scuda(e, what); }
+}  // namespace serve
+}  // namespace gzfp
+
 extern "C" {
 
 void gzfp_serve_default_config(gzfp_serve_config* cfg) {
@@ -115,6 +75,8 @@ void gzfp_serve_default_config(gzfp_serve_config* cfg) {
   cfg->max_inflight = 3;
   gzfp_batch_default_config(&cfg->compress_cfg);
   gzfp_batch_default_config(&cfg->decompress_cfg);
+  cfg->device_queue = 0;
+  cfg->idle_exit_us = 2000;
 }
 
 int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_config* cfg_in,
@@ -127,17 +89,21 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
   if (cfg_in) cfg = *cfg_in;
   if (cfg.max_batch < 1 || cfg.max_batch > 65535 || cfg.max_inflight < 1 ||
       cfg.max_inflight > kMaxInflight || cfg.budget_bytes < kAlign ||
-      !gzfp::bhost::valid_config(cfg.compress_cfg) || !gzfp::bhost::valid_config(cfg.decompress_cfg))
+      !gzfp::bhost::valid_config(cfg.compress_cfg) ||
+      !gzfp::bhost::valid_config(cfg.decompress_cfg) ||
+      (cfg.device_queue != 0 && cfg.device_queue != 1) || cfg.idle_exit_us < 1 ||
+      cfg.idle_exit_us > 10000000u)
     return sfail(GZFP_ERR_ARG, "bad server configuration");
   for (int i = 0; i < count; i++) {
     const gzfp_serve_request& r = reqs[i];
     if ((r.op != GZFP_SERVE_COMPRESS && r.op != GZFP_SERVE_DECOMPRESS) || !r.input ||
         !gzfp::batch_type_ok(r.type) || output_bytes(r) == 0)
       return sfail(GZFP_ERR_ARG, "bad request");
-    results[i] = gzfp_serve_result{0.0, 0.0, output_bytes(r), -1, GZFP_OK};
+    results[i] = gzfp_serve_result{0.0, 0.0, output_bytes(r), -1, GZFP_OK, 0.0, 0.0};
   }
   if (stats) memset(stats, 0, sizeof *stats);
   if (count == 0) return GZFP_OK;
+  if (cfg.device_queue) return gzfp::serve::serve_queue_run(reqs, count, cfg, results, stats);
 
   // requests in arrival order
   std::vector<int> order(count);
@@ -162,7 +128,8 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
   std::deque<int> queue;
   size_t next = 0;
   int completed = 0, batches = 0, kernels = 0;
-  long long batched_reqs = 0;
+  long long batched_reqs = 0, inflight_reqs = 0;
+  double inflight_sum = 0;
   double busy_time = 0, busy_since = -1;
   int inflight = 0;
   const Clock::time_point t0 = Clock::now();
@@ -185,6 +152,7 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
         arena.release(sl.offs[j], results[sl.reqs[j]].output_bytes);
       }
       completed += (int)sl.reqs.size();
+      inflight_reqs -= (long long)sl.reqs.size();
       sl.busy = false;
       if (--inflight == 0) busy_time += t - busy_since;
     }
@@ -267,6 +235,8 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
         sl.busy = true;
         sl.batch = batches++;
         batched_reqs += (long long)sl.reqs.size();
+        inflight_reqs += (long long)sl.reqs.size();  // each of them sees the whole batch
+        inflight_sum += (double)sl.reqs.size() * (double)inflight_reqs;
         const double ta = now();
         for (int r : sl.reqs) {
           results[r].admitted = ta;
@@ -294,6 +264,7 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
     stats->peak_bytes = arena.peak();
     stats->busy = stats->wall > 0 ? busy_time / stats->wall : 0.0;
     stats->kernels = kernels;
+    stats->mean_inflight = batched_reqs ? inflight_sum / (double)batched_reqs : 0.0;
   }
   return st;
 }

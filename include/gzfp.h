@@ -330,15 +330,29 @@ int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompre
 /* ------------------------------------------------------------ serving ---
    A request server.  Compress and decompress requests of mixed shape,
    scalar type and rate arrive over time.  A request is admitted once the
-   server's device-memory budget can hold its output.  Admitted requests are
-   coded together by the batched persistent kernel, and up to `max_inflight`
-   batches run on the device at once, each on its own stream: a request
-   that arrives while earlier batches run joins the next batch without
-   waiting for them (continuous batching).  Inputs stay resident in device
-   memory; outputs live in a device arena of `budget_bytes`, allocated once
-   per run, and are released when their batch completes (optionally after
-   a copy to a caller buffer).  No counterpart in cuZFP, whose calls are
-   synchronous and one array at a time (src/cuZFP/cuZFP.cu:174-269). */
+   server's device-memory budget can hold its output.  Inputs stay resident
+   in device memory; outputs live in a device arena of `budget_bytes`,
+   allocated once per run, and are released when their request completes
+   (optionally after a copy to a caller buffer).  Two modes:
+
+   * slots (device_queue = 0, the default; every scalar type and
+     dimensionality): admitted requests are coded together by the batched
+     persistent kernel, and up to `max_inflight` batches run on the device at
+     once, each on its own stream; a request that arrives while earlier
+     batches run joins the next batch on a free slot.
+   * device queue (device_queue = 1; 3D float and double requests): one
+     persistent kernel stays on the device and drains a request table in
+     pinned host memory that the GPU reads directly.  The host publishes an
+     admitted request by writing its descriptor and raising the published
+     chunk count; CTAs claim published chunks of blocks in order, so a
+     request that arrives while others run is coded as soon as CTAs free up,
+     alongside them, with no launch.  The kernel marks each request done in
+     host memory when its last chunk is coded.  Every wait of the kernel for
+     new work is bounded: after `idle_exit_us` without work its CTAs leave,
+     and the host relaunches it when new work is published.
+
+   No counterpart in cuZFP, whose calls are synchronous and one array at a
+   time (src/cuZFP/cuZFP.cu:174-269). */
 
 #define GZFP_SERVE_COMPRESS 0
 #define GZFP_SERVE_DECOMPRESS 1
@@ -354,28 +368,40 @@ typedef struct {
 } gzfp_serve_request;
 
 typedef struct {
-  double admitted;       /* seconds after the start: output memory granted, batch launched */
-  double completed;      /* seconds after the start: the request's batch finished */
+  double admitted;       /* seconds after the start: output memory granted, batch launched
+                            (device queue: request published) */
+  double completed;      /* seconds after the start: the request's batch finished
+                            (device queue: the kernel marked it done) */
   size_t output_bytes;
-  int batch;             /* index of the batch that ran it (-1 if never run) */
+  int batch;             /* index of the batch (device queue: the publication) that ran it,
+                            -1 if never run */
   int status;            /* GZFP_OK, or GZFP_ERR_CAPACITY for an output larger than the budget */
+  double device_start;   /* device queue: device clock, seconds after the run's first chunk,
+                            when the request's first chunk was claimed (0 in slot mode) */
+  double device_end;     /* device queue: the same, when its last chunk was done */
 } gzfp_serve_result;
 
 typedef struct {
   size_t budget_bytes;   /* device arena for request outputs */
-  int max_batch;         /* requests per batch (1..65535) */
-  int max_inflight;      /* batches on the device at once (1..8) */
-  gzfp_batch_config compress_cfg;   /* launch shapes (see gzfp_batch_autotune) */
+  int max_batch;         /* requests per batch or publication (1..65535) */
+  int max_inflight;      /* slot mode: batches on the device at once (1..8) */
+  gzfp_batch_config compress_cfg;   /* slot mode: launch shapes (see gzfp_batch_autotune) */
   gzfp_batch_config decompress_cfg;
+  int device_queue;      /* 0: slots; 1: device queue (3D float / double requests) */
+  unsigned idle_exit_us; /* device queue: the kernel's CTAs leave after this long without
+                            work (1..10^7 us; default 2000) */
 } gzfp_serve_config;
 
 typedef struct {
   double wall;           /* seconds from the start to the last completion */
-  int batches;
-  double mean_batch;     /* requests per batch */
+  int batches;           /* batches launched (device queue: publications) */
+  double mean_batch;     /* requests per batch (device queue: per publication) */
   size_t peak_bytes;     /* largest arena use */
-  double busy;           /* fraction of the run with at least one batch on the device */
-  int kernels;           /* kernels launched (chunk tables and per-kind persistent kernels) */
+  double busy;           /* fraction of the run with at least one request on the device */
+  int kernels;           /* kernels launched (slots: chunk tables and per-kind persistent
+                            kernels; device queue: launches of the persistent kernel) */
+  double mean_inflight;  /* requests on the device when a request is admitted, itself
+                            included, averaged over the admitted requests */
 } gzfp_serve_stats;
 
 void gzfp_serve_default_config(gzfp_serve_config* cfg);

@@ -109,3 +109,111 @@ def test_serve_bad_config(gz, cuda):
     cfg.max_inflight = 0
     with pytest.raises(gz.GzfpError):
         gz.serve([req], cfg)
+
+
+# ------------------------------------------------------- device-queue mode
+
+def _requests_3d(gz, cuda, rng, count, max_edge, gap, rates=(8.0, 12.5, 16.0, 32.0)):
+    """3D float / double compress and decompress requests (the kinds the
+    device queue serves) with resident inputs and a copy_to buffer each."""
+    import torch
+    reqs, expect, outs = [], [], []
+    t = 0.0
+    for _ in range(count):
+        shape = tuple(int(v) for v in rng.integers(1, max_edge, 3))
+        dt = torch.float32 if rng.random() < 0.5 else torch.float64
+        rate = float(rng.choice(rates))
+        walk = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+        x = torch.from_numpy(walk).to(dt).to(cuda)
+        w = gz.compress_tensor(x, rate)  # alone
+        t += float(rng.exponential(gap))
+        if rng.random() < 0.5:
+            out = torch.full_like(w, -1)
+            reqs.append(gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, rate, t, copy_to=out))
+            expect.append(w)
+        else:
+            y = gz.decompress_tensor(w, shape, dt, rate)  # alone
+            out = torch.full_like(y, float("nan"))
+            reqs.append(gz.serve_request(gz.GZFP_SERVE_DECOMPRESS, w, rate, t, shape=shape,
+                                         dtype=dt, copy_to=out))
+            expect.append(y)
+        outs.append(out)
+    torch.cuda.synchronize()
+    return reqs, expect, outs
+
+
+def _queue_config(gz, **kw):
+    cfg = gz.default_serve_config()
+    cfg.device_queue = 1
+    cfg.budget_bytes = 1 << 30
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def test_serve_queue_alone_equals_mix(gz, cuda):
+    """Requests published into the running persistent kernel give the bits
+    of plain calls, and their chunks overlap on the device."""
+    import torch
+    rng = np.random.default_rng(201)
+    reqs, expect, outs = _requests_3d(gz, cuda, rng, 200, 72, 15e-6)
+    res, stats = gz.serve(reqs, _queue_config(gz))
+    torch.cuda.synchronize()
+    for i, (r, e, o) in enumerate(zip(res, expect, outs)):
+        assert r.status == 0, i
+        assert r.completed >= r.admitted >= reqs[i].arrival - 1e-9, i
+        assert r.device_end >= r.device_start >= 0.0, i
+        assert _same(e, o), (i, reqs[i].op, reqs[i].nx, reqs[i].ny, reqs[i].nz, reqs[i].maxbits)
+    # device-clock spans: some request's chunks ran while another's did
+    spans = sorted((r.device_start, r.device_end) for r in res)
+    ends = np.maximum.accumulate([e for _, e in spans])
+    assert any(spans[i + 1][0] < ends[i] for i in range(len(spans) - 1))
+    assert stats.mean_inflight > 1.0
+    assert 1 <= stats.kernels
+    assert 0 < stats.peak_bytes <= 1 << 30
+
+
+def test_serve_queue_idle_limit(gz, cuda):
+    """Arrival gaps far longer than the kernel's wait limit: its CTAs leave
+    when the limit runs out (no work for idle_exit_us), the server launches
+    it again for the next request, and every result is still exact."""
+    import torch
+    rng = np.random.default_rng(202)
+    reqs, expect, outs = _requests_3d(gz, cuda, rng, 12, 40, 0.0)
+    for i, r in enumerate(reqs):
+        r.arrival = 0.005 * i  # 5 ms apart
+    res, stats = gz.serve(reqs, _queue_config(gz, idle_exit_us=200))
+    torch.cuda.synchronize()
+    assert all(r.status == 0 for r in res)
+    for e, o in zip(expect, outs):
+        assert _same(e, o)
+    assert stats.kernels >= 6  # the limit ran out between requests
+
+
+def test_serve_queue_budget_and_fifo(gz, cuda):
+    """A budget far below the offered outputs: requests wait for memory in
+    arrival order, the arena never exceeds the budget, and a request that
+    can never fit is refused without stalling the rest."""
+    import torch
+    rng = np.random.default_rng(203)
+    reqs, expect, outs = _requests_3d(gz, cuda, rng, 100, 40, 0.0)
+    big = torch.zeros((160, 160, 160), dtype=torch.float64, device=cuda)  # 32 MiB output
+    reqs.insert(50, gz.serve_request(gz.GZFP_SERVE_COMPRESS, big, 64.0, 0.0))
+    res, stats = gz.serve(reqs, _queue_config(gz, budget_bytes=2 << 20, max_batch=8))
+    torch.cuda.synchronize()
+    assert res[50].status == gz.GZFP_ERR_CAPACITY
+    rest = [r for i, r in enumerate(res) if i != 50]
+    assert all(r.status == 0 for r in rest)
+    for e, o in zip(expect, outs):
+        assert _same(e, o)
+    assert stats.peak_bytes <= 2 << 20
+    adm = [r.admitted for r in rest]
+    assert all(a <= b for a, b in zip(adm, adm[1:]))
+
+
+def test_serve_queue_rejects_other_kinds(gz, cuda):
+    import torch
+    x = torch.zeros((8, 8), dtype=torch.float32, device=cuda)
+    req = gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, 8.0, 0.0)
+    with pytest.raises(gz.GzfpError):
+        gz.serve([req], _queue_config(gz))
