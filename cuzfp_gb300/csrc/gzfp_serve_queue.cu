@@ -4,11 +4,12 @@
 // One persistent kernel stays on the device for the run and drains a request
 // table in pinned, device-mapped host memory:
 //
-//   host                                   device (every CTA, thread 0)
-//   write request r's descriptor           poll the published chunk count
-//   published += chunks of r  (release)    claim chunk c < published (CAS)
-//                                          find its request (forward cursor)
-//                                          code the chunk's blocks (all threads)
+//   host                                   device (every CTA)
+//   write request r's descriptor           take ticket c (atomicAdd)
+//   published += chunks of r  (release)    wait until c < published
+//                                          find its request (forward cursor),
+//                                          its descriptor (cached on the device)
+//                                          code the chunk's blocks
 //   poll done[r]                <--------  last chunk of r: done[r] = 1 (release)
 //
 // Chunks are numbered across requests in publication order and claimed in
@@ -19,10 +20,10 @@
 // code (batch_block), so its bits are those of a plain call.
 //
 // Waits are bounded: a CTA that finds no work for `idle_exit_us` leaves the
-// kernel (it holds no claim then: chunks are claimed only once published),
-// and the host relaunches the kernel when new work is published and the
-// previous launch has ended.  Only a few CTAs read the host-side counters;
-// the others read their mirror in device memory.
+// kernel, handing its ticket to the same CTA of the next launch, and the
+// host relaunches the kernel when new work is published and the previous
+// launch has ended.  Only the CTAs holding the next few tickets read the
+// host-side counters; the others read their mirror in device memory.
 #include <stdio.h>
 #include <string.h>
 
@@ -40,11 +41,10 @@ namespace gzfp {
 namespace {
 
 constexpr int kQThreads = 128;     // threads per CTA
-constexpr int kQBpt = 2;           // blocks per thread per chunk
-constexpr int kQChunk = kQThreads * kQBpt;
+constexpr int kQMaxBpt = 4;        // blocks per thread per chunk, at most
 constexpr int kQSlots = 32;        // plane-store slots (4^3 blocks)
 constexpr uint32_t kQStagedW = 32; // decode stages blocks of up to 32 words
-constexpr int kQPollers = 16;      // CTAs that read the host-side counters
+constexpr int kQPollers = 16;      // waiting CTAs that read the host-side counters
 
 // A published request: its descriptor in the batched path's form (first_chunk
 // in the run's chunk numbering), its chunk count and which coder runs it.
@@ -52,7 +52,11 @@ struct QueueReq {
   BatchDesc d;
   uint32_t nchunks;
   uint32_t code;  // 0 / 1: 3D float / double compress; 2 / 3: decompress
+  uint32_t bpt;   // blocks per thread of its chunks (1..kQMaxBpt)
+  uint32_t pad;
 };
+constexpr int kQReqWords = (int)(sizeof(QueueReq) / 8);
+static_assert(sizeof(QueueReq) % 8 == 0 && kQReqWords <= 32, "descriptor words");
 
 // host-mapped control words
 struct QueueCtl {
@@ -63,7 +67,7 @@ struct QueueCtl {
 
 // device-memory state
 struct QueueDev {
-  unsigned long long claim;      // next chunk to claim
+  unsigned long long ticket;     // next chunk to hand out
   unsigned long long published;  // mirror of QueueCtl::published
   unsigned int stop;             // mirror of QueueCtl::stop
 };
@@ -83,8 +87,21 @@ __device__ __forceinline__ unsigned ld_acquire_sys(const unsigned* p) {
   asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ void st_release_sys(unsigned* p, unsigned v) {
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 template <typename X>
 __device__ __forceinline__ X ld_vol(const X* p) {
@@ -95,8 +112,41 @@ size_t queue_smem_bytes() {
   return (size_t)kQSlots * kQThreads * 8 + (size_t)(kQStagedW + kPadRows) * (kQThreads + 1) * 8;
 }
 
+// A request's (first chunk, chunk count), from the device copy of its
+// descriptor once one CTA has made it, else from host memory.
+__device__ __forceinline__ void req_range(const QueueReq* reqs, const QueueReq* dreqs,
+                                          const unsigned* ready, uint32_t r,
+                                          unsigned long long& first, unsigned& n) {
+  if (ld_acquire_gpu(&ready[r])) {
+    first = ld_relaxed_gpu((const unsigned long long*)&dreqs[r].d.first_chunk);
+    n = (unsigned)ld_relaxed_gpu((const unsigned long long*)&dreqs[r].nchunks);
+  } else {
+    first = ld_vol(&reqs[r].d.first_chunk);
+    n = ld_vol(&reqs[r].nchunks);
+  }
+}
+
+// One chunk's blocks of one request, per coder: separate functions, so that
+// each gets its own register allocation inside the kernel's budget.
+template <bool DECODE, typename T>
+__device__ __noinline__ void queue_chunk(const BatchDesc& d, uint64_t first, int bpt,
+                                         uint64_t* smem_planes, uint64_t* sbuf) {
+  BatchPlanes<kQThreads> ps{smem_planes + threadIdx.x, nullptr};
+#pragma unroll 1
+  for (int j = 0; j < bpt; j++)
+    batch_block<kQThreads, DECODE, 3, T>(d, first + (uint64_t)j * kQThreads + threadIdx.x, ps,
+                                         sbuf, kQStagedW);
+}
+
+// Tickets: a CTA takes the next chunk number with one atomicAdd and waits
+// until the host has published that chunk, so chunks are handed out in
+// order with no retries.  A CTA that reaches the idle limit while holding a
+// ticket leaves it in abandoned[blockIdx.x]; the same CTA of the next
+// launch (the grid does not change within a run) takes it up first, so
+// every chunk is coded exactly once.
 __global__ void __launch_bounds__(kQThreads, 3)
-    serve_queue_kernel(const QueueReq* reqs, QueueCtl* ctl, unsigned* done, QueueDev* dev,
+    serve_queue_kernel(const QueueReq* reqs, QueueReq* dreqs, unsigned* ready, QueueCtl* ctl,
+                       unsigned* done, QueueDev* dev, unsigned long long* abandoned,
                        unsigned* finished, unsigned long long* t_first,
                        unsigned long long* t_last, unsigned long long idle_ns, uint32_t r0) {
   extern __shared__ uint64_t smem[];
@@ -106,40 +156,53 @@ __global__ void __launch_bounds__(kQThreads, 3)
   __shared__ int s_cmd;
   BatchPlanes<kQThreads> ps{smem + threadIdx.x, nullptr};
   uint64_t* sbuf = smem + kQSlots * kQThreads;
-  uint32_t r = r0;    // thread 0: request of the last claimed chunk (r0: none earlier is left)
-  bool have = false;  // thread 0: s_req holds request r
+  uint32_t r = r0;              // thread 0: request of the last chunk (none before r0 is left)
+  uint32_t loaded = 0xffffffffu;  // every thread: the request s_req holds
+  bool held = false;            // thread 0: holds ticket t
+  unsigned long long t = 0;
+  if (threadIdx.x == 0) {
+    t = abandoned[blockIdx.x];
+    if (t != ~0ull) {
+      abandoned[blockIdx.x] = ~0ull;
+      held = true;
+    }
+  }
   for (;;) {
     if (threadIdx.x == 0) {
-      // claim a published chunk; leave when stopped with nothing left, or
-      // after idle_ns without work
+      if (!held) {
+        t = atomicAdd(&dev->ticket, 1ull);
+        held = true;
+      }
+      // wait until chunk t is published; leave when stopped (it never will
+      // be) or after idle_ns (handing the ticket on)
       int cmd = 0;
       const unsigned long long t0 = globaltimer();
       unsigned nap = 64;
       for (;;) {
+        // the CTAs holding the next kQPollers tickets -- the ones a new
+        // request will start on -- read the host's count; the others its
+        // mirror
         unsigned long long p = ld_vol(&dev->published);
-        if (blockIdx.x < kQPollers) {
+        const bool poller = t >= p && t < p + kQPollers;
+        if (poller) {
           const unsigned long long hp = ld_acquire_sys(&ctl->published);
           if (hp > p) {
             atomicMax(&dev->published, hp);
             p = hp;
           }
         }
-        const unsigned long long c = ld_vol(&dev->claim);
-        if (c < p) {
-          if (atomicCAS(&dev->claim, c, c + 1) == c) {
-            s_chunk = c;
-            cmd = 1;
-            break;
-          }
-          continue;
+        if (t < p) {
+          cmd = 1;
+          break;
         }
         unsigned stop = ld_vol(&dev->stop);
-        if (!stop && blockIdx.x < kQPollers && ld_acquire_sys(&ctl->stop)) {
+        if (!stop && poller && ld_acquire_sys(&ctl->stop)) {
           atomicExch(&dev->stop, 1u);
           stop = 1;
         }
         if (stop) break;
         if (globaltimer() - t0 > idle_ns) {
+          abandoned[blockIdx.x] = t;
           cmd = 2;
           break;
         }
@@ -147,23 +210,18 @@ __global__ void __launch_bounds__(kQThreads, 3)
         nap = nap < 2048 ? 2 * nap : nap;
       }
       if (cmd == 1) {
-        // the chunk's request: requests are numbered in publication order,
-        // and one CTA's claims only grow, so the cursor moves forward
-        const unsigned long long c = s_chunk;
+        held = false;
+        // the chunk's request: requests are numbered in publication order and
+        // one CTA's tickets only grow, so the cursor moves forward
         for (;;) {
-          const unsigned long long f = ld_vol(&reqs[r].d.first_chunk);
-          const unsigned n = ld_vol(&reqs[r].nchunks);
-          if (c < f + n) break;
+          unsigned long long f;
+          unsigned n;
+          req_range(reqs, dreqs, ready, r, f, n);
+          if (t < f + n) break;
           r++;
-          have = false;
-        }
-        if (!have) {  // (the table, `finished`, `done` and the stamps are in publication order)
-          const unsigned long long* src = (const unsigned long long*)&reqs[r];
-          unsigned long long* dst = (unsigned long long*)&s_req;
-          for (int i = 0; i < (int)(sizeof(QueueReq) / 8); i++) dst[i] = ld_vol(src + i);
-          have = true;
         }
         s_r = r;
+        s_chunk = t;
         atomicMin(&t_first[r], globaltimer());
       }
       s_cmd = cmd;
@@ -174,21 +232,43 @@ __global__ void __launch_bounds__(kQThreads, 3)
       if (cmd == 2 && threadIdx.x == 0) atomicAdd_system(&ctl->idle_exits, 1u);
       return;
     }
-    const QueueReq& q = s_req;
-    const uint64_t first = (s_chunk - q.d.first_chunk) * (uint64_t)kQChunk;
-#pragma unroll 1
-    for (int j = 0; j < kQBpt; j++) {
-      const uint64_t b = first + (uint64_t)j * kQThreads + threadIdx.x;
-      switch (q.code) {
-        case 0: batch_block<kQThreads, false, 3, float>(q.d, b, ps, sbuf, kQStagedW); break;
-        case 1: batch_block<kQThreads, false, 3, double>(q.d, b, ps, sbuf, kQStagedW); break;
-        case 2: batch_block<kQThreads, true, 3, float>(q.d, b, ps, sbuf, kQStagedW); break;
-        default: batch_block<kQThreads, true, 3, double>(q.d, b, ps, sbuf, kQStagedW); break;
+    const uint32_t rr = s_r;
+    if (rr != loaded) {
+      // the descriptor: from its device copy, or from host memory with one
+      // word per thread (then copied to the device for the other CTAs)
+      if (threadIdx.x < 32) {
+        const bool rd = ld_acquire_gpu(&ready[rr]) != 0;
+        const unsigned lane = threadIdx.x;
+        if (lane < (unsigned)kQReqWords) {
+          unsigned long long v;
+          if (rd) {
+            v = ld_relaxed_gpu((const unsigned long long*)&dreqs[rr] + lane);
+          } else {
+            v = ld_vol((const unsigned long long*)&reqs[rr] + lane);
+            ((unsigned long long*)&dreqs[rr])[lane] = v;
+          }
+          ((unsigned long long*)&s_req)[lane] = v;
+        }
+        __syncwarp();
+        if (!rd && lane == 0) {
+          __threadfence();
+          st_release_gpu(&ready[rr], 1u);
+        }
       }
+      __syncthreads();
+      loaded = rr;
+    }
+    const QueueReq& q = s_req;
+    const int bpt = (int)q.bpt;
+    const uint64_t first = (s_chunk - q.d.first_chunk) * (uint64_t)(kQThreads * bpt);
+    switch (q.code) {
+      case 0: queue_chunk<false, float>(q.d, first, bpt, smem, sbuf); break;
+      case 1: queue_chunk<false, double>(q.d, first, bpt, smem, sbuf); break;
+      case 2: queue_chunk<true, float>(q.d, first, bpt, smem, sbuf); break;
+      default: queue_chunk<true, double>(q.d, first, bpt, smem, sbuf); break;
     }
     __syncthreads();  // the chunk's blocks are written
     if (threadIdx.x == 0) {
-      const uint32_t rr = s_r;
       __threadfence();  // this CTA's writes before its count
       const unsigned old = atomicAdd(&finished[rr], 1u);
       atomicMax(&t_last[rr], globaltimer());
@@ -197,7 +277,7 @@ __global__ void __launch_bounds__(kQThreads, 3)
         st_release_sys(&done[rr], 1u);
       }
     }
-    __syncthreads();  // s_req and s_chunk are rewritten next
+    // s_chunk / s_r are rewritten only after the next __syncthreads
   }
 }
 
@@ -222,6 +302,9 @@ struct QueueRun {
   unsigned* h_done = nullptr;
   unsigned* d_done = nullptr;
   QueueDev* dev = nullptr;
+  QueueReq* dreqs = nullptr;               // device copies of the descriptors
+  unsigned* ready = nullptr;               // dreqs[i] is filled in
+  unsigned long long* abandoned = nullptr; // per CTA: a ticket handed to the next launch
   unsigned* finished = nullptr;
   unsigned long long* t_first = nullptr;
   unsigned long long* t_last = nullptr;
@@ -237,6 +320,9 @@ struct QueueRun {
     if (cs) cudaStreamDestroy(cs);
     cudaFree(arena);
     cudaFree(dev);
+    cudaFree(dreqs);
+    cudaFree(ready);
+    cudaFree(abandoned);
     cudaFree(finished);
     cudaFree(t_first);
     cudaFree(t_last);
@@ -280,6 +366,9 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
       (e = host_mapped(&q.h_ctl, &q.d_ctl, 1)) ||
       (e = host_mapped(&q.h_done, &q.d_done, (size_t)count)) ||
       (e = cudaMalloc(&q.dev, sizeof(QueueDev))) ||
+      (e = cudaMalloc(&q.dreqs, count * sizeof(QueueReq))) ||
+      (e = cudaMalloc(&q.ready, count * sizeof(unsigned))) ||
+      (e = cudaMalloc(&q.abandoned, grid * sizeof(unsigned long long))) ||
       (e = cudaMalloc(&q.finished, count * sizeof(unsigned))) ||
       (e = cudaMalloc(&q.t_first, count * sizeof(unsigned long long))) ||
       (e = cudaMalloc(&q.t_last, count * sizeof(unsigned long long))) ||
@@ -287,6 +376,8 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
       (e = cudaStreamCreateWithFlags(&q.cs, cudaStreamNonBlocking)) ||
       (e = cudaEventCreateWithFlags(&q.kdone, cudaEventDisableTiming)) ||
       (e = cudaMemsetAsync(q.dev, 0, sizeof(QueueDev), q.ks)) ||
+      (e = cudaMemsetAsync(q.ready, 0, count * sizeof(unsigned), q.ks)) ||
+      (e = cudaMemsetAsync(q.abandoned, 0xff, grid * sizeof(unsigned long long), q.ks)) ||
       (e = cudaMemsetAsync(q.finished, 0, count * sizeof(unsigned), q.ks)) ||
       (e = cudaMemsetAsync(q.t_first, 0xff, count * sizeof(unsigned long long), q.ks)) ||
       (e = cudaMemsetAsync(q.t_last, 0, count * sizeof(unsigned long long), q.ks)) ||
@@ -296,9 +387,9 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
   const unsigned long long idle_ns = 1000ull * cfg.idle_exit_us;
   std::vector<int> req_of(count), pub_of(count, -1);  // publication <-> request
   auto launch = [&](uint32_t r0) -> cudaError_t {
-    serve_queue_kernel<<<grid, kQThreads, smem, q.ks>>>(q.d_reqs, q.d_ctl, q.d_done, q.dev,
-                                                        q.finished, q.t_first, q.t_last,
-                                                        idle_ns, r0);
+    serve_queue_kernel<<<grid, kQThreads, smem, q.ks>>>(
+        q.d_reqs, q.dreqs, q.ready, q.d_ctl, q.d_done, q.dev, q.abandoned, q.finished, q.t_first,
+        q.t_last, idle_ns, r0);
     cudaError_t le = cudaGetLastError();
     return le ? le : cudaEventRecord(q.kdone, q.ks);
   };
@@ -400,7 +491,12 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
       e_r.d.in = rq.input;           // the field (compress) or stream words (decompress)
       e_r.d.out = q.arena + off;     // the stream words or the field
       e_r.d.first_chunk = published;
-      e_r.nchunks = (uint32_t)((e_r.d.g.nblocks + kQChunk - 1) / kQChunk);
+      // chunks small enough that a request of under a few waves of blocks
+      // still spreads over every CTA, larger for large requests
+      const uint64_t wave = (uint64_t)grid * kQThreads;
+      e_r.bpt = (uint32_t)std::min<uint64_t>(kQMaxBpt, std::max<uint64_t>(1, e_r.d.g.nblocks / wave));
+      const uint64_t chunk = (uint64_t)kQThreads * e_r.bpt;
+      e_r.nchunks = (uint32_t)((e_r.d.g.nblocks + chunk - 1) / chunk);
       e_r.code = (decode ? 2u : 0u) + (rq.type == GZFP_TYPE_DOUBLE ? 1u : 0u);
       if (!decode && rq.maxbits % 64) {
         // blocks that share words are merged with atomic ORs: zero the
