@@ -705,7 +705,9 @@ def run_accuracy(args, rank, world, local):
     enc_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
     dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
     ms_per_step = max_over_ranks(enc_ms + dec_ms, world, dev)
-    # the serial walk, on a small field
+    # the serial walk, on a small field (too few blocks for the parallel
+    # index), and the parallel index of the whole stream, checked against
+    # the compressor's start bits
     small = synth.sinusoids_device((64, 64, 64), 16, 32, seed=rank, dtype=torch.float64,
                                    device=dev)
     sw = gz.compress_mode(small, mode, cuda_stream=stream)
@@ -716,6 +718,13 @@ def run_accuracy(args, rank, world, local):
     b.record(stream)
     b.synchronize()
     walk_us = a.elapsed_time(b) * 1e3 / (16 ** 3)
+    idx = gz.index_blocks(words, SHAPE, torch.float64, mode, cuda_stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = gz.index_blocks(words, SHAPE, torch.float64, mode, cuda_stream=stream)
+    torch.cuda.synchronize()
+    index_ms = (time.perf_counter() - t0) * 1e3
+    index_ok = bool(torch.equal(idx, offs))
     if rank != 0:
         return
     peak, peak_kind = peaks()
@@ -743,6 +752,9 @@ def run_accuracy(args, rank, world, local):
                      "frac": round(2 * alg / (ms_per_step * 1e-3) / 1e9 / peak, 4),
                      "traffic": None},
         "block_walk_us_per_block": round(walk_us, 3),
+        "parallel_index": {"ms": round(index_ms, 3), "blocks": int(offs.numel()),
+                           "equal_to_compressor_offsets": index_ok,
+                           "serial_walk_estimate_ms": round(walk_us * offs.numel() / 1e3, 1)},
         "gpu_launches": 6 * args.steps,
         "clocks": clk.summary(),
     }

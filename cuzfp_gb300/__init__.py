@@ -759,8 +759,10 @@ def decompress_mode(words, shape, dtype, mode: Mode, offsets=None, out=None,
 
 
 def index_blocks(words, shape, dtype, mode: Mode, cuda_stream: Any = None):
-    """Every block's start bit in a stream written under `mode` (one GPU
-    thread walks the blocks)."""
+    """Every block's start bit in a stream written under `mode`: walkers over
+    segments of the stream whose block chains are joined where they merge
+    (one GPU thread walks short streams, and any stream whose chains do not
+    merge)."""
     t = _type_of(dtype)
     nx, ny, nz = _dims_of(shape)
     nb = _nblocks(shape)

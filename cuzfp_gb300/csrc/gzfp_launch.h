@@ -68,6 +68,37 @@ uint32_t block_bound_host(int dims, int P, int ebits, const General& mode);
 // offsets[b] = first + b * maxbits: the start bits of a fixed-rate stream
 cudaError_t launch_fixed_offsets(unsigned long long* offsets, uint64_t n, uint64_t first,
                                  uint32_t maxbits, cudaStream_t s);
+// Parallel index of a general-mode stream (gzfp_modes.cuh): walkers over
+// segments of the stream, their extensions up to the chain they merge with,
+// and the assembly of the true chain's pieces into the block offsets.
+struct IndexJob {
+  const uint64_t* in;
+  uint64_t nwords;
+  General mode;
+  uint64_t first;                // bit of block 0
+  uint64_t seg_bits;             // segment length
+  uint32_t nseg, cap;            // segments, positions a segment's list holds
+  uint32_t ext_cap;              // steps an extension may take
+  unsigned long long* lists;     // nseg * cap block starts, in stream order
+  unsigned long long* counts;    // per segment: entries in its list (cap + 1: overflow)
+  unsigned long long* exits;     // per segment: the walker's first start past its end
+  unsigned long long* info;      // per segment: extension steps, merge segment, merge
+                                 // index, status (0 merged, 1 stream end, 2 failed)
+};
+struct IndexPiece {
+  unsigned long long src;    // list piece: entry index in `lists`
+  unsigned long long count;  // starts in the piece
+  unsigned long long dst;    // index of its first start in the offsets
+  unsigned long long seg;    // walk piece: the segment whose extension it re-walks
+  unsigned long long walk;   // 1: walk piece, 0: list piece
+};
+template <typename T>
+cudaError_t launch_index_walk(int dims, const IndexJob& j, bool extend, cudaStream_t s);
+template <typename T>
+cudaError_t launch_index_assemble(int dims, const IndexJob& j, const IndexPiece* pieces,
+                                  uint32_t npieces, unsigned long long* offsets, uint64_t nblocks,
+                                  unsigned long long* end, cudaStream_t s);
+
 cudaError_t launch_place_blocks(const uint64_t* scratch, uint32_t slot_words,
                                 const uint32_t* lengths, const unsigned long long* offsets,
                                 uint64_t nblocks, uint64_t* out, cudaStream_t s);

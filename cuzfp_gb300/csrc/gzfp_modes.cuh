@@ -8,9 +8,10 @@
 // into its own scratch slot and its length recorded; an exclusive scan of
 // the lengths gives every block's start bit; every block's bits are then
 // moved to that position.  Decompression decodes every block from its start
-// bit when the offsets are known (the compressor returns them); otherwise a
-// single thread first walks the blocks to find them, which is serial in the
-// number of blocks.
+// bit when the offsets are known (the compressor returns them); otherwise
+// the starts are found first, by walkers over segments of the stream whose
+// chains are joined where they merge (below), or, failing that, by a single
+// thread walking every block in order.
 #pragma once
 
 #include "gzfp_kernels.cuh"
@@ -95,6 +96,115 @@ __global__ void index_blocks_kernel(const uint64_t* __restrict__ in, uint64_t nw
   *end = pos;
 }
 
+// ---------------------------------------------------------- parallel index
+// A block's length is known only by parsing it, so the block starts of a
+// stream without offsets form a chain p -> p + block_bits(p) from block 0.
+// A chain started at any other bit soon lands on a start of the true chain
+// (on fixed-accuracy streams of smooth fields, after a few hundred to a few
+// thousand blocks), and from there on the two are the same chain.  So:
+//  1. one walker per segment of the stream records the chain from the
+//     segment's first bit to its end (index_walk_kernel, extend = false);
+//  2. each walker goes on past its end until its chain reaches a start that
+//     a later segment's walker recorded (extend = true): the merge;
+//  3. the host follows the merges from segment 0, whose walker starts at
+//     block 0, and index_assemble_kernel copies the true chain's pieces --
+//     list entries, and re-walked extensions -- into the offsets.
+// A walker whose list overflows or whose extension does not merge within
+// ext_cap steps makes the host fall back to the serial walk.
+
+GZ_HD uint64_t index_step_bits(uint32_t bits) { return bits ? bits : 1; }
+
+template <int D, typename T>
+__global__ void index_walk_kernel(IndexJob j, bool extend) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= j.nseg) return;
+  const uint64_t total = j.nwords * 64;
+  const DevWords words{nullptr, j.in, j.nwords};
+  if (!extend) {
+    const uint64_t lo = j.first + (uint64_t)s * j.seg_bits, hi = lo + j.seg_bits;
+    uint64_t p = lo, n = 0;
+    unsigned long long* list = j.lists + (uint64_t)s * j.cap;
+    while (p < hi && p < total) {
+      if (n == j.cap) {  // more starts than the list holds
+        n = j.cap + 1ull;
+        break;
+      }
+      list[n++] = p;
+      BitReader<DevWords> r(words, p);
+      p += index_step_bits(block_bits<D, T>(r, j.mode));
+    }
+    j.counts[s] = n;
+    j.exits[s] = p;
+    return;
+  }
+  // extension: from the walker's exit to the first start recorded by a
+  // later segment
+  uint64_t p = j.exits[s], steps = 0, k = s + 1, idx = 0;
+  unsigned long long status = 2;
+  if (j.counts[s] <= j.cap) {
+    for (;;) {
+      if (p >= total || k >= j.nseg) {
+        status = 1;
+        break;
+      }
+      while (k + 1 < j.nseg && p >= j.first + (k + 1) * j.seg_bits) k++;
+      const unsigned long long n = j.counts[k];
+      if (n > j.cap) break;  // that list overflowed: no merge can be trusted
+      const unsigned long long* list = j.lists + k * j.cap;
+      uint64_t lo = 0, hi = n;  // first entry >= p
+      while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (list[mid] < p) lo = mid + 1; else hi = mid;
+      }
+      if (lo < n && list[lo] == p) {
+        idx = lo;
+        status = 0;
+        break;
+      }
+      if (steps == j.ext_cap) break;
+      steps++;
+      BitReader<DevWords> r(words, p);
+      p += index_step_bits(block_bits<D, T>(r, j.mode));
+    }
+  }
+  unsigned long long* inf = j.info + 4ull * s;
+  inf[0] = steps;
+  inf[1] = k;
+  inf[2] = idx;
+  inf[3] = status;
+}
+
+// one CTA per piece: list pieces are copied by all threads, walk pieces
+// re-walk an extension on one thread; offsets past nblocks are dropped
+template <int D, typename T>
+__global__ void index_assemble_kernel(IndexJob j, const IndexPiece* pieces,
+                                      unsigned long long* offsets, uint64_t nblocks) {
+  const IndexPiece pc = pieces[blockIdx.x];
+  if (!pc.walk) {
+    for (uint64_t i = threadIdx.x; i < pc.count && pc.dst + i < nblocks; i += blockDim.x)
+      offsets[pc.dst + i] = j.lists[pc.src + i];
+    return;
+  }
+  if (threadIdx.x != 0) return;
+  const DevWords words{nullptr, j.in, j.nwords};
+  uint64_t p = j.exits[pc.seg];
+  for (uint64_t i = 0; i < pc.count && pc.dst + i < nblocks; i++) {
+    offsets[pc.dst + i] = p;
+    BitReader<DevWords> r(words, p);
+    p += index_step_bits(block_bits<D, T>(r, j.mode));
+  }
+}
+
+// the bit after the last block
+template <int D, typename T>
+__global__ void index_end_kernel(IndexJob j, const unsigned long long* offsets, uint64_t nblocks,
+                                 unsigned long long* end) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const uint64_t p = offsets[nblocks - 1];
+  BitReader<DevWords> r(DevWords{nullptr, j.in, j.nwords}, p);
+  *end = p + block_bits<D, T>(r, j.mode);
+}
+
 template <int D, typename T>
 cudaError_t launch_encode_mode_t(const T* in, const Geom& g, const General& mode,
                                  uint64_t* scratch, uint32_t slot_words, uint32_t* lengths,
@@ -143,6 +253,46 @@ cudaError_t launch_decode_mode(int dims, const uint64_t* in, uint64_t nwords,
     case 1: return launch_decode_mode_t<1, T>(in, nwords, offsets, g, mode, out, s);
     case 2: return launch_decode_mode_t<2, T>(in, nwords, offsets, g, mode, out, s);
     case 3: return launch_decode_mode_t<3, T>(in, nwords, offsets, g, mode, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int D, typename T>
+cudaError_t launch_index_walk_t(const IndexJob& j, bool extend, cudaStream_t s) {
+  const unsigned threads = 64;
+  index_walk_kernel<D, T><<<(j.nseg + threads - 1) / threads, threads, 0, s>>>(j, extend);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_index_walk(int dims, const IndexJob& j, bool extend, cudaStream_t s) {
+  switch (dims) {
+    case 1: return launch_index_walk_t<1, T>(j, extend, s);
+    case 2: return launch_index_walk_t<2, T>(j, extend, s);
+    case 3: return launch_index_walk_t<3, T>(j, extend, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int D, typename T>
+cudaError_t launch_index_assemble_t(const IndexJob& j, const IndexPiece* pieces, uint32_t npieces,
+                                    unsigned long long* offsets, uint64_t nblocks,
+                                    unsigned long long* end, cudaStream_t s) {
+  index_assemble_kernel<D, T><<<npieces, 128, 0, s>>>(j, pieces, offsets, nblocks);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  index_end_kernel<D, T><<<1, 1, 0, s>>>(j, offsets, nblocks, end);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_index_assemble(int dims, const IndexJob& j, const IndexPiece* pieces,
+                                  uint32_t npieces, unsigned long long* offsets, uint64_t nblocks,
+                                  unsigned long long* end, cudaStream_t s) {
+  switch (dims) {
+    case 1: return launch_index_assemble_t<1, T>(j, pieces, npieces, offsets, nblocks, end, s);
+    case 2: return launch_index_assemble_t<2, T>(j, pieces, npieces, offsets, nblocks, end, s);
+    case 3: return launch_index_assemble_t<3, T>(j, pieces, npieces, offsets, nblocks, end, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -6,7 +6,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "gzfp.h"
 #include "gzfp_host.h"
@@ -26,6 +28,8 @@ struct ModeSpace {
   void* sums = nullptr;     size_t sums_cap = 0;      // scan partials + total; walk end
   void* field = nullptr;    size_t field_cap = 0;     // staged host field
   void* stream = nullptr;   size_t stream_cap = 0;    // staged host stream
+  void* index = nullptr;    size_t index_cap = 0;     // parallel index: lists and per-segment state
+  void* pieces = nullptr;   size_t pieces_cap = 0;    // parallel index: the true chain's pieces
 };
 ModeSpace g_mode[kMaxDevices];
 
@@ -117,12 +121,105 @@ cudaError_t index_launch(int type, int dims, const uint64_t* in, uint64_t nwords
   }
 }
 
+// The block starts of a device stream by the parallel index
+// (gzfp_modes.cuh): walkers over segments of the stream, joined where their
+// chains merge.  Returns false, with nothing written that counts, when a
+// list overflows or a chain does not merge; the caller then walks serially.
+bool parallel_index(ModeSpace& ms, int type, int dims, const uint64_t* words, uint64_t nwords,
+                    uint64_t nblocks, const gzfp::General& mode, uint64_t first,
+                    uint64_t& end_bit, cudaStream_t s, cudaError_t& err) {
+  err = cudaSuccess;
+  const uint64_t total = nwords * 64;
+  if (nblocks < 4096 || first >= total) return false;  // short streams: the serial walk
+  gzfp::IndexJob j{};
+  j.in = words;
+  j.nwords = nwords;
+  j.mode = mode;
+  j.first = first;
+  j.nseg = (uint32_t)std::min<uint64_t>(4096, nblocks / 1024);
+  j.seg_bits = (total - first + j.nseg - 1) / j.nseg;
+  j.cap = (uint32_t)(4 * ((nblocks + j.nseg - 1) / j.nseg) + 256);
+  j.ext_cap = 16384;
+  const size_t nseg = j.nseg;
+  const size_t bytes = (nseg * j.cap + 7 * nseg) * 8;
+  if ((err = reserve(ms.index, ms.index_cap, bytes))) return false;
+  j.lists = (unsigned long long*)ms.index;
+  j.counts = j.lists + nseg * j.cap;
+  j.exits = j.counts + nseg;
+  j.info = j.exits + nseg;
+  auto walk = [&](bool extend) {
+    switch (type) {
+      case GZFP_TYPE_FLOAT: return gzfp::launch_index_walk<float>(dims, j, extend, s);
+      case GZFP_TYPE_DOUBLE: return gzfp::launch_index_walk<double>(dims, j, extend, s);
+      case GZFP_TYPE_INT32: return gzfp::launch_index_walk<int32_t>(dims, j, extend, s);
+      default: return gzfp::launch_index_walk<int64_t>(dims, j, extend, s);
+    }
+  };
+  std::vector<unsigned long long> state(6 * nseg);  // counts, info (exits are not needed)
+  if ((err = walk(false)) || (err = walk(true)) ||
+      (err = cudaMemcpyAsync(state.data(), j.counts, nseg * 8, cudaMemcpyDeviceToHost, s)) ||
+      (err = cudaMemcpyAsync(state.data() + 2 * nseg, j.info, 4 * nseg * 8,
+                             cudaMemcpyDeviceToHost, s)) ||
+      (err = cudaStreamSynchronize(s)))
+    return false;
+  const unsigned long long* counts = state.data();
+  const unsigned long long* info = state.data() + 2 * nseg;
+  // follow the true chain from segment 0 (whose walker starts at block 0)
+  std::vector<gzfp::IndexPiece> pieces;
+  uint64_t dst = 0, seg = 0, start = 0;
+  for (size_t it = 0; it <= nseg && dst < nblocks; it++) {
+    const unsigned long long n = counts[seg];
+    if (n > j.cap) return false;
+    if (n > start) {
+      pieces.push_back(gzfp::IndexPiece{seg * j.cap + start, n - start, dst, 0, 0});
+      dst += n - start;
+    }
+    const unsigned long long* inf = info + 4 * seg;
+    if (inf[3] == 2) return false;  // no merge within the extension's cap
+    if (inf[0]) {
+      pieces.push_back(gzfp::IndexPiece{0, inf[0], dst, seg, 1});
+      dst += inf[0];
+    }
+    if (inf[3] == 1) break;  // the chain ran to the end of the stream
+    if (inf[1] <= seg) return false;
+    seg = inf[1];
+    start = inf[2];
+  }
+  if (dst < nblocks) return false;  // fewer starts than blocks: the serial walk reports it
+  if ((err = reserve(ms.pieces, ms.pieces_cap, pieces.size() * sizeof(gzfp::IndexPiece))) ||
+      (err = reserve(ms.offsets, ms.offsets_cap, (size_t)nblocks * 8)) ||
+      (err = reserve(ms.sums, ms.sums_cap, 64)) ||
+      (err = cudaMemcpyAsync(ms.pieces, pieces.data(), pieces.size() * sizeof(gzfp::IndexPiece),
+                             cudaMemcpyHostToDevice, s)))
+    return false;
+  const gzfp::IndexPiece* dp = (const gzfp::IndexPiece*)ms.pieces;
+  unsigned long long* off = (unsigned long long*)ms.offsets;
+  unsigned long long* endp = (unsigned long long*)ms.sums;
+  const uint32_t np = (uint32_t)pieces.size();
+  switch (type) {
+    case GZFP_TYPE_FLOAT: err = gzfp::launch_index_assemble<float>(dims, j, dp, np, off, nblocks, endp, s); break;
+    case GZFP_TYPE_DOUBLE: err = gzfp::launch_index_assemble<double>(dims, j, dp, np, off, nblocks, endp, s); break;
+    case GZFP_TYPE_INT32: err = gzfp::launch_index_assemble<int32_t>(dims, j, dp, np, off, nblocks, endp, s); break;
+    default: err = gzfp::launch_index_assemble<int64_t>(dims, j, dp, np, off, nblocks, endp, s); break;
+  }
+  unsigned long long end = 0;
+  if (err || (err = cudaMemcpyAsync(&end, endp, 8, cudaMemcpyDeviceToHost, s)) ||
+      (err = cudaStreamSynchronize(s)))  // also keeps `pieces` alive for its copy
+    return false;
+  end_bit = end;
+  return true;
+}
+
 // Walk the blocks of a device stream into ms.offsets; *end_bit = the bit
-// after the last block.  Synchronises `s`.
+// after the last block: the parallel index, or one thread walking every
+// block when that cannot join its pieces.  Synchronises `s`.
 int walk_blocks(ModeSpace& ms, int type, int dims, const uint64_t* words, uint64_t nwords,
                 const gzfp::Geom& g, const gzfp::General& mode, uint64_t first, uint64_t& end_bit,
                 cudaStream_t s) {
   cudaError_t e;
+  if (parallel_index(ms, type, dims, words, nwords, g.nblocks, mode, first, end_bit, s, e))
+    return GZFP_OK;
+  if (e) return cuda_fail(e, "parallel block index");
   if ((e = reserve(ms.offsets, ms.offsets_cap, (size_t)g.nblocks * 8)) ||
       (e = reserve(ms.sums, ms.sums_cap, 64)))
     return cuda_fail(e, "cudaMalloc(block offsets)");

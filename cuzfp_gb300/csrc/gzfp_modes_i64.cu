@@ -10,6 +10,10 @@ template cudaError_t launch_encode_mode<int64_t>(int, const int64_t*, const Geom
 template cudaError_t launch_decode_mode<int64_t>(int, const uint64_t*, uint64_t,
                                             const unsigned long long*, const Geom&,
                                             const General&, int64_t*, cudaStream_t);
+template cudaError_t launch_index_walk<int64_t>(int, const IndexJob&, bool, cudaStream_t);
+template cudaError_t launch_index_assemble<int64_t>(int, const IndexJob&, const IndexPiece*, uint32_t,
+                                            unsigned long long*, uint64_t, unsigned long long*,
+                                            cudaStream_t);
 template cudaError_t launch_index_blocks<int64_t>(int, const uint64_t*, uint64_t, uint64_t,
                                              const General&, uint64_t, unsigned long long*,
                                              unsigned long long*, cudaStream_t);

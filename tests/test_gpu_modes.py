@@ -195,3 +195,48 @@ def test_mirror_compress_in_general_mode(gz, orc, cuda):
                               orc.decompress_params(exp, a.shape, a.dtype,
                                                     (zfp.minbits, zfp.maxbits, zfp.maxprec,
                                                      zfp.minexp)))
+
+
+@pytest.mark.parametrize("case", ["3d_f64_acc", "3d_f64_prec", "3d_f32_acc", "2d_f64_acc",
+                                  "1d_f32_prec", "3d_i64_prec"])
+def test_parallel_index(gz, orc, cuda, case):
+    """Streams of thousands of blocks are indexed by the parallel walkers:
+    the start bits equal the compressor's, and decompressing without them
+    (the index runs inside the call) gives the same field, plain and headed."""
+    import torch
+    from cuzfp_gb300 import synth
+    if case == "3d_f64_acc":
+        a = synth.sinusoids((128, 128, 128), 16, 32, seed=1, dtype=np.float64)
+        m = gz.mode_accuracy(gz.zfp_type.double, 1e-6)
+    elif case == "3d_f64_prec":
+        a = synth.sinusoids((112, 120, 128), 16, 32, seed=2, dtype=np.float64)
+        m = gz.mode_precision(gz.zfp_type.double, 16)
+    elif case == "3d_f32_acc":
+        a = synth.smooth_noisy_3d(96, 3, np.float32)
+        m = gz.mode_accuracy(gz.zfp_type.float, 1e-4)
+    elif case == "2d_f64_acc":
+        a = synth.sinusoids((510, 517), 8, 64, seed=4, dtype=np.float64)
+        m = gz.mode_accuracy(gz.zfp_type.double, 1e-6)
+    elif case == "1d_f32_prec":
+        a = synth.random_walk((1 << 16) - 5, seed=5, dtype=np.float32)
+        m = gz.mode_precision(gz.zfp_type.float, 12)
+    else:
+        a = (synth.sinusoids((80, 81, 82), 16, 32, seed=6) * 1e9).astype(np.int64)
+        m = gz.mode_precision(gz.zfp_type.int64, 32)
+    x = torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    w, offs = gz.compress_mode(x, m, with_offsets=True)
+    assert offs.numel() >= 4096
+    idx = gz.index_blocks(w, a.shape, x.dtype, m)
+    torch.cuda.synchronize()
+    assert torch.equal(idx, offs)
+    d0 = gz.decompress_mode(w, a.shape, x.dtype, m, offsets=offs)
+    d1 = gz.decompress_mode(w, a.shape, x.dtype, m)
+    torch.cuda.synchronize()
+    it = {np.float32: torch.int32, np.float64: torch.int64, np.int64: torch.int64}[a.dtype.type]
+    assert torch.equal(d0.view(it), d1.view(it))
+    s = orc.compress_params(a, m.as_tuple())
+    assert np.array_equal(w.cpu().numpy().view(np.uint64), s)
+    hw = gz.compress_mode_headed(x, m)
+    hd = gz.decompress_headed(hw)
+    torch.cuda.synchronize()
+    assert torch.equal(hd.reshape(d0.shape).view(it), d0.view(it))
