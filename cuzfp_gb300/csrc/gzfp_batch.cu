@@ -51,7 +51,7 @@ namespace gzfp {
 namespace bhost {
 
 bool valid_config(const gzfp_batch_config& c) {
-  return (c.threads == 64 || c.threads == 128 || c.threads == 256) && c.ctas_per_sm >= 1 &&
+  return (c.threads == 64 || c.threads == 128 || c.threads == 256) && c.ctas_per_sm >= 0 &&
          c.ctas_per_sm <= kMaxCtasPerSm && (c.blocks_per_thread == 1 || c.blocks_per_thread == 2 ||
                                  c.blocks_per_thread == 4);
 }
@@ -98,8 +98,7 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
       d.first_chunk = p.nchunks;
       p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
       if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
-      if (decode && it.maxbits % 64 == 0 && it.maxbits / 64 <= kBatchMaxStagedWords)
-        p.staged_w = std::max(p.staged_w, it.maxbits / 64);
+      p.staged_w = std::max(p.staged_w, batch_item_staged_w(decode, it.maxbits));
     }
     p.kind_hi[k] = p.nchunks;
   }
@@ -163,13 +162,16 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev))) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
-  const uint32_t sw = decode ? p.staged_w : 0;
+  const uint32_t sw = p.staged_w;
   const bool ahead = cfg.claim_ahead != 0;
   // one persistent kernel per kind present, in sequence on the stream
   for (int k = 0; k < kBatchKinds && !e; k++) {
     if (p.kind_hi[k] == p.kind_lo[k]) continue;
-    const int occ = std::max(1, batch_occupancy(cfg.threads, decode, k, sw));
-    const int grid = sms * std::min(cfg.ctas_per_sm, occ);
+    // ctas_per_sm 0: the grid kernel, one CTA per slice of a chunk
+    const int grid = cfg.ctas_per_sm == 0
+                         ? 0
+                         : sms * std::min(cfg.ctas_per_sm,
+                                          std::max(1, batch_occupancy(cfg.threads, decode, k, sw)));
     e = launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, wl.descs,
                      wl.chunk_item, p.kind_lo[k], p.kind_hi[k], wl.counter + k, s);
   }
@@ -242,7 +244,7 @@ const char* gzfp_batch_last_error(void) { return g_batch_error; }
 void gzfp_batch_default_config(gzfp_batch_config* cfg) {
   if (!cfg) return;
   cfg->threads = 128;
-  cfg->ctas_per_sm = 16;  // as many as fit
+  cfg->ctas_per_sm = 0;  // the grid kernel
   cfg->blocks_per_thread = 1;
   cfg->claim_ahead = 1;
 }
@@ -323,11 +325,10 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
   int st = GZFP_OK;
   const int threads[] = {64, 128, 256};
   const int bpts[] = {1, 2, 4};
-  uint32_t sw = 0;  // the decode staging depth the kernel will use for this batch
-  if (decompress && items)
+  uint32_t sw = 0;  // the staging depth the kernels will use for this batch
+  if (items)
     for (int i = 0; i < count; i++)
-      if (items[i].maxbits % 64 == 0 && items[i].maxbits / 64 <= gzfp::kBatchMaxStagedWords)
-        sw = std::max(sw, items[i].maxbits / 64);
+      sw = std::max(sw, gzfp::batch_item_staged_w(decompress != 0, items[i].maxbits));
   // the kinds present: their occupancy bounds the CTAs per SM worth trying
   bool present[gzfp::kBatchKinds] = {};
   if (items)
@@ -342,9 +343,10 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
     for (int k = 0; k < gzfp::kBatchKinds; k++)
       if (present[k]) occ = std::max(occ, gzfp::batch_occupancy(nt, decompress != 0, k, sw));
     occ = std::min(occ, kMaxCtasPerSm);
-    for (int per_sm = 1; per_sm <= occ && !st; per_sm++) {
+    // per_sm 0: the grid kernel (no claims, so no claim-ahead either)
+    for (int per_sm = 0; per_sm <= occ && !st; per_sm++) {
       for (int bpt : bpts) {
-        for (int ahead = 0; ahead < 2 && !st; ahead++) {
+        for (int ahead = 0; ahead < (per_sm ? 2 : 1) && !st; ahead++) {
           const gzfp_batch_config cfg{nt, per_sm, bpt, ahead};
           gzfp_batch_plan* plan = nullptr;
           st = gzfp_batch_plan_create(items, count, decompress, &cfg, &plan);

@@ -55,8 +55,17 @@ struct BatchPlanes {
 
 // Blocks of whole 64-bit words, up to this many per block, are decoded from
 // a shared-memory copy of the warp's 32 slots made with coalesced loads (as
-// the plain decoder does); others read the stream directly.
+// the plain decoder does); others read the stream directly.  Encoding
+// assembles blocks of whole words, up to kMaxStagedOut per block, in the
+// same buffer and the warp stores its 32 slots with coalesced stores (as
+// the plain encoder does).
 constexpr uint32_t kBatchMaxStagedWords = 32;
+
+// Staging rows an item asks for (0: none).
+GZ_HD uint32_t batch_item_staged_w(bool decode, uint32_t maxbits) {
+  const uint32_t w = maxbits / 64;
+  return maxbits % 64 == 0 && w <= (decode ? kBatchMaxStagedWords : kMaxStagedOut) ? w : 0;
+}
 
 template <int NT, bool DECODE, int D, typename T>
 __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, BatchPlanes<NT>& ps,
@@ -85,6 +94,21 @@ __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, Batc
     decode_one<D, T>((T*)d.out, d.g, b, d.maxbits,
                      DevWords{nullptr, (const uint64_t*)d.in, d.nwords}, ps);
   } else {
+    const uint32_t W = d.maxbits >> 6;
+    if (d.maxbits % 64 == 0 && W <= staged_w && W <= kMaxStagedOut) {  // the whole warp
+      if (b < d.g.nblocks)
+        encode_one<D, T, true>((const T*)d.in, d.g, b, d.maxbits,
+                               StagedWords<NT + 1>{sbuf + threadIdx.x, b * W, W}, ps);
+      __syncwarp();
+      const uint64_t b0 = b - (threadIdx.x & 31);
+      if (b0 < d.g.nblocks) {
+        const uint64_t left = d.g.nblocks - b0;
+        warp_copy<true, NT + 1>(sbuf + (threadIdx.x & ~31u), (uint64_t*)d.out + b0 * W, W,
+                                left < 32 ? (uint32_t)left : 32);
+      }
+      __syncwarp();  // the next chunk's blocks reuse the buffer
+      return;
+    }
     if (b >= d.g.nblocks) return;
     encode_one<D, T>((const T*)d.in, d.g, b, d.maxbits,
                      DevWords{(uint64_t*)d.out, nullptr, d.nwords}, ps);
@@ -105,12 +129,48 @@ struct BatchSlots {
   static constexpr int value = DECODE ? decode_slots<D, T>() : store_slots<D, T>();
 };
 
-// Persistent kernel for one kind: chunks [lo, hi) of the work list.  NT
-// threads per CTA, bpt blocks per thread per chunk.  `counter` must be zero
-// at launch.  Decoding stages items of up to staged_w words per block in
-// shared memory behind the plane store.
+// The 4^3 64-bit decoder is latency-bound on its plane chain: like the plain
+// decoder it gets a tighter register budget for a fourth CTA of 128 threads
+// per SM whenever shared memory allows one.
 template <int NT, bool DECODE, int D, typename T>
-__global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
+struct BatchMinBlocksWide {
+  static constexpr int value =
+      DECODE && D == 3 && sizeof(T) == 8 ? 4 * 128 / NT : BatchMinBlocks<NT, D, T>::value;
+};
+
+// Grid kernel for one kind: CTA i codes slice i % bpt (NT blocks, one per
+// thread) of chunk lo + i / bpt, so the hardware's CTA scheduler spreads the
+// kind's chunks over the SMs and no thread loops over blocks.  The block
+// code then compiles as in the plain kernels: under a loop, the 4^3 64-bit
+// coders spill several hundred bytes per thread at the same register
+// budget.  Items of up to staged_w words per block are staged in shared
+// memory behind the plane store.
+template <int NT, bool DECODE, int D, typename T, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    batch_grid_kernel(const BatchDesc* __restrict__ descs,
+                      const uint32_t* __restrict__ chunk_item, uint64_t lo, int bpt,
+                      uint32_t staged_w) {
+  extern __shared__ uint64_t smem[];
+  __shared__ BatchDesc s_desc;
+  const Plane4Tables* t4 = stage_tables<D, NT>(smem);
+  BatchPlanes<NT> ps{smem + table_words<D>() + threadIdx.x, t4};
+  uint64_t* sbuf = smem + table_words<D>() + BatchSlots<DECODE, D, T>::value * NT;
+  const uint32_t j = blockIdx.x % (uint32_t)bpt;
+  const uint64_t chunk = lo + blockIdx.x / (uint32_t)bpt;
+  if (threadIdx.x == 0) s_desc = descs[chunk_item[chunk]];
+  __syncthreads();
+  const BatchDesc& d = s_desc;
+  const uint64_t first = (chunk - d.first_chunk) * (uint64_t)(NT * bpt) + (uint64_t)j * NT;
+  batch_block<NT, DECODE, D, T>(d, first + threadIdx.x, ps, sbuf, staged_w);
+}
+
+// Persistent kernel for one kind: chunks [lo, hi) of the work list.  NT
+// threads per CTA, bpt blocks per thread per chunk, register budget for
+// MINB resident CTAs per SM.  `counter` must be zero at launch.  Items of
+// up to staged_w words per block are staged in shared memory behind the
+// plane store.
+template <int NT, bool DECODE, int D, typename T, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     batch_kernel(const BatchDesc* __restrict__ descs, const uint32_t* __restrict__ chunk_item,
                  uint64_t lo, uint64_t hi, unsigned long long* counter, int bpt, int ahead,
                  uint32_t staged_w) {
@@ -140,35 +200,83 @@ __global__ void __launch_bounds__(NT, (BatchMinBlocks<NT, D, T>::value))
   }
 }
 
-// shared memory of a batch CTA of one kind: the plane store, and for
-// decoding the staged word buffer (staged_w words per block and the zero
-// rows after them, at pitch NT + 1)
+// shared memory of a batch CTA of one kind: the plane store, and the staged
+// word buffer (staged_w words per block and the zero rows after them, at
+// pitch NT + 1)
 template <int NT, bool DECODE, int D, typename T>
-size_t batch_smem_bytes(uint32_t staged_w) {
+GZ_HD size_t batch_smem_bytes(uint32_t staged_w) {
   return ((size_t)NT * BatchSlots<DECODE, D, T>::value + (size_t)table_words<D>()) * 8 +
-         (DECODE && staged_w ? (size_t)(staged_w + kPadRows) * (NT + 1) * 8 : 0);
+         (staged_w ? (size_t)(staged_w + kPadRows) * (NT + 1) * 8 : 0);
 }
 
+// CTAs of `sm` bytes of shared memory that fit one SM (228 KB, 1 KB
+// reserved per CTA)
+GZ_HD bool batch_smem_fits(size_t sm, int ctas) { return (sm + 1024) * ctas <= 228 * 1024; }
+
+// The launch of one kind: the kernels (register budget) and the staging
+// depth they run with.  Encoding stages output only where the buffer costs
+// no resident CTA, as the plain encoder; decoding takes the wide budget
+// where shared memory allows its CTAs.
+template <int NT, bool DECODE, int D, typename T>
+struct BatchLaunch {
+  void (*persistent)(const BatchDesc*, const uint32_t*, uint64_t, uint64_t, unsigned long long*,
+                     int, int, uint32_t);
+  void (*grid)(const BatchDesc*, const uint32_t*, uint64_t, int, uint32_t);
+  uint32_t staged_w;
+  size_t smem;
+  explicit BatchLaunch(uint32_t sw) {
+    constexpr int MB = BatchMinBlocks<NT, D, T>::value;
+    constexpr int WIDE = BatchMinBlocksWide<NT, DECODE, D, T>::value;
+    staged_w = sw;
+    if (!DECODE && sw && !batch_smem_fits(batch_smem_bytes<NT, DECODE, D, T>(sw), MB)) staged_w = 0;
+    smem = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
+    const bool wide = WIDE != MB && batch_smem_fits(smem, WIDE);
+    persistent = wide ? batch_kernel<NT, DECODE, D, T, WIDE> : batch_kernel<NT, DECODE, D, T, MB>;
+    grid = wide ? batch_grid_kernel<NT, DECODE, D, T, WIDE> : batch_grid_kernel<NT, DECODE, D, T, MB>;
+  }
+};
+
+// CTAs of one grid launch at most (the rest go to further launches)
+constexpr uint64_t kBatchGridPiece = 1ull << 30;
+
+// grid > 0: the persistent kernel on `grid` CTAs; grid == 0: the grid
+// kernel over every (chunk, slice) of [lo, hi)
 template <int NT, bool DECODE, int D, typename T>
 cudaError_t launch_batch_kind(int grid, int bpt, bool ahead, uint32_t staged_w,
                               const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,
                               uint64_t hi, unsigned long long* counter, cudaStream_t s) {
-  const size_t sm = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
-  auto k = batch_kernel<NT, DECODE, D, T>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const BatchLaunch<NT, DECODE, D, T> L(staged_w);
+  cudaError_t e;
+  if (grid > 0) {
+    e = cudaFuncSetAttribute(L.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)L.smem);
+    if (e != cudaSuccess) return e;
+    L.persistent<<<grid, NT, L.smem, s>>>(descs, chunk_item, lo, hi, counter, bpt,
+                                          ahead ? 1 : 0, L.staged_w);
+    return cudaGetLastError();
+  }
+  e = cudaFuncSetAttribute(L.grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
   if (e != cudaSuccess) return e;
-  k<<<grid, NT, sm, s>>>(descs, chunk_item, lo, hi, counter, bpt, ahead ? 1 : 0, staged_w);
-  return cudaGetLastError();
+  const uint64_t per = kBatchGridPiece / (uint64_t)bpt;  // chunks per launch
+  for (uint64_t c = lo; c < hi; c += per) {
+    const uint64_t n = hi - c < per ? hi - c : per;
+    L.grid<<<(unsigned)(n * (uint64_t)bpt), NT, L.smem, s>>>(descs, chunk_item, c, bpt,
+                                                              L.staged_w);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
+// resident CTAs per SM of the persistent kernel
 template <int NT, bool DECODE, int D, typename T>
 int batch_occupancy_kind(uint32_t staged_w) {
   int n = 0;
-  auto k = batch_kernel<NT, DECODE, D, T>;
-  const size_t sm = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+  const BatchLaunch<NT, DECODE, D, T> L(staged_w);
+  if (cudaFuncSetAttribute(L.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)L.smem) != cudaSuccess)
     return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, sm) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, L.persistent, NT, L.smem) != cudaSuccess)
+    return 0;
   return n;
 }
 

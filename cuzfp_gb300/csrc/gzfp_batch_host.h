@@ -20,7 +20,7 @@ struct Prepared {
   std::vector<BatchDesc> descs;  // grouped by kind (kBatchKind order)
   uint64_t nchunks = 0;
   uint64_t kind_lo[kBatchKinds] = {}, kind_hi[kBatchKinds] = {};  // each kind's chunk range
-  uint32_t staged_w = 0;  // decode: largest words per block staged in shared memory
+  uint32_t staged_w = 0;  // largest words per block staged in shared memory
   // kernels enqueue launches: the chunk table and one per kind present
   int kernels() const {
     int n = nchunks ? 1 : 0;

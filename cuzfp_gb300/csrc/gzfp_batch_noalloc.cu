@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "gzfp.h"
+#include "gzfp_batch_host.h"
 #include "gzfp_batch_launch.h"
 
 namespace {
@@ -63,10 +64,7 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   gzfp_batch_config cfg;
   gzfp_batch_default_config(&cfg);
   if (cfg_in) cfg = *cfg_in;
-  if (!(cfg.threads == 64 || cfg.threads == 128 || cfg.threads == 256) || cfg.ctas_per_sm < 1 ||
-      cfg.ctas_per_sm > 16 ||
-      !(cfg.blocks_per_thread == 1 || cfg.blocks_per_thread == 2 || cfg.blocks_per_thread == 4))
-    return nfail(GZFP_ERR_ARG, "bad batch configuration");
+  if (!gzfp::bhost::valid_config(cfg)) return nfail(GZFP_ERR_ARG, "bad batch configuration");
   if (!items || count < 0) return nfail(GZFP_ERR_ARG, "bad item list");
   if (count > kMaxItems) {
     char msg[160];
@@ -111,7 +109,7 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   }
   uint64_t nchunks = 0;
   uint64_t lo[gzfp::kBatchKinds], hi[gzfp::kBatchKinds];
-  uint32_t sw = 0;  // decode staging depth, as the allocating path chooses it
+  uint32_t sw = 0;  // staging depth, as the allocating path chooses it
   int slot = 0;
   for (int k = 0; k < gzfp::kBatchKinds; k++) {
     lo[k] = nchunks;
@@ -131,8 +129,8 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
       d.out = decode ? it.field : it.stream;
       d.first_chunk = nchunks;
       nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
-      if (decode && it.maxbits % 64 == 0 && it.maxbits / 64 <= gzfp::kBatchMaxStagedWords)
-        sw = it.maxbits / 64 > sw ? it.maxbits / 64 : sw;
+      const uint32_t w = gzfp::batch_item_staged_w(decode, it.maxbits);
+      sw = w > sw ? w : sw;
     }
     hi[k] = nchunks;
   }
@@ -166,9 +164,9 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   const bool ahead = cfg.claim_ahead != 0;
   for (int k = 0; k < gzfp::kBatchKinds && !e; k++) {
     if (hi[k] == lo[k]) continue;
-    int occ = gzfp::batch_occupancy(cfg.threads, decode, k, sw);
+    int occ = cfg.ctas_per_sm ? gzfp::batch_occupancy(cfg.threads, decode, k, sw) : 0;
     occ = occ > 1 ? occ : 1;
-    const int grid = sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : occ);
+    const int grid = cfg.ctas_per_sm ? sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : occ) : 0;
     e = gzfp::launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, descs,
                            chunk_item, lo[k], hi[k], counter + k, s);
   }

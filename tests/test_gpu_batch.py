@@ -1,4 +1,4 @@
-"""Batched persistent path: every array of a mixed batch gets exactly the
+"""Batched path (grid and persistent kernels): every array of a mixed batch gets exactly the
 stream (and decoded array) that the plain per-array path and the oracle
 give; graph plans replay bit-identically; the autotuner returns a shape
 that runs."""
@@ -37,7 +37,9 @@ def test_batch_matches_plain_and_oracle(gz, orc, cuda):
     rng = np.random.default_rng(77)
     arrs, rates = mixed_batch(rng)
     fields = [torch.from_numpy(a).to(cuda) for a in arrs]
-    for cfg in (None, gz.BatchConfig(64, 2, 4, 0), gz.BatchConfig(256, 1, 2, 1)):
+    for cfg in (None, gz.BatchConfig(256, 0, 4, 0), gz.BatchConfig(64, 0, 2, 0),
+                gz.BatchConfig(64, 2, 4, 0), gz.BatchConfig(256, 1, 2, 1),
+                gz.BatchConfig(128, 16, 1, 1)):
         streams = gz.compress_batch(fields, rates, config=cfg)
         outs = [torch.empty_like(f) for f in fields]
         gz.decompress_batch(streams, outs, rates, config=cfg)
@@ -99,3 +101,5 @@ def test_batch_errors(gz, cuda):
     assert e.value.status == gz.GZFP_ERR_CAPACITY
     with pytest.raises(gz.GzfpError):
         gz.compress_batch([f], [16.0], config=gz.BatchConfig(96, 1, 1, 0))
+    with pytest.raises(gz.GzfpError):
+        gz.compress_batch([f], [16.0], config=gz.BatchConfig(128, -1, 1, 0))

@@ -50,7 +50,7 @@ def _bits(t):
 def test_noalloc_matches_batch_entry_points(gz, cuda):
     import torch
     run = _bind(gz)
-    cfgs = [None, gz.BatchConfig(64, 3, 2, 0)]
+    cfgs = [None, gz.BatchConfig(64, 3, 2, 0), gz.BatchConfig(256, 0, 4, 0)]
     for call, (seed, count) in enumerate(((11, 30), (12, 17))):
         rng = np.random.default_rng(seed)
         arrs, rates = _batch(rng, count)
