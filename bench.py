@@ -538,7 +538,7 @@ def run_serving(args, rank, world, local, emit=True):
                    "uncompressed_bytes": float(nbytes.sum()),
                    "l2": "inputs larger than L2 (a 384^3 field per dtype, ~2 GB of streams "
                          "per second of arrivals)",
-                   "server": "device queue (one persistent kernel drains published requests)"},
+                   "server": "device queue (a persistent scheduler kernel drains published requests and launches each as its own grid from the device)"},
         "latency_ms": {"p50": round(p50 * 1e3, 4), "p99": round(p99 * 1e3, 4),
                        "mean": round(float(lat.mean()) * 1e3, 4)},
         "plain_serial_latency_ms": {"p50": round(np.percentile(lat_plain, 50) * 1e3, 4),

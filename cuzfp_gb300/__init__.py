@@ -948,7 +948,7 @@ class ServeResult(ctypes.Structure):
 
 class ServeConfig(ctypes.Structure):
     """gzfp_serve_config: device_queue = 1 selects the device-queue mode
-    (3D float / double requests), idle_exit_us its kernel's wait limit."""
+    (3D float / double requests), idle_exit_us its scheduler's wait limit."""
     _fields_ = [("budget_bytes", _SZ), ("max_batch", _I), ("max_inflight", _I),
                 ("compress_cfg", BatchConfig), ("decompress_cfg", BatchConfig),
                 ("device_queue", _I), ("idle_exit_us", _U)]
@@ -957,7 +957,7 @@ class ServeConfig(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [("wall", ctypes.c_double), ("batches", _I), ("mean_batch", ctypes.c_double),
                 ("peak_bytes", _SZ), ("busy", ctypes.c_double), ("kernels", _I),
-                ("mean_inflight", ctypes.c_double)]
+                ("mean_inflight", ctypes.c_double), ("schedulers", _I)]
 
     def as_dict(self) -> dict:
         return {f: (float(getattr(self, f)) if t is ctypes.c_double else int(getattr(self, f)))

@@ -3,7 +3,9 @@
 Each translation unit under csrc/ is compiled by nvcc in parallel, then
 linked into cuzfp_gb300/libgzfp.so.  Objects go to cuzfp_gb300/_build/.
 A unit is rebuilt when it or any header under csrc/ or include/ is newer
-than its object.
+than its object.  The units in RDC_UNITS launch kernels from the device and
+are compiled as relocatable device code; the link then runs the device
+linker and adds the CUDA device runtime.
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ LIB = os.path.join(HERE, "libgzfp.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + CSRC, "-I" + INCLUDE]
+RDC_UNITS = {"gzfp_serve_queue.cu"}
 
 
 def nvcc() -> str:
@@ -65,7 +68,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
     def compile_one(so):
         s, o = so
-        cmd = [cc] + NVCC_FLAGS + ["-c", s, "-o", o]
+        rdc = ["-rdc=true"] if os.path.basename(s) in RDC_UNITS else []
+        cmd = [cc] + NVCC_FLAGS + rdc + ["-c", s, "-o", o]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -79,7 +83,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             list(ex.map(compile_one, todo))
     if todo or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
-        cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
+        cmd = [cc] + ARCH + ["-shared", "-rdc=true", "-o", tmp] + objs + ["-lcudadevrt"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

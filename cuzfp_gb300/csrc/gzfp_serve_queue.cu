@@ -1,34 +1,38 @@
 // gzfp_serve_queue.cu -- the request server's device-queue mode
 // (gzfp_serve_config.device_queue = 1).
 //
-// One persistent kernel stays on the device for the run and drains a request
-// table in pinned, device-mapped host memory:
+// A request table in pinned, device-mapped host memory is drained on the
+// device by a persistent scheduler kernel (one thread), which launches each
+// published request as its own grid with a device-side launch:
 //
-//   host                                   device (every CTA)
-//   write request r's descriptor           take ticket c (atomicAdd)
-//   published += chunks of r  (release)    wait until c < published
-//                                          find its request (forward cursor),
-//                                          its descriptor (cached on the device)
-//                                          code the chunk's blocks
-//   poll done[r]                <--------  last chunk of r: done[r] = 1 (release)
+//   host                                   scheduler (device)
+//   write request p's descriptor           wait until p < published
+//   published = p + 1  (release)           read p's descriptor
+//                                          launch p's grid (fire and forget)
+//   poll done[p]                <--------  p's last CTA: done[p] = 1 (release)
 //
-// Chunks are numbered across requests in publication order and claimed in
-// that order, so the device works first-in first-out at chunk granularity
-// while the chunks of consecutive requests run side by side on the SMs: a
-// request that arrives while others are coded starts as soon as CTAs free
-// up, with no launch.  Each block is coded by the batched path's per-block
-// code (batch_block), so its bits are those of a plain call.
+// A request's grid is the per-kind kernel below: one CTA per 128 blocks,
+// one block per thread, the descriptor a kernel parameter, and the batched
+// path's per-block code (batch_block), so its bits are those of a plain call
+// and its register budget is that coder's own.  Grids of consecutive
+// requests run side by side as the SMs free up, with no host launch and no
+// batching delay.  (Claiming chunks from inside one persistent coding kernel
+// was measured slower: that kernel has one register budget for every coder,
+// and its loop around the block code makes the 4^3 double coders spill.)
 //
-// Waits are bounded: a CTA that finds no work for `idle_exit_us` leaves the
-// kernel, handing its ticket to the same CTA of the next launch, and the
-// host relaunches the kernel when new work is published and the previous
-// launch has ended.  Only the CTAs holding the next few tickets read the
-// host-side counters; the others read their mirror in device memory.
+// Waits are bounded: a scheduler that sees nothing published for
+// `idle_exit_us` leaves, recording how far it launched, and the host starts
+// a new one when work is published again.  Requests launched and not yet
+// done are capped below the device runtime's pending-launch limit; a
+// scheduler held at the cap with no request finishing for 10 s reports an
+// error and leaves.  A failed device-side launch is reported, not retried.
+//
+// This translation unit is compiled as relocatable device code and linked
+// with the CUDA device runtime (cudadevrt).
 #include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
-#include <atomic>
 #include <chrono>
 #include <deque>
 #include <numeric>
@@ -40,36 +44,27 @@
 namespace gzfp {
 namespace {
 
-constexpr int kQThreads = 128;     // threads per CTA
-constexpr int kQMaxBpt = 4;        // blocks per thread per chunk, at most
-constexpr int kQSlots = 32;        // plane-store slots (4^3 blocks)
-constexpr uint32_t kQStagedW = 32; // decode stages blocks of up to 32 words
-constexpr int kQPollers = 16;      // waiting CTAs that read the host-side counters
+constexpr int kQThreads = 128;                // threads (= blocks) per CTA of a request's grid
+constexpr unsigned long long kQMaxLaunched = 1024;  // requests launched and not done, at most
+constexpr unsigned long long kQStallNs = 10000000000ull;  // 10 s at the cap with no completion
 
-// A published request: its descriptor in the batched path's form (first_chunk
-// in the run's chunk numbering), its chunk count and which coder runs it.
+// A published request: its descriptor in the batched path's form, the CTAs
+// of its grid and which coder runs it.
 struct QueueReq {
   BatchDesc d;
-  uint32_t nchunks;
+  uint32_t ctas;
   uint32_t code;  // 0 / 1: 3D float / double compress; 2 / 3: decompress
-  uint32_t bpt;   // blocks per thread of its chunks (1..kQMaxBpt)
-  uint32_t pad;
 };
-constexpr int kQReqWords = (int)(sizeof(QueueReq) / 8);
-static_assert(sizeof(QueueReq) % 8 == 0 && kQReqWords <= 32, "descriptor words");
 
 // host-mapped control words
 struct QueueCtl {
-  unsigned long long published;  // host: chunks of all published requests
+  unsigned long long published;  // host: requests published
+  unsigned long long launched;   // device: requests launched, written when a scheduler leaves
   unsigned int stop;             // host: no more requests will come
-  unsigned int idle_exits;       // device: CTAs that left on the idle limit
-};
-
-// device-memory state
-struct QueueDev {
-  unsigned long long ticket;     // next chunk to hand out
-  unsigned long long published;  // mirror of QueueCtl::published
-  unsigned int stop;             // mirror of QueueCtl::stop
+  unsigned int idle_exits;       // device: schedulers that left on the idle limit
+  unsigned int ended;            // device: generation of the last scheduler that left
+  int error;                     // device: cudaError_t of a failed launch (or a stall)
+  unsigned long long error_req;  // device: the request it concerned
 };
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -87,11 +82,6 @@ __device__ __forceinline__ unsigned ld_acquire_sys(const unsigned* p) {
   asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 __device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -100,185 +90,146 @@ __device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long
 __device__ __forceinline__ void st_release_sys(unsigned* p, unsigned v) {
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-template <typename X>
-__device__ __forceinline__ X ld_vol(const X* p) {
-  return *(const volatile X*)p;
-}
 
-size_t queue_smem_bytes() {
-  return (size_t)kQSlots * kQThreads * 8 + (size_t)(kQStagedW + kPadRows) * (kQThreads + 1) * 8;
-}
+// per-request device state
+struct QueueDev {
+  unsigned* finished;            // CTAs of each request done
+  unsigned long long* t_first;   // device clock at its first CTA's start
+  unsigned long long* t_last;    // ... and at its last CTA's end
+  unsigned long long* completed; // requests done (one counter)
+  unsigned* done;                // host-mapped done flags
+};
 
-// A request's (first chunk, chunk count), from the device copy of its
-// descriptor once one CTA has made it, else from host memory.
-__device__ __forceinline__ void req_range(const QueueReq* reqs, const QueueReq* dreqs,
-                                          const unsigned* ready, uint32_t r,
-                                          unsigned long long& first, unsigned& n) {
-  if (ld_acquire_gpu(&ready[r])) {
-    first = ld_relaxed_gpu((const unsigned long long*)&dreqs[r].d.first_chunk);
-    n = (unsigned)ld_relaxed_gpu((const unsigned long long*)&dreqs[r].nchunks);
-  } else {
-    first = ld_vol(&reqs[r].d.first_chunk);
-    n = ld_vol(&reqs[r].nchunks);
-  }
-}
+// registers per thread that let MINB CTAs of kQThreads share an SM
+constexpr int queue_maxnreg(int minb) { return 65536 / (kQThreads * minb) / 8 * 8; }
 
-// One chunk's blocks of one request, per coder: separate functions, so that
-// each gets its own register allocation inside the kernel's budget.
-template <bool DECODE, typename T>
-__device__ __noinline__ void queue_chunk(const BatchDesc& d, uint64_t first, int bpt,
-                                         uint64_t* smem_planes, uint64_t* sbuf) {
-  BatchPlanes<kQThreads> ps{smem_planes + threadIdx.x, nullptr};
-#pragma unroll 1
-  for (int j = 0; j < bpt; j++)
-    batch_block<kQThreads, DECODE, 3, T>(d, first + (uint64_t)j * kQThreads + threadIdx.x, ps,
-                                         sbuf, kQStagedW);
-}
-
-// Tickets: a CTA takes the next chunk number with one atomicAdd and waits
-// until the host has published that chunk, so chunks are handed out in
-// order with no retries.  A CTA that reaches the idle limit while holding a
-// ticket leaves it in abandoned[blockIdx.x]; the same CTA of the next
-// launch (the grid does not change within a run) takes it up first, so
-// every chunk is coded exactly once.
-__global__ void __launch_bounds__(kQThreads, 3)
-    serve_queue_kernel(const QueueReq* reqs, QueueReq* dreqs, unsigned* ready, QueueCtl* ctl,
-                       unsigned* done, QueueDev* dev, unsigned long long* abandoned,
-                       unsigned* finished, unsigned long long* t_first,
-                       unsigned long long* t_last, unsigned long long idle_ns, uint32_t r0) {
+// One request's grid: CTA i codes blocks [128 i, 128 i + 128).  The last CTA
+// to finish raises the request's done flag.  The register budget is set with
+// __maxnreg__, not __launch_bounds__: measured on GB300, a device-launched
+// grid of a kernel with launch bounds and dynamic shared memory gets one
+// resident CTA per SM, with __maxnreg__ as many as fit.
+template <bool DECODE, typename T, int MINB>
+__global__ void __maxnreg__(queue_maxnreg(MINB))
+    serve_request_kernel(const __grid_constant__ BatchDesc d, uint32_t p, uint32_t staged_w,
+                         QueueDev q) {
   extern __shared__ uint64_t smem[];
-  __shared__ QueueReq s_req;
-  __shared__ unsigned long long s_chunk;
-  __shared__ uint32_t s_r;
-  __shared__ int s_cmd;
   BatchPlanes<kQThreads> ps{smem + threadIdx.x, nullptr};
-  uint64_t* sbuf = smem + kQSlots * kQThreads;
-  uint32_t r = r0;              // thread 0: request of the last chunk (none before r0 is left)
-  uint32_t loaded = 0xffffffffu;  // every thread: the request s_req holds
-  bool held = false;            // thread 0: holds ticket t
-  unsigned long long t = 0;
+  uint64_t* sbuf = smem + BatchSlots<DECODE, 3, T>::value * kQThreads;
+  if (threadIdx.x == 0) atomicMin(&q.t_first[p], globaltimer());
+  batch_block<kQThreads, DECODE, 3, T>(d, (uint64_t)blockIdx.x * kQThreads + threadIdx.x, ps,
+                                       sbuf, staged_w);
+  __syncthreads();  // the CTA's blocks are written
   if (threadIdx.x == 0) {
-    t = abandoned[blockIdx.x];
-    if (t != ~0ull) {
-      abandoned[blockIdx.x] = ~0ull;
-      held = true;
+    __threadfence();
+    atomicMax(&q.t_last[p], globaltimer());
+    if (atomicAdd(&q.finished[p], 1u) + 1 == gridDim.x) {  // every CTA of the request is done
+      __threadfence_system();
+      st_release_sys(&q.done[p], 1u);
+      atomicAdd(q.completed, 1ull);
     }
   }
+}
+
+// The coders' launches: register budget as the plain kernels' (the double
+// decoder's wide budget where shared memory allows its fourth CTA),
+// staging depth as the batched path chooses it.
+template <bool DECODE, typename T>
+struct QueueCoder {
+  static constexpr int MB = BatchMinBlocks<kQThreads, 3, T>::value;
+  static constexpr int WIDE = BatchMinBlocksWide<kQThreads, DECODE, 3, T>::value;
+  __host__ __device__ static uint32_t staged_w(uint32_t maxbits) {
+    const uint32_t sw = batch_item_staged_w(DECODE, maxbits);
+    return !DECODE && sw && !batch_smem_fits(batch_smem_bytes<kQThreads, DECODE, 3, T>(sw), MB) ? 0
+                                                                                            : sw;
+  }
+  __host__ __device__ static bool wide(size_t smem) {
+    return WIDE != MB && batch_smem_fits(smem, WIDE);
+  }
+  // largest dynamic shared memory a launch asks for
+  static size_t max_smem() {
+    return batch_smem_bytes<kQThreads, DECODE, 3, T>(DECODE ? kBatchMaxStagedWords : kMaxStagedOut);
+  }
+  __device__ static cudaError_t launch(const QueueReq& r, uint32_t p, const QueueDev& q) {
+    const uint32_t sw = staged_w(r.d.maxbits);
+    const size_t smem = batch_smem_bytes<kQThreads, DECODE, 3, T>(sw);
+    if (wide(smem))
+      serve_request_kernel<DECODE, T, WIDE>
+          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
+    else
+      serve_request_kernel<DECODE, T, MB>
+          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
+    return cudaGetLastError();
+  }
+  static cudaError_t setup() {
+    cudaError_t e = cudaFuncSetAttribute(serve_request_kernel<DECODE, T, MB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_smem());
+    if (e || WIDE == MB) return e;
+    return cudaFuncSetAttribute(serve_request_kernel<DECODE, T, WIDE>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem());
+  }
+};
+
+// The scheduler: one thread launches published requests in order, from
+// request `next` on.  It leaves when stopped, when nothing is published for
+// idle_ns, on a failed launch, or when held at the cap for kQStallNs with no
+// request finishing; it then records how far it launched and its
+// generation.
+__global__ void serve_sched_kernel(const QueueReq* reqs, QueueCtl* ctl, QueueDev q,
+                                   unsigned long long next, unsigned long long idle_ns,
+                                   unsigned gen) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long launched = next;
+  unsigned long long t_idle = globaltimer(), t_prog = t_idle;
+  unsigned long long seen = ld_relaxed_gpu(q.completed);
+  unsigned nap = 32;
   for (;;) {
-    if (threadIdx.x == 0) {
-      if (!held) {
-        t = atomicAdd(&dev->ticket, 1ull);
-        held = true;
+    const unsigned long long now = globaltimer();
+    if (launched < ld_acquire_sys(&ctl->published)) {
+      const unsigned long long c = ld_relaxed_gpu(q.completed);
+      if (c != seen) {
+        seen = c;
+        t_prog = now;
       }
-      // wait until chunk t is published; leave when stopped (it never will
-      // be) or after idle_ns (handing the ticket on)
-      int cmd = 0;
-      const unsigned long long t0 = globaltimer();
-      unsigned nap = 64;
-      for (;;) {
-        // the CTAs holding the next kQPollers tickets -- the ones a new
-        // request will start on -- read the host's count; the others its
-        // mirror
-        unsigned long long p = ld_vol(&dev->published);
-        const bool poller = t >= p && t < p + kQPollers;
-        if (poller) {
-          const unsigned long long hp = ld_acquire_sys(&ctl->published);
-          if (hp > p) {
-            atomicMax(&dev->published, hp);
-            p = hp;
-          }
+      if (launched - c < kQMaxLaunched) {
+        const QueueReq r = reqs[launched];  // written before its publication
+        cudaError_t e;
+        switch (r.code) {
+          case 0: e = QueueCoder<false, float>::launch(r, (uint32_t)launched, q); break;
+          case 1: e = QueueCoder<false, double>::launch(r, (uint32_t)launched, q); break;
+          case 2: e = QueueCoder<true, float>::launch(r, (uint32_t)launched, q); break;
+          case 3: e = QueueCoder<true, double>::launch(r, (uint32_t)launched, q); break;
+          default: e = cudaErrorInvalidValue; break;
         }
-        if (t < p) {
-          cmd = 1;
+        if (e != cudaSuccess) {
+          ctl->error = (int)e;
+          ctl->error_req = launched;
           break;
         }
-        unsigned stop = ld_vol(&dev->stop);
-        if (!stop && poller && ld_acquire_sys(&ctl->stop)) {
-          atomicExch(&dev->stop, 1u);
-          stop = 1;
-        }
-        if (stop) break;
-        if (globaltimer() - t0 > idle_ns) {
-          abandoned[blockIdx.x] = t;
-          cmd = 2;
-          break;
-        }
-        __nanosleep(nap);
-        nap = nap < 2048 ? 2 * nap : nap;
+        launched++;
+        t_idle = t_prog = now;
+        nap = 32;
+        continue;
       }
-      if (cmd == 1) {
-        held = false;
-        // the chunk's request: requests are numbered in publication order and
-        // one CTA's tickets only grow, so the cursor moves forward
-        for (;;) {
-          unsigned long long f;
-          unsigned n;
-          req_range(reqs, dreqs, ready, r, f, n);
-          if (t < f + n) break;
-          r++;
-        }
-        s_r = r;
-        s_chunk = t;
-        atomicMin(&t_first[r], globaltimer());
+      if (now - t_prog > kQStallNs) {  // at the cap and nothing finishes
+        ctl->error = (int)cudaErrorLaunchTimeout;
+        ctl->error_req = launched;
+        break;
       }
-      s_cmd = cmd;
-    }
-    __syncthreads();
-    const int cmd = s_cmd;
-    if (cmd != 1) {
-      if (cmd == 2 && threadIdx.x == 0) atomicAdd_system(&ctl->idle_exits, 1u);
-      return;
-    }
-    const uint32_t rr = s_r;
-    if (rr != loaded) {
-      // the descriptor: from its device copy, or from host memory with one
-      // word per thread (then copied to the device for the other CTAs)
-      if (threadIdx.x < 32) {
-        const bool rd = ld_acquire_gpu(&ready[rr]) != 0;
-        const unsigned lane = threadIdx.x;
-        if (lane < (unsigned)kQReqWords) {
-          unsigned long long v;
-          if (rd) {
-            v = ld_relaxed_gpu((const unsigned long long*)&dreqs[rr] + lane);
-          } else {
-            v = ld_vol((const unsigned long long*)&reqs[rr] + lane);
-            ((unsigned long long*)&dreqs[rr])[lane] = v;
-          }
-          ((unsigned long long*)&s_req)[lane] = v;
-        }
-        __syncwarp();
-        if (!rd && lane == 0) {
-          __threadfence();
-          st_release_gpu(&ready[rr], 1u);
-        }
-      }
-      __syncthreads();
-      loaded = rr;
-    }
-    const QueueReq& q = s_req;
-    const int bpt = (int)q.bpt;
-    const uint64_t first = (s_chunk - q.d.first_chunk) * (uint64_t)(kQThreads * bpt);
-    switch (q.code) {
-      case 0: queue_chunk<false, float>(q.d, first, bpt, smem, sbuf); break;
-      case 1: queue_chunk<false, double>(q.d, first, bpt, smem, sbuf); break;
-      case 2: queue_chunk<true, float>(q.d, first, bpt, smem, sbuf); break;
-      default: queue_chunk<true, double>(q.d, first, bpt, smem, sbuf); break;
-    }
-    __syncthreads();  // the chunk's blocks are written
-    if (threadIdx.x == 0) {
-      __threadfence();  // this CTA's writes before its count
-      const unsigned old = atomicAdd(&finished[rr], 1u);
-      atomicMax(&t_last[rr], globaltimer());
-      if (old + 1 == q.nchunks) {  // every chunk of the request is coded
-        __threadfence_system();
-        st_release_sys(&done[rr], 1u);
+      t_idle = now;  // work is waiting: not idle
+    } else {
+      if (ld_acquire_sys(&ctl->stop)) break;
+      if (now - t_idle > idle_ns) {
+        atomicAdd_system(&ctl->idle_exits, 1u);
+        break;
       }
     }
-    // s_chunk / s_r are rewritten only after the next __syncthreads
+    __nanosleep(nap);
+    nap = nap < 1024 ? 2 * nap : nap;
   }
+  ctl->launched = launched;
+  __threadfence_system();
+  st_release_sys(&ctl->ended, gen);
 }
 
 using Clock = std::chrono::steady_clock;
@@ -300,35 +251,49 @@ struct QueueRun {
   QueueCtl* h_ctl = nullptr;
   QueueCtl* d_ctl = nullptr;
   unsigned* h_done = nullptr;
-  unsigned* d_done = nullptr;
-  QueueDev* dev = nullptr;
-  QueueReq* dreqs = nullptr;               // device copies of the descriptors
-  unsigned* ready = nullptr;               // dreqs[i] is filled in
-  unsigned long long* abandoned = nullptr; // per CTA: a ticket handed to the next launch
-  unsigned* finished = nullptr;
-  unsigned long long* t_first = nullptr;
-  unsigned long long* t_last = nullptr;
-  cudaStream_t ks = nullptr, cs = nullptr;  // kernel stream, copy stream
-  cudaEvent_t kdone = nullptr;
+  QueueDev dev{};  // device pointers (done: host-mapped)
+  // schedulers run on a pool of streams: a scheduler's grid completes only
+  // once the requests it launched are done, so the next one takes a stream
+  // whose last scheduler grid has completed (or a new stream)
+  std::vector<cudaStream_t> ks;
+  std::vector<cudaEvent_t> kdone;
+  cudaStream_t cs = nullptr;  // copy stream
   std::vector<cudaEvent_t> events;
   ~QueueRun() {
-    if (ks) cudaStreamSynchronize(ks);
+    for (cudaStream_t s : ks) cudaStreamSynchronize(s);
     if (cs) cudaStreamSynchronize(cs);
     for (cudaEvent_t ev : events) cudaEventDestroy(ev);
-    if (kdone) cudaEventDestroy(kdone);
-    if (ks) cudaStreamDestroy(ks);
+    for (cudaEvent_t ev : kdone) cudaEventDestroy(ev);
+    for (cudaStream_t s : ks) cudaStreamDestroy(s);
     if (cs) cudaStreamDestroy(cs);
     cudaFree(arena);
-    cudaFree(dev);
-    cudaFree(dreqs);
-    cudaFree(ready);
-    cudaFree(abandoned);
-    cudaFree(finished);
-    cudaFree(t_first);
-    cudaFree(t_last);
+    cudaFree(dev.finished);
+    cudaFree(dev.t_first);
+    cudaFree(dev.t_last);
+    cudaFree(dev.completed);
     if (h_reqs) cudaFreeHost(h_reqs);
     if (h_ctl) cudaFreeHost(h_ctl);
     if (h_done) cudaFreeHost(h_done);
+  }
+  // a stream whose last scheduler grid has completed
+  cudaError_t free_stream(size_t* i) {
+    for (size_t j = 0; j < ks.size(); j++) {
+      const cudaError_t e = cudaEventQuery(kdone[j]);
+      if (e == cudaSuccess) {
+        *i = j;
+        return cudaSuccess;
+      }
+      if (e != cudaErrorNotReady) return e;
+    }
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking))) return e;
+    ks.push_back(s);
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming))) return e;
+    kdone.push_back(ev);
+    *i = ks.size() - 1;
+    return cudaSuccess;
   }
 };
 
@@ -346,58 +311,47 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
     if (r.maxbits < batch_ebits(r.type) + 1 || r.maxbits > (1u << 20))
       return serve_fail(GZFP_ERR_ARG, "bits per block out of range");
     const Geom g = make_geom_blocks(r.nx, r.ny, r.nz);
-    if (g.nblocks >= (1ull << 32)) return serve_fail(GZFP_ERR_ARG, "too many blocks");
+    if ((g.nblocks + kQThreads - 1) / kQThreads >= (1ull << 31))
+      return serve_fail(GZFP_ERR_ARG, "too many blocks");
   }
-  int device = 0, sms = 0, occ = 0;
   cudaError_t e;
   QueueRun q;
-  const size_t smem = queue_smem_bytes();
-  if ((e = cudaGetDevice(&device)) ||
-      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) ||
-      (e = cudaFuncSetAttribute(serve_queue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem)) ||
-      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_queue_kernel, kQThreads,
-                                                         smem)))
+  if ((e = QueueCoder<false, float>::setup()) || (e = QueueCoder<false, double>::setup()) ||
+      (e = QueueCoder<true, float>::setup()) || (e = QueueCoder<true, double>::setup()))
     return serve_cuda(e, "device-queue kernel set-up");
-  if (occ < 1) return serve_fail(GZFP_ERR_CUDA, "device-queue kernel does not fit on an SM");
-  const int grid = sms * occ;  // every CTA resident
   if ((e = cudaMalloc(&q.arena, cfg.budget_bytes)) ||
       (e = host_mapped(&q.h_reqs, &q.d_reqs, (size_t)count)) ||
       (e = host_mapped(&q.h_ctl, &q.d_ctl, 1)) ||
-      (e = host_mapped(&q.h_done, &q.d_done, (size_t)count)) ||
-      (e = cudaMalloc(&q.dev, sizeof(QueueDev))) ||
-      (e = cudaMalloc(&q.dreqs, count * sizeof(QueueReq))) ||
-      (e = cudaMalloc(&q.ready, count * sizeof(unsigned))) ||
-      (e = cudaMalloc(&q.abandoned, grid * sizeof(unsigned long long))) ||
-      (e = cudaMalloc(&q.finished, count * sizeof(unsigned))) ||
-      (e = cudaMalloc(&q.t_first, count * sizeof(unsigned long long))) ||
-      (e = cudaMalloc(&q.t_last, count * sizeof(unsigned long long))) ||
-      (e = cudaStreamCreateWithFlags(&q.ks, cudaStreamNonBlocking)) ||
+      (e = host_mapped(&q.h_done, &q.dev.done, (size_t)count)) ||
+      (e = cudaMalloc(&q.dev.finished, count * sizeof(unsigned))) ||
+      (e = cudaMalloc(&q.dev.t_first, count * sizeof(unsigned long long))) ||
+      (e = cudaMalloc(&q.dev.t_last, count * sizeof(unsigned long long))) ||
+      (e = cudaMalloc(&q.dev.completed, sizeof(unsigned long long))) ||
       (e = cudaStreamCreateWithFlags(&q.cs, cudaStreamNonBlocking)) ||
-      (e = cudaEventCreateWithFlags(&q.kdone, cudaEventDisableTiming)) ||
-      (e = cudaMemsetAsync(q.dev, 0, sizeof(QueueDev), q.ks)) ||
-      (e = cudaMemsetAsync(q.ready, 0, count * sizeof(unsigned), q.ks)) ||
-      (e = cudaMemsetAsync(q.abandoned, 0xff, grid * sizeof(unsigned long long), q.ks)) ||
-      (e = cudaMemsetAsync(q.finished, 0, count * sizeof(unsigned), q.ks)) ||
-      (e = cudaMemsetAsync(q.t_first, 0xff, count * sizeof(unsigned long long), q.ks)) ||
-      (e = cudaMemsetAsync(q.t_last, 0, count * sizeof(unsigned long long), q.ks)) ||
-      (e = cudaStreamSynchronize(q.ks)))
+      (e = cudaMemsetAsync(q.dev.finished, 0, count * sizeof(unsigned), q.cs)) ||
+      (e = cudaMemsetAsync(q.dev.t_first, 0xff, count * sizeof(unsigned long long), q.cs)) ||
+      (e = cudaMemsetAsync(q.dev.t_last, 0, count * sizeof(unsigned long long), q.cs)) ||
+      (e = cudaMemsetAsync(q.dev.completed, 0, sizeof(unsigned long long), q.cs)) ||
+      (e = cudaStreamSynchronize(q.cs)))
     return serve_cuda(e, "device-queue set-up");
   Arena arena(cfg.budget_bytes);
   const unsigned long long idle_ns = 1000ull * cfg.idle_exit_us;
-  std::vector<int> req_of(count), pub_of(count, -1);  // publication <-> request
-  auto launch = [&](uint32_t r0) -> cudaError_t {
-    serve_queue_kernel<<<grid, kQThreads, smem, q.ks>>>(
-        q.d_reqs, q.dreqs, q.ready, q.d_ctl, q.d_done, q.dev, q.abandoned, q.finished, q.t_first,
-        q.t_last, idle_ns, r0);
-    cudaError_t le = cudaGetLastError();
-    return le ? le : cudaEventRecord(q.kdone, q.ks);
+  unsigned gen = 0;  // schedulers started
+  auto launch = [&](unsigned long long next) -> cudaError_t {
+    size_t i = 0;
+    cudaError_t le = q.free_stream(&i);
+    if (le) return le;
+    gen++;
+    serve_sched_kernel<<<1, 32, 0, q.ks[i]>>>(q.d_reqs, q.d_ctl, q.dev, next, idle_ns, gen);
+    le = cudaGetLastError();
+    return le ? le : cudaEventRecord(q.kdone[i], q.ks[i]);
   };
 
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return reqs[a].arrival < reqs[b].arrival; });
+  std::vector<int> req_of(count), pub_of(count, -1);  // publication <-> request
   std::vector<size_t> offs(count, 0);
   std::vector<int> inflight;                       // published, not yet done
   struct Copy { cudaEvent_t ev; size_t off, bytes; };
@@ -405,22 +359,29 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
   std::vector<cudaEvent_t> spare;
   std::deque<int> queue;
   size_t next = 0;
-  int completed = 0, publications = 0, kernels = 0, npub = 0;
-  unsigned long long published = 0;
+  int completed = 0, publications = 0, npub = 0;
   double inflight_sum = 0, busy_time = 0, busy_since = -1, last_progress = 0;
-  bool running = false;
+  bool running = false;  // a scheduler is in its loop
   int st = GZFP_OK;
   const Clock::time_point t0 = Clock::now();
   auto now = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
+  // a scheduler left: note it, and fail the run if it reported an error
+  auto poll_scheduler = [&]() {
+    if (!running || __atomic_load_n(&q.h_ctl->ended, __ATOMIC_ACQUIRE) != gen) return;
+    running = false;
+    const int err = __atomic_load_n(&q.h_ctl->error, __ATOMIC_ACQUIRE);
+    if (err) {
+      char msg[128];
+      snprintf(msg, sizeof msg, "device-side launch of request %llu",
+               (unsigned long long)q.h_ctl->error_req);
+      st = serve_cuda((cudaError_t)err, msg);
+    }
+  };
 
   while (!st && completed < count) {
     double t = now();
-    // the kernel's CTAs leave when idle; note when the launch has ended
-    if (running) {
-      e = cudaEventQuery(q.kdone);
-      if (e == cudaSuccess) running = false;
-      else if (e != cudaErrorNotReady) { st = serve_cuda(e, "device-queue kernel"); break; }
-    }
+    poll_scheduler();
+    if (st) break;
     // completions
     for (size_t j = 0; j < inflight.size();) {
       const int r = inflight[j];
@@ -490,13 +451,8 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
       e_r.d.kind = batch_kind(rq.type, 3);
       e_r.d.in = rq.input;           // the field (compress) or stream words (decompress)
       e_r.d.out = q.arena + off;     // the stream words or the field
-      e_r.d.first_chunk = published;
-      // chunks small enough that a request of under a few waves of blocks
-      // still spreads over every CTA, larger for large requests
-      const uint64_t wave = (uint64_t)grid * kQThreads;
-      e_r.bpt = (uint32_t)std::min<uint64_t>(kQMaxBpt, std::max<uint64_t>(1, e_r.d.g.nblocks / wave));
-      const uint64_t chunk = (uint64_t)kQThreads * e_r.bpt;
-      e_r.nchunks = (uint32_t)((e_r.d.g.nblocks + chunk - 1) / chunk);
+      e_r.d.first_chunk = 0;
+      e_r.ctas = (uint32_t)((e_r.d.g.nblocks + kQThreads - 1) / kQThreads);
       e_r.code = (decode ? 2u : 0u) + (rq.type == GZFP_TYPE_DOUBLE ? 1u : 0u);
       if (!decode && rq.maxbits % 64) {
         // blocks that share words are merged with atomic ORs: zero the
@@ -506,32 +462,27 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
           st = serve_cuda(e, "cudaMemsetAsync(stream)"); break;
         }
       }
-      // a request is published by the count that covers its chunks: its
-      // descriptor (and every earlier one) is written first
-      published += e_r.nchunks;
-      if (e_r.nchunks == 0) {  // nothing to code (cannot happen: every request has a block)
-        st = serve_fail(GZFP_ERR_ARG, "empty request"); break;
-      }
-      __atomic_store_n(&q.h_ctl->published, published, __ATOMIC_RELEASE);
+      // a request is published by the count that covers it: its descriptor
+      // (and every earlier one) is written first
+      npub++;
+      __atomic_store_n(&q.h_ctl->published, (unsigned long long)npub, __ATOMIC_RELEASE);
       t = now();
       results[r].admitted = t;
       results[r].batch = publications;
       if (inflight.empty()) busy_since = t;
       inflight.push_back(r);
       inflight_sum += (double)inflight.size();
-      npub++;
       added++;
     }
     if (st) break;
     if (added) publications++;
-    // work published and no launch running: (re)launch the kernel
-    if (!running && !inflight.empty()) {
-      // every publication before the oldest one in flight is done
-      int r0 = npub;
-      for (int r : inflight) r0 = std::min(r0, pub_of[r]);
-      if ((e = launch((uint32_t)r0))) { st = serve_cuda(e, "device-queue kernel launch"); break; }
+    // work published and no scheduler in its loop: start one where the last
+    // one stopped
+    if (!running && __atomic_load_n(&q.h_ctl->launched, __ATOMIC_ACQUIRE) < (unsigned long long)npub) {
+      if ((e = launch(__atomic_load_n(&q.h_ctl->launched, __ATOMIC_ACQUIRE)))) {
+        st = serve_cuda(e, "device-queue scheduler launch"); break;
+      }
       running = true;
-      kernels++;
     }
     if (inflight.empty() && queue.empty()) last_progress = now();
     if (!inflight.empty() && now() - last_progress > 60.0) {
@@ -541,15 +492,17 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
   }
 
   const double wall = now();
-  // no more requests: the kernel leaves once nothing is left to claim
+  // no more requests: the scheduler leaves once it has launched everything
+  // published; every grid (schedulers, and with them their requests) ends
   __atomic_store_n(&q.h_ctl->stop, 1u, __ATOMIC_RELEASE);
-  if (running && (e = cudaEventSynchronize(q.kdone)) && !st) st = serve_cuda(e, "device-queue kernel");
+  for (cudaStream_t s : q.ks)
+    if ((e = cudaStreamSynchronize(s)) && !st) st = serve_cuda(e, "device-queue kernels");
   if ((e = cudaStreamSynchronize(q.cs)) && !st) st = serve_cuda(e, "output copy");
-  // device clock stamps of every request, relative to the run's first chunk
+  // device clock stamps of every request, relative to the run's first CTA
   std::vector<unsigned long long> tf(count), tl(count);
   if (!st && npub &&
-      ((e = cudaMemcpy(tf.data(), q.t_first, npub * 8, cudaMemcpyDeviceToHost)) ||
-       (e = cudaMemcpy(tl.data(), q.t_last, npub * 8, cudaMemcpyDeviceToHost))))
+      ((e = cudaMemcpy(tf.data(), q.dev.t_first, npub * 8, cudaMemcpyDeviceToHost)) ||
+       (e = cudaMemcpy(tl.data(), q.dev.t_last, npub * 8, cudaMemcpyDeviceToHost))))
     st = serve_cuda(e, "device stamps");
   if (!st) {
     unsigned long long base = ~0ull;
@@ -568,7 +521,8 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
     stats->mean_batch = publications ? (double)npub / publications : 0.0;
     stats->peak_bytes = arena.peak();
     stats->busy = stats->wall > 0 ? busy_time / stats->wall : 0.0;
-    stats->kernels = kernels;
+    stats->kernels = (int)gen + npub;  // schedulers, and one grid per request
+    stats->schedulers = (int)gen;
     stats->mean_inflight = npub ? inflight_sum / npub : 0.0;
   }
   return st;

@@ -239,8 +239,8 @@ int gzfp_compress_mode_headed(int type, unsigned nx, unsigned ny, unsigned nz,
 
 /* ------------------------------------------------------------ batches ---
    Many arrays -- each with its own shape, scalar type, dimensionality and
-   bits per block -- coded by one persistent kernel over a device-side work
-   list of (array, chunk of blocks) items.  Every array's stream is the one
+   bits per block -- coded by one kernel per kind (dimensionality x scalar
+   type) over a device-side work list of (array, chunk of blocks) items.  Every array's stream is the one
    gzfp_compress_bits would write.  Device pointers only; calls are
    asynchronous on `cuda_stream`.  No counterpart in cuZFP, which codes one
    array per call (src/cuZFP/cuZFP.cu:174-269). */
@@ -254,10 +254,13 @@ typedef struct {
   size_t stream_capacity; /* bytes at `stream` */
 } gzfp_batch_item;
 
-/* Launch shape of the persistent kernel: threads per CTA (64, 128, 256),
-   resident CTAs per SM (capped at what fits), blocks per thread per claimed
-   chunk (1, 2, 4) and whether the next chunk is claimed while the current
-   one is coded (claim_ahead). */
+/* Launch shape: threads per CTA (64, 128, 256); ctas_per_sm 0 (the default)
+   for the grid kernel, one CTA per slice of threads blocks of a chunk, one
+   block per thread, scheduled by the hardware; else the persistent kernel
+   with that many resident CTAs per SM (capped at what fits), which claim
+   chunks from a counter; blocks per thread per chunk (1, 2, 4); and, for
+   the persistent kernel, whether the next chunk is claimed while the
+   current one is coded (claim_ahead). */
 typedef struct {
   int threads;
   int ctas_per_sm;
@@ -280,7 +283,7 @@ int gzfp_batch_decompress(const gzfp_batch_item* items, int count, const gzfp_ba
                           void* cuda_stream);
 
 /* A batch prepared once and captured in a CUDA graph (work list upload,
-   zeroing, claim counter reset, persistent kernel); each launch replays it
+   zeroing, claim counter reset, per-kind kernels); each launch replays it
    on the same buffers. */
 typedef struct gzfp_batch_plan gzfp_batch_plan;
 int gzfp_batch_plan_create(const gzfp_batch_item* items, int count, int decompress,
@@ -337,19 +340,20 @@ int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompre
 
    * slots (device_queue = 0, the default; every scalar type and
      dimensionality): admitted requests are coded together by the batched
-     persistent kernel, and up to `max_inflight` batches run on the device at
+     path's kernels, and up to `max_inflight` batches run on the device at
      once, each on its own stream; a request that arrives while earlier
      batches run joins the next batch on a free slot.
-   * device queue (device_queue = 1; 3D float and double requests): one
-     persistent kernel stays on the device and drains a request table in
-     pinned host memory that the GPU reads directly.  The host publishes an
-     admitted request by writing its descriptor and raising the published
-     chunk count; CTAs claim published chunks of blocks in order, so a
-     request that arrives while others run is coded as soon as CTAs free up,
-     alongside them, with no launch.  The kernel marks each request done in
-     host memory when its last chunk is coded.  Every wait of the kernel for
-     new work is bounded: after `idle_exit_us` without work its CTAs leave,
-     and the host relaunches it when new work is published.
+   * device queue (device_queue = 1; 3D float and double requests): a
+     persistent scheduler kernel stays on the device and drains a request
+     table in pinned host memory that the GPU reads directly.  The host
+     publishes an admitted request by writing its descriptor and raising the
+     published count; the scheduler launches each published request, in
+     order, as its own grid of the request's coder with a device-side
+     launch, so a request that arrives while others run starts as soon as
+     SMs free up, alongside them, with no host launch.  The request's last
+     CTA marks it done in host memory.  Every wait of the scheduler is
+     bounded: after `idle_exit_us` with nothing published it leaves, and the
+     host starts a new one when new work is published.
 
    No counterpart in cuZFP, whose calls are synchronous and one array at a
    time (src/cuZFP/cuZFP.cu:174-269). */
@@ -371,14 +375,14 @@ typedef struct {
   double admitted;       /* seconds after the start: output memory granted, batch launched
                             (device queue: request published) */
   double completed;      /* seconds after the start: the request's batch finished
-                            (device queue: the kernel marked it done) */
+                            (device queue: its grid marked it done) */
   size_t output_bytes;
   int batch;             /* index of the batch (device queue: the publication) that ran it,
                             -1 if never run */
   int status;            /* GZFP_OK, or GZFP_ERR_CAPACITY for an output larger than the budget */
-  double device_start;   /* device queue: device clock, seconds after the run's first chunk,
-                            when the request's first chunk was claimed (0 in slot mode) */
-  double device_end;     /* device queue: the same, when its last chunk was done */
+  double device_start;   /* device queue: device clock, seconds after the run's first CTA,
+                            when the request's first CTA started (0 in slot mode) */
+  double device_end;     /* device queue: the same, when its last CTA was done */
 } gzfp_serve_result;
 
 typedef struct {
@@ -388,8 +392,8 @@ typedef struct {
   gzfp_batch_config compress_cfg;   /* slot mode: launch shapes (see gzfp_batch_autotune) */
   gzfp_batch_config decompress_cfg;
   int device_queue;      /* 0: slots; 1: device queue (3D float / double requests) */
-  unsigned idle_exit_us; /* device queue: the kernel's CTAs leave after this long without
-                            work (1..10^7 us; default 2000) */
+  unsigned idle_exit_us; /* device queue: the scheduler leaves after this long with nothing
+                            published (1..10^7 us; default 2000) */
 } gzfp_serve_config;
 
 typedef struct {
@@ -398,10 +402,11 @@ typedef struct {
   double mean_batch;     /* requests per batch (device queue: per publication) */
   size_t peak_bytes;     /* largest arena use */
   double busy;           /* fraction of the run with at least one request on the device */
-  int kernels;           /* kernels launched (slots: chunk tables and per-kind persistent
-                            kernels; device queue: launches of the persistent kernel) */
+  int kernels;           /* kernels launched (slots: chunk tables and per-kind kernels;
+                            device queue: schedulers and one grid per request) */
   double mean_inflight;  /* requests on the device when a request is admitted, itself
                             included, averaged over the admitted requests */
+  int schedulers;        /* device queue: scheduler launches (0 in slot mode) */
 } gzfp_serve_stats;
 
 void gzfp_serve_default_config(gzfp_serve_config* cfg);

@@ -152,8 +152,8 @@ def _queue_config(gz, **kw):
 
 
 def test_serve_queue_alone_equals_mix(gz, cuda):
-    """Requests published into the running persistent kernel give the bits
-    of plain calls, and their chunks overlap on the device."""
+    """Requests published to the running scheduler give the bits of plain
+    calls, and the grids it launches overlap on the device."""
     import torch
     rng = np.random.default_rng(201)
     reqs, expect, outs = _requests_3d(gz, cuda, rng, 200, 72, 15e-6)
@@ -164,19 +164,20 @@ def test_serve_queue_alone_equals_mix(gz, cuda):
         assert r.completed >= r.admitted >= reqs[i].arrival - 1e-9, i
         assert r.device_end >= r.device_start >= 0.0, i
         assert _same(e, o), (i, reqs[i].op, reqs[i].nx, reqs[i].ny, reqs[i].nz, reqs[i].maxbits)
-    # device-clock spans: some request's chunks ran while another's did
+    # device-clock spans: some request's CTAs ran while another's did
     spans = sorted((r.device_start, r.device_end) for r in res)
     ends = np.maximum.accumulate([e for _, e in spans])
     assert any(spans[i + 1][0] < ends[i] for i in range(len(spans) - 1))
     assert stats.mean_inflight > 1.0
-    assert 1 <= stats.kernels
+    assert stats.schedulers >= 1 and stats.kernels == stats.schedulers + len(reqs)
     assert 0 < stats.peak_bytes <= 1 << 30
 
 
 def test_serve_queue_idle_limit(gz, cuda):
-    """Arrival gaps far longer than the kernel's wait limit: its CTAs leave
-    when the limit runs out (no work for idle_exit_us), the server launches
-    it again for the next request, and every result is still exact."""
+    """Arrival gaps far longer than the scheduler's wait limit: it leaves
+    when the limit runs out (nothing published for idle_exit_us), the server
+    starts a new one for the next request, and every result is still
+    exact."""
     import torch
     rng = np.random.default_rng(202)
     reqs, expect, outs = _requests_3d(gz, cuda, rng, 12, 40, 0.0)
@@ -187,7 +188,7 @@ def test_serve_queue_idle_limit(gz, cuda):
     assert all(r.status == 0 for r in res)
     for e, o in zip(expect, outs):
         assert _same(e, o)
-    assert stats.kernels >= 6  # the limit ran out between requests
+    assert stats.schedulers >= 6  # the limit ran out between requests
 
 
 def test_serve_queue_budget_and_fifo(gz, cuda):
