@@ -507,6 +507,7 @@ def run_serving(args, rank, world, local, emit=True):
     qcfg.max_batch = args.max_batch
     qcfg.device_queue = 1
     cfg = gz.default_serve_config()
+    cfg.device_queue = 0  # slots
     cfg.budget_bytes = 40 << 30
     cfg.max_inflight = args.inflight
     cfg.max_batch = args.max_batch

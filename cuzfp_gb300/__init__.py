@@ -947,8 +947,9 @@ class ServeResult(ctypes.Structure):
 
 
 class ServeConfig(ctypes.Structure):
-    """gzfp_serve_config: device_queue = 1 selects the device-queue mode
-    (3D float / double requests), idle_exit_us its scheduler's wait limit."""
+    """gzfp_serve_config: device_queue = 1 (the default) selects the
+    device-queue mode, 0 the slot mode; idle_exit_us is the device queue's
+    scheduler wait limit."""
     _fields_ = [("budget_bytes", _SZ), ("max_batch", _I), ("max_inflight", _I),
                 ("compress_cfg", BatchConfig), ("decompress_cfg", BatchConfig),
                 ("device_queue", _I), ("idle_exit_us", _U)]

@@ -25,7 +25,8 @@ LIB = os.path.join(HERE, "libgzfp.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + CSRC, "-I" + INCLUDE]
-RDC_UNITS = {"gzfp_serve_queue.cu"}
+RDC_UNITS = {"gzfp_serve_queue.cu", "gzfp_serve_req_f32.cu", "gzfp_serve_req_f64.cu",
+             "gzfp_serve_req_i32.cu", "gzfp_serve_req_i64.cu"}
 
 
 def nvcc() -> str:

@@ -1,12 +1,14 @@
-// gzfp_serve.cu -- the request server of include/gzfp.h ("serving").
+// gzfp_serve.cu -- the request server of include/gzfp.h ("serving"): its
+// entry point, and the slot mode (device_queue = 0; the device-queue mode,
+// the default, is in gzfp_serve_queue.cu).
 //
-// One host thread runs an event loop over three things: arrivals (requests
+// In slot mode one host thread runs an event loop over three things: arrivals (requests
 // whose arrival time has passed join a FIFO queue), completions (a slot
 // whose batch event has fired releases its requests' output memory) and
 // launches (while a slot is free and requests wait, the head of the queue
 // is admitted request by request as long as its output fits in the arena,
 // and the admitted set is launched on that slot's stream as one compress
-// batch and one decompress batch of the persistent kernel).  Slots give the
+// batch and one decompress batch of the batched path).  Slots give the
 // overlap: a batch launched while others still run starts on the SMs as
 // their CTAs drain, so a new request waits for a free slot, not for the
 // whole device.  Admission is strictly FIFO so that a large request is
@@ -75,7 +77,7 @@ void gzfp_serve_default_config(gzfp_serve_config* cfg) {
   cfg->max_inflight = 3;
   gzfp_batch_default_config(&cfg->compress_cfg);
   gzfp_batch_default_config(&cfg->decompress_cfg);
-  cfg->device_queue = 0;
+  cfg->device_queue = 1;
   cfg->idle_exit_us = 2000;
 }
 

@@ -1,5 +1,6 @@
 // gzfp_serve_queue.cu -- the request server's device-queue mode
-// (gzfp_serve_config.device_queue = 1).
+// (gzfp_serve_config.device_queue = 1), for every scalar type and
+// dimensionality.
 //
 // A request table in pinned, device-mapped host memory is drained on the
 // device by a persistent scheduler kernel (one thread), which launches each
@@ -11,7 +12,8 @@
 //                                          launch p's grid (fire and forget)
 //   poll done[p]                <--------  p's last CTA: done[p] = 1 (release)
 //
-// A request's grid is the per-kind kernel below: one CTA per 128 blocks,
+// A request's grid is the per-kind kernel of gzfp_serve_queue.cuh (its
+// instances in gzfp_serve_req_<type>.cu): one CTA per 128 blocks,
 // one block per thread, the descriptor a kernel parameter, and the batched
 // path's per-block code (batch_block), so its bits are those of a plain call
 // and its register budget is that coder's own.  Grids of consecutive
@@ -27,8 +29,8 @@
 // scheduler held at the cap with no request finishing for 10 s reports an
 // error and leaves.  A failed device-side launch is reported, not retried.
 //
-// This translation unit is compiled as relocatable device code and linked
-// with the CUDA device runtime (cudadevrt).
+// These translation units are compiled as relocatable device code and
+// linked with the CUDA device runtime (cudadevrt).
 #include <stdio.h>
 #include <string.h>
 
@@ -38,23 +40,14 @@
 #include <numeric>
 #include <vector>
 
-#include "gzfp_batch.cuh"
 #include "gzfp_serve_host.h"
+#include "gzfp_serve_queue.cuh"
 
 namespace gzfp {
 namespace {
 
-constexpr int kQThreads = 128;                // threads (= blocks) per CTA of a request's grid
 constexpr unsigned long long kQMaxLaunched = 1024;  // requests launched and not done, at most
 constexpr unsigned long long kQStallNs = 10000000000ull;  // 10 s at the cap with no completion
-
-// A published request: its descriptor in the batched path's form, the CTAs
-// of its grid and which coder runs it.
-struct QueueReq {
-  BatchDesc d;
-  uint32_t ctas;
-  uint32_t code;  // 0 / 1: 3D float / double compress; 2 / 3: decompress
-};
 
 // host-mapped control words
 struct QueueCtl {
@@ -91,85 +84,6 @@ __device__ __forceinline__ void st_release_sys(unsigned* p, unsigned v) {
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// per-request device state
-struct QueueDev {
-  unsigned* finished;            // CTAs of each request done
-  unsigned long long* t_first;   // device clock at its first CTA's start
-  unsigned long long* t_last;    // ... and at its last CTA's end
-  unsigned long long* completed; // requests done (one counter)
-  unsigned* done;                // host-mapped done flags
-};
-
-// registers per thread that let MINB CTAs of kQThreads share an SM
-constexpr int queue_maxnreg(int minb) { return 65536 / (kQThreads * minb) / 8 * 8; }
-
-// One request's grid: CTA i codes blocks [128 i, 128 i + 128).  The last CTA
-// to finish raises the request's done flag.  The register budget is set with
-// __maxnreg__, not __launch_bounds__: measured on GB300, a device-launched
-// grid of a kernel with launch bounds and dynamic shared memory gets one
-// resident CTA per SM, with __maxnreg__ as many as fit.
-template <bool DECODE, typename T, int MINB>
-__global__ void __maxnreg__(queue_maxnreg(MINB))
-    serve_request_kernel(const __grid_constant__ BatchDesc d, uint32_t p, uint32_t staged_w,
-                         QueueDev q) {
-  extern __shared__ uint64_t smem[];
-  BatchPlanes<kQThreads> ps{smem + threadIdx.x, nullptr};
-  uint64_t* sbuf = smem + BatchSlots<DECODE, 3, T>::value * kQThreads;
-  if (threadIdx.x == 0) atomicMin(&q.t_first[p], globaltimer());
-  batch_block<kQThreads, DECODE, 3, T>(d, (uint64_t)blockIdx.x * kQThreads + threadIdx.x, ps,
-                                       sbuf, staged_w);
-  __syncthreads();  // the CTA's blocks are written
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicMax(&q.t_last[p], globaltimer());
-    if (atomicAdd(&q.finished[p], 1u) + 1 == gridDim.x) {  // every CTA of the request is done
-      __threadfence_system();
-      st_release_sys(&q.done[p], 1u);
-      atomicAdd(q.completed, 1ull);
-    }
-  }
-}
-
-// The coders' launches: register budget as the plain kernels' (the double
-// decoder's wide budget where shared memory allows its fourth CTA),
-// staging depth as the batched path chooses it.
-template <bool DECODE, typename T>
-struct QueueCoder {
-  static constexpr int MB = BatchMinBlocks<kQThreads, 3, T>::value;
-  static constexpr int WIDE = BatchMinBlocksWide<kQThreads, DECODE, 3, T>::value;
-  __host__ __device__ static uint32_t staged_w(uint32_t maxbits) {
-    const uint32_t sw = batch_item_staged_w(DECODE, maxbits);
-    return !DECODE && sw && !batch_smem_fits(batch_smem_bytes<kQThreads, DECODE, 3, T>(sw), MB) ? 0
-                                                                                            : sw;
-  }
-  __host__ __device__ static bool wide(size_t smem) {
-    return WIDE != MB && batch_smem_fits(smem, WIDE);
-  }
-  // largest dynamic shared memory a launch asks for
-  static size_t max_smem() {
-    return batch_smem_bytes<kQThreads, DECODE, 3, T>(DECODE ? kBatchMaxStagedWords : kMaxStagedOut);
-  }
-  __device__ static cudaError_t launch(const QueueReq& r, uint32_t p, const QueueDev& q) {
-    const uint32_t sw = staged_w(r.d.maxbits);
-    const size_t smem = batch_smem_bytes<kQThreads, DECODE, 3, T>(sw);
-    if (wide(smem))
-      serve_request_kernel<DECODE, T, WIDE>
-          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
-    else
-      serve_request_kernel<DECODE, T, MB>
-          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
-    return cudaGetLastError();
-  }
-  static cudaError_t setup() {
-    cudaError_t e = cudaFuncSetAttribute(serve_request_kernel<DECODE, T, MB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_smem());
-    if (e || WIDE == MB) return e;
-    return cudaFuncSetAttribute(serve_request_kernel<DECODE, T, WIDE>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem());
-  }
-};
-
 // The scheduler: one thread launches published requests in order, from
 // request `next` on.  It leaves when stopped, when nothing is published for
 // idle_ns, on a failed launch, or when held at the cap for kQStallNs with no
@@ -194,11 +108,11 @@ __global__ void serve_sched_kernel(const QueueReq* reqs, QueueCtl* ctl, QueueDev
       if (launched - c < kQMaxLaunched) {
         const QueueReq r = reqs[launched];  // written before its publication
         cudaError_t e;
-        switch (r.code) {
-          case 0: e = QueueCoder<false, float>::launch(r, (uint32_t)launched, q); break;
-          case 1: e = QueueCoder<false, double>::launch(r, (uint32_t)launched, q); break;
-          case 2: e = QueueCoder<true, float>::launch(r, (uint32_t)launched, q); break;
-          case 3: e = QueueCoder<true, double>::launch(r, (uint32_t)launched, q); break;
+        switch ((r.code & (kQDecode - 1)) / 3) {  // scalar type of the kind
+          case 0: e = queue_launch_f32(r, (uint32_t)launched, q); break;
+          case 1: e = queue_launch_f64(r, (uint32_t)launched, q); break;
+          case 2: e = queue_launch_i32(r, (uint32_t)launched, q); break;
+          case 3: e = queue_launch_i64(r, (uint32_t)launched, q); break;
           default: e = cudaErrorInvalidValue; break;
         }
         if (e != cudaSuccess) {
@@ -305,19 +219,17 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
                     gzfp_serve_result* results, gzfp_serve_stats* stats) {
   for (int i = 0; i < count; i++) {
     const gzfp_serve_request& r = reqs[i];
-    if (r.nz == 0 || (r.type != GZFP_TYPE_FLOAT && r.type != GZFP_TYPE_DOUBLE))
-      return serve_fail(GZFP_ERR_UNSUPPORTED,
-                        "the device-queue server codes 3D float and double requests");
+    if (r.nx == 0 || (r.nz != 0 && r.ny == 0)) return serve_fail(GZFP_ERR_ARG, "bad dimensions");
     if (r.maxbits < batch_ebits(r.type) + 1 || r.maxbits > (1u << 20))
       return serve_fail(GZFP_ERR_ARG, "bits per block out of range");
-    const Geom g = make_geom_blocks(r.nx, r.ny, r.nz);
+    const Geom g = make_geom_blocks(r.nx, r.ny ? r.ny : 1, r.nz ? r.nz : 1);
     if ((g.nblocks + kQThreads - 1) / kQThreads >= (1ull << 31))
       return serve_fail(GZFP_ERR_ARG, "too many blocks");
   }
   cudaError_t e;
   QueueRun q;
-  if ((e = QueueCoder<false, float>::setup()) || (e = QueueCoder<false, double>::setup()) ||
-      (e = QueueCoder<true, float>::setup()) || (e = QueueCoder<true, double>::setup()))
+  if ((e = queue_setup_f32()) || (e = queue_setup_f64()) || (e = queue_setup_i32()) ||
+      (e = queue_setup_i64()))
     return serve_cuda(e, "device-queue kernel set-up");
   if ((e = cudaMalloc(&q.arena, cfg.budget_bytes)) ||
       (e = host_mapped(&q.h_reqs, &q.d_reqs, (size_t)count)) ||
@@ -443,17 +355,18 @@ int serve_queue_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_
       req_of[npub] = r;
       pub_of[r] = npub;
       const void* field = decode ? (const void*)(q.arena + off) : rq.input;
-      e_r.d.g = make_geom_blocks(rq.nx, rq.ny, rq.nz);
+      const int dims = rq.nz ? 3 : rq.ny ? 2 : 1;
+      e_r.d.g = make_geom_blocks(rq.nx, rq.ny ? rq.ny : 1, rq.nz ? rq.nz : 1);
       e_r.d.g.vec =
           (rq.nx % 4 == 0 && (uintptr_t)field % batch_row_align(rq.type) == 0) ? 1u : 0u;
       e_r.d.nwords = (e_r.d.g.nblocks * rq.maxbits + 63) / 64;
       e_r.d.maxbits = rq.maxbits;
-      e_r.d.kind = batch_kind(rq.type, 3);
+      e_r.d.kind = batch_kind(rq.type, dims);
       e_r.d.in = rq.input;           // the field (compress) or stream words (decompress)
       e_r.d.out = q.arena + off;     // the stream words or the field
       e_r.d.first_chunk = 0;
       e_r.ctas = (uint32_t)((e_r.d.g.nblocks + kQThreads - 1) / kQThreads);
-      e_r.code = (decode ? 2u : 0u) + (rq.type == GZFP_TYPE_DOUBLE ? 1u : 0u);
+      e_r.code = (uint32_t)batch_kind_index(e_r.d.kind) | (decode ? kQDecode : 0u);
       if (!decode && rq.maxbits % 64) {
         // blocks that share words are merged with atomic ORs: zero the
         // output before the request is published

@@ -338,13 +338,12 @@ int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, int decompre
    allocated once per run, and are released when their request completes
    (optionally after a copy to a caller buffer).  Two modes:
 
-   * slots (device_queue = 0, the default; every scalar type and
-     dimensionality): admitted requests are coded together by the batched
+   * slots (device_queue = 0; every scalar type and dimensionality): admitted requests are coded together by the batched
      path's kernels, and up to `max_inflight` batches run on the device at
      once, each on its own stream; a request that arrives while earlier
      batches run joins the next batch on a free slot.
-   * device queue (device_queue = 1; 3D float and double requests): a
-     persistent scheduler kernel stays on the device and drains a request
+   * device queue (device_queue = 1, the default; every scalar type and
+     dimensionality): a persistent scheduler kernel stays on the device and drains a request
      table in pinned host memory that the GPU reads directly.  The host
      publishes an admitted request by writing its descriptor and raising the
      published count; the scheduler launches each published request, in
@@ -391,7 +390,7 @@ typedef struct {
   int max_inflight;      /* slot mode: batches on the device at once (1..8) */
   gzfp_batch_config compress_cfg;   /* slot mode: launch shapes (see gzfp_batch_autotune) */
   gzfp_batch_config decompress_cfg;
-  int device_queue;      /* 0: slots; 1: device queue (3D float / double requests) */
+  int device_queue;      /* 0: slots; 1: device queue (the default) */
   unsigned idle_exit_us; /* device queue: the scheduler leaves after this long with nothing
                             published (1..10^7 us; default 2000) */
 } gzfp_serve_config;

@@ -57,10 +57,13 @@ def _same(a, b):
 
 
 def test_serve_alone_equals_mix(gz, cuda):
+    """Slot mode: requests coded together in batches give the bits of plain
+    calls, and requests share batches."""
     import torch
     rng = np.random.default_rng(101)
     reqs, expect, outs = _requests(gz, cuda, rng, 240, 48, 20e-6)
     cfg = gz.default_serve_config()
+    cfg.device_queue = 0  # slots
     cfg.budget_bytes = 1 << 30
     cfg.max_inflight = 3
     res, stats = gz.serve(reqs, cfg)
@@ -83,6 +86,7 @@ def test_serve_budget_and_fifo(gz, cuda):
     big = torch.zeros((160, 160, 160), dtype=torch.float64, device=cuda)  # 32 MiB output
     reqs.insert(60, gz.serve_request(gz.GZFP_SERVE_COMPRESS, big, 64.0, 0.0))
     cfg = gz.default_serve_config()
+    cfg.device_queue = 0  # slots
     cfg.budget_bytes = 2 << 20
     cfg.max_batch = 8
     cfg.max_inflight = 2
@@ -106,6 +110,8 @@ def test_serve_bad_config(gz, cuda):
     x = torch.zeros((8, 8, 8), dtype=torch.float32, device=cuda)
     req = gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, 8.0, 0.0)
     cfg = gz.default_serve_config()
+    assert cfg.device_queue == 1  # the default mode
+    cfg.device_queue = 0
     cfg.max_inflight = 0
     with pytest.raises(gz.GzfpError):
         gz.serve([req], cfg)
@@ -114,8 +120,8 @@ def test_serve_bad_config(gz, cuda):
 # ------------------------------------------------------- device-queue mode
 
 def _requests_3d(gz, cuda, rng, count, max_edge, gap, rates=(8.0, 12.5, 16.0, 32.0)):
-    """3D float / double compress and decompress requests (the kinds the
-    device queue serves) with resident inputs and a copy_to buffer each."""
+    """3D float / double compress and decompress requests with resident
+    inputs and a copy_to buffer each."""
     import torch
     reqs, expect, outs = [], [], []
     t = 0.0
@@ -212,9 +218,26 @@ def test_serve_queue_budget_and_fifo(gz, cuda):
     assert all(a <= b for a, b in zip(adm, adm[1:]))
 
 
-def test_serve_queue_rejects_other_kinds(gz, cuda):
+def test_serve_queue_every_kind(gz, cuda):
+    """1D, 2D and 3D arrays of all four scalar types, rates whose blocks are
+    and are not whole words: the device queue gives every request the bits
+    of its plain call."""
     import torch
-    x = torch.zeros((8, 8), dtype=torch.float32, device=cuda)
+    rng = np.random.default_rng(204)
+    reqs, expect, outs = _requests(gz, cuda, rng, 240, 48, 20e-6)
+    res, stats = gz.serve(reqs, _queue_config(gz))
+    torch.cuda.synchronize()
+    for i, (r, e, o) in enumerate(zip(res, expect, outs)):
+        assert r.status == 0, i
+        assert _same(e, o), (i, reqs[i].op, reqs[i].type, reqs[i].nx, reqs[i].ny, reqs[i].nz,
+                             reqs[i].maxbits)
+    assert stats.kernels == stats.schedulers + len(reqs)
+
+
+def test_serve_queue_bad_request(gz, cuda):
+    import torch
+    x = torch.zeros((8, 8, 8), dtype=torch.float32, device=cuda)
     req = gz.serve_request(gz.GZFP_SERVE_COMPRESS, x, 8.0, 0.0)
+    req.maxbits = 3  # below the 9 bits of a float block's header
     with pytest.raises(gz.GzfpError):
         gz.serve([req], _queue_config(gz))
