@@ -80,13 +80,17 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
       return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
     kind_of[i] = batch_kind_index(batch_kind(it.type, dims));
   }
-  // descriptors grouped by kind, so each kind's chunks form one range
+  // descriptors grouped by kind, so each kind's chunks form one range, and
+  // within a kind the staged items first
   int slot = 0;
   for (int k = 0; k < kBatchKinds; k++) {
     p.kind_lo[k] = p.nchunks;
-    for (int i = 0; i < count; i++) {
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) p.kind_mid[k] = p.nchunks;
+      for (int i = 0; i < count; i++) {
       if (kind_of[i] != k) continue;
       const gzfp_batch_item& it = items[i];
+      if ((batch_item_staged_w(decode, it.maxbits) != 0) != (pass == 0)) continue;
       BatchDesc& d = p.descs[slot++];
       d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
       d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % batch_row_align(it.type) == 0) ? 1u : 0u;
@@ -99,6 +103,7 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
       p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
       if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
       p.staged_w = std::max(p.staged_w, batch_item_staged_w(decode, it.maxbits));
+      }
     }
     p.kind_hi[k] = p.nchunks;
   }
@@ -164,14 +169,22 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
   const uint32_t sw = p.staged_w;
   const bool ahead = cfg.claim_ahead != 0;
-  // one persistent kernel per kind present, in sequence on the stream
+  // per kind present, in sequence on the stream: one persistent kernel, or
+  // (ctas_per_sm 0) the grid kernel over the staged items and the grid
+  // kernel over the others
   for (int k = 0; k < kBatchKinds && !e; k++) {
     if (p.kind_hi[k] == p.kind_lo[k]) continue;
-    // ctas_per_sm 0: the grid kernel, one CTA per slice of a chunk
-    const int grid = cfg.ctas_per_sm == 0
-                         ? 0
-                         : sms * std::min(cfg.ctas_per_sm,
-                                          std::max(1, batch_occupancy(cfg.threads, decode, k, sw)));
+    if (cfg.ctas_per_sm == 0) {
+      if (p.kind_mid[k] > p.kind_lo[k])
+        e = launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, sw, wl.descs,
+                         wl.chunk_item, p.kind_lo[k], p.kind_mid[k], wl.counter + k, s);
+      if (!e && p.kind_hi[k] > p.kind_mid[k])
+        e = launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, 0, wl.descs,
+                         wl.chunk_item, p.kind_mid[k], p.kind_hi[k], wl.counter + k, s);
+      continue;
+    }
+    const int grid =
+        sms * std::min(cfg.ctas_per_sm, std::max(1, batch_occupancy(cfg.threads, decode, k, sw)));
     e = launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, wl.descs,
                      wl.chunk_item, p.kind_lo[k], p.kind_hi[k], wl.counter + k, s);
   }

@@ -67,12 +67,19 @@ GZ_HD uint32_t batch_item_staged_w(bool decode, uint32_t maxbits) {
   return maxbits % 64 == 0 && w <= (decode ? kBatchMaxStagedWords : kMaxStagedOut) ? w : 0;
 }
 
-template <int NT, bool DECODE, int D, typename T>
+// Which path a kernel compiles: kPathDirect (stream words read or written
+// in place), kPathStaged (every item it codes is staged: the caller
+// guarantees batch_item_staged_w(DECODE, maxbits) != 0 and <= staged_w), or
+// kPathEither (decided per item).  A kernel with one path spills less.
+constexpr int kPathDirect = 0, kPathStaged = 1, kPathEither = 2;
+
+template <int NT, bool DECODE, int D, typename T, int PATH = kPathEither>
 __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, BatchPlanes<NT>& ps,
                                             uint64_t* sbuf, uint32_t staged_w) {
   if (DECODE) {
     const uint32_t W = d.maxbits >> 6;
-    if (d.maxbits % 64 == 0 && W <= staged_w) {  // the same for the whole warp (one item)
+    if (PATH == kPathStaged ||
+        (PATH == kPathEither && d.maxbits % 64 == 0 && W <= staged_w)) {  // the whole warp (one item)
       const uint32_t lane = threadIdx.x & 31;
       const uint64_t b0 = b - lane;
       if (b0 < d.g.nblocks) {
@@ -95,7 +102,8 @@ __device__ __forceinline__ void batch_block(const BatchDesc& d, uint64_t b, Batc
                      DevWords{nullptr, (const uint64_t*)d.in, d.nwords}, ps);
   } else {
     const uint32_t W = d.maxbits >> 6;
-    if (d.maxbits % 64 == 0 && W <= staged_w && W <= kMaxStagedOut) {  // the whole warp
+    if (PATH == kPathStaged ||
+        (PATH == kPathEither && d.maxbits % 64 == 0 && W <= staged_w && W <= kMaxStagedOut)) {
       if (b < d.g.nblocks)
         encode_one<D, T, true>((const T*)d.in, d.g, b, d.maxbits,
                                StagedWords<NT + 1>{sbuf + threadIdx.x, b * W, W}, ps);
@@ -143,9 +151,10 @@ struct BatchMinBlocksWide {
 // kind's chunks over the SMs and no thread loops over blocks.  The block
 // code then compiles as in the plain kernels: under a loop, the 4^3 64-bit
 // coders spill several hundred bytes per thread at the same register
-// budget.  Items of up to staged_w words per block are staged in shared
-// memory behind the plane store.
-template <int NT, bool DECODE, int D, typename T, int MINB>
+// budget.  PATH is kPathStaged (every item of [lo, ...) stages, in up to
+// staged_w words per block, in shared memory behind the plane store) or
+// kPathDirect.
+template <int NT, bool DECODE, int D, typename T, int MINB, int PATH>
 __global__ void __launch_bounds__(NT, MINB)
     batch_grid_kernel(const BatchDesc* __restrict__ descs,
                       const uint32_t* __restrict__ chunk_item, uint64_t lo, int bpt,
@@ -161,7 +170,7 @@ __global__ void __launch_bounds__(NT, MINB)
   __syncthreads();
   const BatchDesc& d = s_desc;
   const uint64_t first = (chunk - d.first_chunk) * (uint64_t)(NT * bpt) + (uint64_t)j * NT;
-  batch_block<NT, DECODE, D, T>(d, first + threadIdx.x, ps, sbuf, staged_w);
+  batch_block<NT, DECODE, D, T, PATH>(d, first + threadIdx.x, ps, sbuf, staged_w);
 }
 
 // Persistent kernel for one kind: chunks [lo, hi) of the work list.  NT
@@ -213,10 +222,11 @@ GZ_HD size_t batch_smem_bytes(uint32_t staged_w) {
 // reserved per CTA)
 GZ_HD bool batch_smem_fits(size_t sm, int ctas) { return (sm + 1024) * ctas <= 228 * 1024; }
 
-// The launch of one kind: the kernels (register budget) and the staging
-// depth they run with.  Encoding stages output only where the buffer costs
-// no resident CTA, as the plain encoder; decoding takes the wide budget
-// where shared memory allows its CTAs.
+// The launch of one kind: the kernels (register budget, path) and the
+// staging depth they run with.  Encoding stages output only where the
+// buffer costs no resident CTA, as the plain encoder; decoding takes the
+// wide budget where shared memory allows its CTAs.  The grid kernel stages
+// every item when staged_w > 0 (a range of staged items), none otherwise.
 template <int NT, bool DECODE, int D, typename T>
 struct BatchLaunch {
   void (*persistent)(const BatchDesc*, const uint32_t*, uint64_t, uint64_t, unsigned long long*,
@@ -232,15 +242,23 @@ struct BatchLaunch {
     smem = batch_smem_bytes<NT, DECODE, D, T>(staged_w);
     const bool wide = WIDE != MB && batch_smem_fits(smem, WIDE);
     persistent = wide ? batch_kernel<NT, DECODE, D, T, WIDE> : batch_kernel<NT, DECODE, D, T, MB>;
-    grid = wide ? batch_grid_kernel<NT, DECODE, D, T, WIDE> : batch_grid_kernel<NT, DECODE, D, T, MB>;
+    if (staged_w)
+      grid = wide ? batch_grid_kernel<NT, DECODE, D, T, WIDE, kPathStaged>
+                  : batch_grid_kernel<NT, DECODE, D, T, MB, kPathStaged>;
+    else
+      grid = wide ? batch_grid_kernel<NT, DECODE, D, T, WIDE, kPathDirect>
+                  : batch_grid_kernel<NT, DECODE, D, T, MB, kPathDirect>;
   }
 };
 
 // CTAs of one grid launch at most (the rest go to further launches)
 constexpr uint64_t kBatchGridPiece = 1ull << 30;
 
-// grid > 0: the persistent kernel on `grid` CTAs; grid == 0: the grid
-// kernel over every (chunk, slice) of [lo, hi)
+// grid > 0: the persistent kernel on `grid` CTAs, items staged per item up
+// to staged_w words; grid == 0: the grid kernel over every (chunk, slice)
+// of [lo, hi), every item staged (staged_w > 0: the caller's range holds
+// only items with batch_item_staged_w != 0, each at most staged_w) or none
+// (staged_w == 0)
 template <int NT, bool DECODE, int D, typename T>
 cudaError_t launch_batch_kind(int grid, int bpt, bool ahead, uint32_t staged_w,
                               const BatchDesc* descs, const uint32_t* chunk_item, uint64_t lo,

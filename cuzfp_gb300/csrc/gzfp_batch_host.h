@@ -19,12 +19,16 @@ namespace bhost {
 struct Prepared {
   std::vector<BatchDesc> descs;  // grouped by kind (kBatchKind order)
   uint64_t nchunks = 0;
-  uint64_t kind_lo[kBatchKinds] = {}, kind_hi[kBatchKinds] = {};  // each kind's chunk range
+  // each kind's chunk range [lo, hi): its staged items in [lo, mid), the
+  // others in [mid, hi)
+  uint64_t kind_lo[kBatchKinds] = {}, kind_mid[kBatchKinds] = {}, kind_hi[kBatchKinds] = {};
   uint32_t staged_w = 0;  // largest words per block staged in shared memory
-  // kernels enqueue launches: the chunk table and one per kind present
-  int kernels() const {
+  // kernels enqueue launches: the chunk table, and per kind present one
+  // persistent kernel or (grid) one grid kernel per non-empty range
+  int kernels(bool grid) const {
     int n = nchunks ? 1 : 0;
-    for (int k = 0; k < kBatchKinds; k++) n += kind_hi[k] > kind_lo[k];
+    for (int k = 0; k < kBatchKinds; k++)
+      n += grid ? (kind_mid[k] > kind_lo[k]) + (kind_hi[k] > kind_mid[k]) : kind_hi[k] > kind_lo[k];
     return n;
   }
   std::vector<std::pair<void*, size_t>> zero;

@@ -108,16 +108,21 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
       return nfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
   }
   uint64_t nchunks = 0;
-  uint64_t lo[gzfp::kBatchKinds], hi[gzfp::kBatchKinds];
+  // per kind: staged items in [lo, mid), the others in [mid, hi), as the
+  // allocating path groups them
+  uint64_t lo[gzfp::kBatchKinds], mid[gzfp::kBatchKinds], hi[gzfp::kBatchKinds];
   uint32_t sw = 0;  // staging depth, as the allocating path chooses it
   int slot = 0;
   for (int k = 0; k < gzfp::kBatchKinds; k++) {
-    lo[k] = nchunks;
-    for (int i = 0; i < count; i++) {
+    lo[k] = mid[k] = nchunks;
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) mid[k] = nchunks;
+      for (int i = 0; i < count; i++) {
       const gzfp_batch_item& it = items[i];
       const int dims = it.nz ? 3 : it.ny ? 2 : 1;
       const uint32_t kind = gzfp::batch_kind(it.type, dims);
       if (kind != gzfp::kBatchKind[k]) continue;
+      if ((gzfp::batch_item_staged_w(decode, it.maxbits) != 0) != (pass == 0)) continue;
       gzfp::BatchDesc& d = g_host[slot++];
       d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
       d.g.vec =
@@ -131,6 +136,7 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
       nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
       const uint32_t w = gzfp::batch_item_staged_w(decode, it.maxbits);
       sw = w > sw ? w : sw;
+      }
     }
     hi[k] = nchunks;
   }
@@ -164,9 +170,18 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   const bool ahead = cfg.claim_ahead != 0;
   for (int k = 0; k < gzfp::kBatchKinds && !e; k++) {
     if (hi[k] == lo[k]) continue;
-    int occ = cfg.ctas_per_sm ? gzfp::batch_occupancy(cfg.threads, decode, k, sw) : 0;
+    if (cfg.ctas_per_sm == 0) {  // grid kernels: the staged items, then the others
+      if (mid[k] > lo[k])
+        e = gzfp::launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, sw, descs,
+                               chunk_item, lo[k], mid[k], counter + k, s);
+      if (!e && hi[k] > mid[k])
+        e = gzfp::launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, 0, descs,
+                               chunk_item, mid[k], hi[k], counter + k, s);
+      continue;
+    }
+    int occ = gzfp::batch_occupancy(cfg.threads, decode, k, sw);
     occ = occ > 1 ? occ : 1;
-    const int grid = cfg.ctas_per_sm ? sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : occ) : 0;
+    const int grid = sms * (cfg.ctas_per_sm < occ ? cfg.ctas_per_sm : occ);
     e = gzfp::launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, descs,
                            chunk_item, lo[k], hi[k], counter + k, s);
   }

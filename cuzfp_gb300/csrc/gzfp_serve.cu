@@ -223,7 +223,7 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
           }
           memcpy(wl.host, p.descs.data(), p.descs.size() * sizeof(gzfp::BatchDesc));
           if ((e = gzfp::bhost::enqueue(p, wl, d == 1, bc, sl.s))) st = scuda(e, "batch launch");
-          kernels += p.kernels();
+          kernels += p.kernels(bc.ctas_per_sm == 0);
         }
         for (size_t j = 0; j < sl.reqs.size() && !st; j++) {
           const gzfp_serve_request& r = reqs[sl.reqs[j]];

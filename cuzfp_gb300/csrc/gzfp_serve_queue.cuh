@@ -47,8 +47,9 @@ constexpr int queue_maxnreg(int minb) { return 65536 / (kQThreads * minb) / 8 * 
 // to finish raises the request's done flag.  The register budget is set with
 // __maxnreg__, not __launch_bounds__: measured on GB300, a device-launched
 // grid of a kernel with launch bounds and dynamic shared memory gets one
-// resident CTA per SM, with __maxnreg__ as many as fit.
-template <bool DECODE, int D, typename T, int MINB>
+// resident CTA per SM, with __maxnreg__ as many as fit.  PATH: kPathStaged
+// (the request stages its words in shared memory) or kPathDirect.
+template <bool DECODE, int D, typename T, int MINB, int PATH>
 __global__ void __maxnreg__(queue_maxnreg(MINB))
     serve_request_kernel(const __grid_constant__ BatchDesc d, uint32_t p, uint32_t staged_w,
                          QueueDev q) {
@@ -57,8 +58,8 @@ __global__ void __maxnreg__(queue_maxnreg(MINB))
   BatchPlanes<kQThreads> ps{smem + table_words<D>() + threadIdx.x, t4};
   uint64_t* sbuf = smem + table_words<D>() + BatchSlots<DECODE, D, T>::value * kQThreads;
   if (threadIdx.x == 0) atomicMin(&q.t_first[p], queue_clock());
-  batch_block<kQThreads, DECODE, D, T>(d, (uint64_t)blockIdx.x * kQThreads + threadIdx.x, ps,
-                                       sbuf, staged_w);
+  batch_block<kQThreads, DECODE, D, T, PATH>(d, (uint64_t)blockIdx.x * kQThreads + threadIdx.x,
+                                             ps, sbuf, staged_w);
   __syncthreads();  // the CTA's blocks are written
   if (threadIdx.x == 0) {
     __threadfence();
@@ -89,24 +90,33 @@ struct QueueCoder {
     return batch_smem_bytes<kQThreads, DECODE, D, T>(DECODE ? kBatchMaxStagedWords
                                                             : kMaxStagedOut);
   }
+  template <int M, int PATH>
+  __device__ static void go(const QueueReq& r, uint32_t p, uint32_t sw, size_t smem,
+                            const QueueDev& q) {
+    serve_request_kernel<DECODE, D, T, M, PATH>
+        <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
+  }
   __device__ static cudaError_t launch(const QueueReq& r, uint32_t p, const QueueDev& q) {
     const uint32_t sw = staged_w(r.d.maxbits);
     const size_t smem = batch_smem_bytes<kQThreads, DECODE, D, T>(sw);
-    if (WIDE != MB && batch_smem_fits(smem, WIDE))
-      serve_request_kernel<DECODE, D, T, WIDE>
-          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
+    const bool wide = WIDE != MB && batch_smem_fits(smem, WIDE);
+    if (sw)
+      wide ? go<WIDE, kPathStaged>(r, p, sw, smem, q) : go<MB, kPathStaged>(r, p, sw, smem, q);
     else
-      serve_request_kernel<DECODE, D, T, MB>
-          <<<r.ctas, kQThreads, smem, cudaStreamFireAndForget>>>(r.d, p, sw, q);
+      wide ? go<WIDE, kPathDirect>(r, p, sw, smem, q) : go<MB, kPathDirect>(r, p, sw, smem, q);
     return cudaGetLastError();
   }
-  static cudaError_t setup() {
-    cudaError_t e = cudaFuncSetAttribute(serve_request_kernel<DECODE, D, T, MB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_smem());
-    if (e || WIDE == MB) return e;
-    return cudaFuncSetAttribute(serve_request_kernel<DECODE, D, T, WIDE>,
+  template <int M, int PATH>
+  static cudaError_t attr() {
+    return cudaFuncSetAttribute(serve_request_kernel<DECODE, D, T, M, PATH>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem());
+  }
+  static cudaError_t setup() {
+    cudaError_t e;
+    if ((e = attr<MB, kPathStaged>()) || (e = attr<MB, kPathDirect>())) return e;
+    if (WIDE == MB) return cudaSuccess;
+    if ((e = attr<WIDE, kPathStaged>()) || (e = attr<WIDE, kPathDirect>())) return e;
+    return cudaSuccess;
   }
 };
 
