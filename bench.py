@@ -75,6 +75,11 @@ def parse():
     p.add_argument("--max-batch", type=int, default=256, help="serving workload: requests per batch")
     p.add_argument("--load", type=float, default=0.7,
                    help="serving workload: arrival rate as a fraction of plain-path capacity")
+    p.add_argument("--batch-compress-config", default="",
+                   help="batched workload: threads,ctas_per_sm,blocks_per_thread,claim_ahead of "
+                        "the compress plan instead of the autotuner's choice")
+    p.add_argument("--batch-decompress-config", default="",
+                   help="batched workload: the same for the decompress plan")
     args = p.parse_args()
     global SHAPE, RATE, WORKLOAD
     SHAPE = (args.edge,) * 3
@@ -310,11 +315,17 @@ def run_batched(args, rank, world, local, emit=True):
             if lib.gzfp_decompress_bits(*a) != 0:
                 raise RuntimeError(lib.gzfp_last_error().decode())
 
+    def launch_shape(spec, decompress, out):
+        # a fixed shape (so that a profiler's run codes with the kernels the
+        # timed run chose), or the autotuner's
+        if spec:
+            return gz.BatchConfig(*[int(v) for v in spec.split(",")]), None
+        return gz.autotune_batch(fields if not decompress else out, batch_s, rates,
+                                 decompress=decompress, repeats=2, cuda_stream=stream)
+
     t0 = time.perf_counter()
-    cfg_c, ms_c = gz.autotune_batch(fields, batch_s, rates, decompress=False, repeats=2,
-                                    cuda_stream=stream)
-    cfg_d, ms_d = gz.autotune_batch(batch_o, batch_s, rates, decompress=True, repeats=2,
-                                    cuda_stream=stream)
+    cfg_c, ms_c = launch_shape(args.batch_compress_config, False, None)
+    cfg_d, ms_d = launch_shape(args.batch_decompress_config, True, batch_o)
     tune_s = time.perf_counter() - t0
     cplan = gz.BatchPlan(fields, batch_s, rates, decompress=False, config=cfg_c)
     dplan = gz.BatchPlan(batch_o, batch_s, rates, decompress=True, config=cfg_d)
