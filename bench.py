@@ -537,6 +537,38 @@ def run_serving(args, rank, world, local, emit=True):
     ok = ok and all(r.status == 0 for r in res_s)
 
     bit_identical = bit_q and ok and all(_same_bits(expect[i], check[i]) for i in sample)
+
+    # one 384^3 rate-16 request alone, per kind: the device queue's grid
+    # (device-clock span of its CTAs, median of 3 runs) against the plain
+    # call (CUDA events, mean of 5)
+    lone = {}
+    for dt in ("float32", "float64"):
+        x = field(384, dt)
+        w = gz.compress_tensor(x, 16.0)
+        w_out, x_out = torch.empty_like(w), torch.empty_like(x)
+        for op, name in ((0, "compress"), (1, "decompress")):
+            def plain():
+                if op == 0:
+                    gz.compress_tensor(x, 16.0, out=w_out, cuda_stream=stream)
+                else:
+                    gz.decompress_tensor(w, x.shape, dts[dt], 16.0, out=x_out, cuda_stream=stream)
+            plain()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(5):
+                plain()
+            b.record(stream)
+            b.synchronize()
+            spans = []
+            for _ in range(3):
+                rq = (gz.serve_request(0, x, 16.0, 0.0) if op == 0 else
+                      gz.serve_request(1, w, 16.0, 0.0, shape=x.shape, dtype=dts[dt]))
+                r1, _ = gz.serve([rq], qcfg)
+                spans.append(r1[0].device_end - r1[0].device_start)
+            lone[f"{name}_{dt}"] = {"plain_ms": round(a.elapsed_time(b) / 5, 4),
+                                    "queue_ms": round(float(np.median(spans)) * 1e3, 4)}
     if rank != 0:
         return
     p50, p99 = np.percentile(lat, 50), np.percentile(lat, 99)
@@ -565,6 +597,7 @@ def run_serving(args, rank, world, local, emit=True):
                                  "p99": round(np.percentile(lat_s, 99) * 1e3, 4)},
                   "saturated_gbs": round(nbytes.sum() / ssstats.wall / 1e9, 2),
                   "stats": stats_s.as_dict()},
+        "lone_384cube_rate16": lone,
         "bit_identical_sample": bool(bit_identical), "checked": len(sample),
         "gpu_launches": int(stats.kernels), "clocks": clk.summary(),
     }
@@ -932,6 +965,7 @@ def run(args, rank, world, local):
                        "slots_latency_ms": s["slots"]["latency_ms"],
                        "served_gbs": s["served_gbs"], "saturated_vs_plain": s["saturated_vs_plain"],
                        "mean_inflight": round(s["stats"]["mean_inflight"], 3),
+                       "lone_384cube_rate16": s["lone_384cube_rate16"],
                        "bit_identical_sample": s["bit_identical_sample"]}
         torch.cuda.empty_cache()
 
