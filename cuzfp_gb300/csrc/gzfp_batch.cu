@@ -56,15 +56,15 @@ bool valid_config(const gzfp_batch_config& c) {
                                  c.blocks_per_thread == 4);
 }
 
-int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
-            Prepared& p) {
-  if (!items || count < 0 || count > kMaxBatchItems) return bfail(GZFP_ERR_ARG, "bad item list");
-  const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
-  p.descs.resize(count);
-  p.nchunks = 0;
-  p.staged_w = 0;
-  p.zero.clear();
-  std::vector<int> kind_of(count);
+// kind index of an item (its type and shape already validated)
+static int item_kind(const gzfp_batch_item& it) {
+  const int dims = it.nz ? 3 : it.ny ? 2 : 1;
+  return batch_kind_index(batch_kind(it.type, dims));
+}
+
+int layout(const gzfp_batch_item* items, int count, bool decode, uint64_t chunk_blocks,
+           BatchDesc* descs, Layout& L) {
+  L = Layout{};
   for (int i = 0; i < count; i++) {
     const gzfp_batch_item& it = items[i];
     if (!batch_type_ok(it.type)) return bfail(GZFP_ERR_UNSUPPORTED, "unknown scalar type");
@@ -72,41 +72,54 @@ int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_bat
     if (!it.field || !it.stream) return bfail(GZFP_ERR_ARG, "null pointer");
     if (it.maxbits < batch_ebits(it.type) + 1 || it.maxbits > (1u << 20))
       return bfail(GZFP_ERR_ARG, "bits per block out of range");
-    const int dims = it.nz ? 3 : it.ny ? 2 : 1;
     const Geom g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
     if (g.nblocks >= (1ull << 32)) return bfail(GZFP_ERR_ARG, "too many blocks");
     const uint64_t nwords = (g.nblocks * it.maxbits + 63) / 64;
     if (it.stream_capacity < nwords * 8)
       return bfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
-    kind_of[i] = batch_kind_index(batch_kind(it.type, dims));
   }
   // descriptors grouped by kind, so each kind's chunks form one range, and
   // within a kind the staged items first
   int slot = 0;
   for (int k = 0; k < kBatchKinds; k++) {
-    p.kind_lo[k] = p.nchunks;
+    L.lo[k] = L.nchunks;
     for (int pass = 0; pass < 2; pass++) {
-      if (pass == 1) p.kind_mid[k] = p.nchunks;
+      if (pass == 1) L.mid[k] = L.nchunks;
       for (int i = 0; i < count; i++) {
-      if (kind_of[i] != k) continue;
-      const gzfp_batch_item& it = items[i];
-      if ((batch_item_staged_w(decode, it.maxbits) != 0) != (pass == 0)) continue;
-      BatchDesc& d = p.descs[slot++];
-      d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-      d.g.vec = (it.nx % 4 == 0 && (uintptr_t)it.field % batch_row_align(it.type) == 0) ? 1u : 0u;
-      d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
-      d.maxbits = it.maxbits;
-      d.kind = kBatchKind[k];
-      d.in = decode ? it.stream : it.field;
-      d.out = decode ? it.field : it.stream;
-      d.first_chunk = p.nchunks;
-      p.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
-      if (!decode && it.maxbits % 64) p.zero.push_back({it.stream, (size_t)(d.nwords * 8)});
-      p.staged_w = std::max(p.staged_w, batch_item_staged_w(decode, it.maxbits));
+        const gzfp_batch_item& it = items[i];
+        if (item_kind(it) != k) continue;
+        if ((batch_item_staged_w(decode, it.maxbits) != 0) != (pass == 0)) continue;
+        BatchDesc& d = descs[slot++];
+        d.g = make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
+        d.g.vec =
+            (it.nx % 4 == 0 && (uintptr_t)it.field % batch_row_align(it.type) == 0) ? 1u : 0u;
+        d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
+        d.maxbits = it.maxbits;
+        d.kind = kBatchKind[k];
+        d.in = decode ? it.stream : it.field;
+        d.out = decode ? it.field : it.stream;
+        d.first_chunk = L.nchunks;
+        L.nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
+        L.staged_w = std::max(L.staged_w, batch_item_staged_w(decode, it.maxbits));
       }
     }
-    p.kind_hi[k] = p.nchunks;
+    L.hi[k] = L.nchunks;
   }
+  return GZFP_OK;
+}
+
+int prepare(const gzfp_batch_item* items, int count, bool decode, const gzfp_batch_config& cfg,
+            Prepared& p) {
+  if (!items || count < 0 || count > kMaxBatchItems) return bfail(GZFP_ERR_ARG, "bad item list");
+  p.descs.resize(count);
+  p.zero.clear();
+  const int st = layout(items, count, decode, (uint64_t)cfg.threads * cfg.blocks_per_thread,
+                        p.descs.data(), p.lay);
+  if (st) return st;
+  // streams whose blocks share edge words are zeroed before an encode
+  if (!decode)
+    for (const BatchDesc& d : p.descs)
+      if (d.maxbits % 64) p.zero.push_back({d.out, (size_t)(d.nwords * 8)});
   return GZFP_OK;
 }
 
@@ -154,39 +167,39 @@ cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_bat
                     cudaStream_t s) {
   cudaError_t e;
   const int count = (int)p.descs.size();
-  if (count == 0 || p.nchunks == 0) return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
+  if (count == 0 || p.lay.nchunks == 0) return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
   for (const auto& z : p.zero)
     if ((e = cudaMemsetAsync(z.first, 0, z.second, s))) return e;
   if ((e = cudaMemcpyAsync(wl.descs, wl.host, count * sizeof(BatchDesc),
                            cudaMemcpyHostToDevice, s)))
     return e;
   const dim3 tgrid(64, (unsigned)count);
-  batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.nchunks);
+  batch_chunk_table<<<tgrid, 256, 0, s>>>(wl.descs, count, wl.chunk_item, p.lay.nchunks);
   if ((e = cudaGetLastError())) return e;
   if ((e = cudaMemsetAsync(wl.counter, 0, kBatchKinds * sizeof(unsigned long long), s))) return e;
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev))) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev))) return e;
-  const uint32_t sw = p.staged_w;
+  const uint32_t sw = p.lay.staged_w;
   const bool ahead = cfg.claim_ahead != 0;
   // per kind present, in sequence on the stream: one persistent kernel, or
   // (ctas_per_sm 0) the grid kernel over the staged items and the grid
   // kernel over the others
   for (int k = 0; k < kBatchKinds && !e; k++) {
-    if (p.kind_hi[k] == p.kind_lo[k]) continue;
+    if (p.lay.hi[k] == p.lay.lo[k]) continue;
     if (cfg.ctas_per_sm == 0) {
-      if (p.kind_mid[k] > p.kind_lo[k])
+      if (p.lay.mid[k] > p.lay.lo[k])
         e = launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, sw, wl.descs,
-                         wl.chunk_item, p.kind_lo[k], p.kind_mid[k], wl.counter + k, s);
-      if (!e && p.kind_hi[k] > p.kind_mid[k])
+                         wl.chunk_item, p.lay.lo[k], p.lay.mid[k], wl.counter + k, s);
+      if (!e && p.lay.hi[k] > p.lay.mid[k])
         e = launch_batch(cfg.threads, decode, k, 0, cfg.blocks_per_thread, false, 0, wl.descs,
-                         wl.chunk_item, p.kind_mid[k], p.kind_hi[k], wl.counter + k, s);
+                         wl.chunk_item, p.lay.mid[k], p.lay.hi[k], wl.counter + k, s);
       continue;
     }
     const int grid =
         sms * std::min(cfg.ctas_per_sm, std::max(1, batch_occupancy(cfg.threads, decode, k, sw)));
     e = launch_batch(cfg.threads, decode, k, grid, cfg.blocks_per_thread, ahead, sw, wl.descs,
-                     wl.chunk_item, p.kind_lo[k], p.kind_hi[k], wl.counter + k, s);
+                     wl.chunk_item, p.lay.lo[k], p.lay.hi[k], wl.counter + k, s);
   }
   if (e) return e;
   return wl.done ? cudaEventRecord(wl.done, s) : cudaSuccess;
@@ -229,7 +242,7 @@ int run_batch(const gzfp_batch_item* items, int count, const gzfp_batch_config* 
   // on whatever stream it ran, has finished with it
   if (dw.wl.done && (e = cudaEventSynchronize(dw.wl.done)))
     return bcuda(e, "cudaEventSynchronize(previous batch)");
-  if ((e = dw.wl.reserve(p.descs.size(), p.nchunks))) return bcuda(e, "batch work list allocation");
+  if ((e = dw.wl.reserve(p.descs.size(), p.lay.nchunks))) return bcuda(e, "batch work list allocation");
   memcpy(dw.wl.host, p.descs.data(), p.descs.size() * sizeof(gzfp::BatchDesc));
   if ((e = enqueue(p, dw.wl, decode, cfg, s))) return bcuda(e, "batch launch");
   return GZFP_OK;
@@ -287,7 +300,7 @@ int gzfp_batch_plan_create(const gzfp_batch_item* items, int count, int decompre
   cudaError_t e = cudaSuccess;
   cudaStream_t s = nullptr;
   if (!st && (e = cudaGetDevice(&plan->device))) st = bcuda(e, "cudaGetDevice");
-  if (!st && (e = plan->wl.reserve(plan->p.descs.size(), plan->p.nchunks)))
+  if (!st && (e = plan->wl.reserve(plan->p.descs.size(), plan->p.lay.nchunks)))
     st = bcuda(e, "plan work list allocation");
   if (!st) memcpy(plan->wl.host, plan->p.descs.data(), plan->p.descs.size() * sizeof(gzfp::BatchDesc));
   if (!st && (e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking))) st = bcuda(e, "cudaStreamCreate");

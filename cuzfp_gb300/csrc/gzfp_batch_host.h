@@ -14,21 +14,34 @@
 namespace gzfp {
 namespace bhost {
 
-// Host-side description of a batch: descriptors, chunk count, and the
+// The layout of a batch's descriptors: per kind its chunk range [lo, hi),
+// its staged items in [lo, mid) and the others in [mid, hi); the chunk
+// count; the largest words per block staged in shared memory.
+struct Layout {
+  uint64_t nchunks = 0;
+  uint64_t lo[kBatchKinds] = {}, mid[kBatchKinds] = {}, hi[kBatchKinds] = {};
+  uint32_t staged_w = 0;
+};
+
+// Validate `items` and write one descriptor per item into descs[0..count),
+// grouped by kind (kBatchKind order), each kind's staged items first, with
+// chunks of chunk_blocks blocks.  No heap use: the no-alloc entry point
+// calls it too.  Returns a gzfp status (the detail goes to
+// gzfp_batch_last_error).
+int layout(const gzfp_batch_item* items, int count, bool decode, uint64_t chunk_blocks,
+           BatchDesc* descs, Layout& L);
+
+// Host-side description of a batch: descriptors, their layout, and the
 // streams whose blocks share words (zeroed before an encode launch).
 struct Prepared {
-  std::vector<BatchDesc> descs;  // grouped by kind (kBatchKind order)
-  uint64_t nchunks = 0;
-  // each kind's chunk range [lo, hi): its staged items in [lo, mid), the
-  // others in [mid, hi)
-  uint64_t kind_lo[kBatchKinds] = {}, kind_mid[kBatchKinds] = {}, kind_hi[kBatchKinds] = {};
-  uint32_t staged_w = 0;  // largest words per block staged in shared memory
+  std::vector<BatchDesc> descs;
+  Layout lay;
   // kernels enqueue launches: the chunk table, and per kind present one
   // persistent kernel or (grid) one grid kernel per non-empty range
   int kernels(bool grid) const {
-    int n = nchunks ? 1 : 0;
+    int n = lay.nchunks ? 1 : 0;
     for (int k = 0; k < kBatchKinds; k++)
-      n += grid ? (kind_mid[k] > kind_lo[k]) + (kind_hi[k] > kind_mid[k]) : kind_hi[k] > kind_lo[k];
+      n += grid ? (lay.mid[k] > lay.lo[k]) + (lay.hi[k] > lay.mid[k]) : lay.hi[k] > lay.lo[k];
     return n;
   }
   std::vector<std::pair<void*, size_t>> zero;

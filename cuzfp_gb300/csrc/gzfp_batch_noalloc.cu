@@ -35,8 +35,7 @@ static_assert(sizeof(gzfp::BatchDesc) % 8 == 0, "descriptor alignment");
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices];  // per device, set once
-std::mutex g_mu;                    // guards g_scratch_addr and g_host
+std::mutex g_mu;                    // guards g_host
 gzfp::BatchDesc g_host[kMaxItems];  // descriptors of the call in flight on the host
 
 // failures are reported through gzfp_batch_last_error
@@ -80,66 +79,33 @@ extern "C" int gzfp_batch_run_noalloc(const gzfp_batch_item* items, int count, i
   if (e) return ncuda(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return nfail(GZFP_ERR_CUDA, "device index out of range");
 
+  // a capture would record the pageable descriptor upload from g_host, and
+  // a replay would upload whatever a later call left there
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if ((e = cudaStreamIsCapturing(s, &cap))) return ncuda(e, "cudaStreamIsCapturing");
+  if (cap != cudaStreamCaptureStatusNone)
+    return nfail(GZFP_ERR_ARG, "the no-alloc batch call cannot be captured in a CUDA graph");
+
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    if ((e = cudaGetSymbolAddress(&p, g_scratch)))
-      return ncuda(e, "cudaGetSymbolAddress(no-alloc scratch)");
-    g_scratch_addr[dev] = p;
-  }
-  unsigned char* base = (unsigned char*)g_scratch_addr[dev];
+  // the scratch's address in the current context (looked up on every call:
+  // the runtime caches it, and a reset context reloads the module)
+  void* scratch = nullptr;
+  if ((e = cudaGetSymbolAddress(&scratch, g_scratch)))
+    return ncuda(e, "cudaGetSymbolAddress(no-alloc scratch)");
+  unsigned char* base = (unsigned char*)scratch;
   unsigned long long* counter = (unsigned long long*)base;
   gzfp::BatchDesc* descs = (gzfp::BatchDesc*)(base + kDescOffset);
   uint32_t* chunk_item = (uint32_t*)(base + kTableOffset);
 
-  // descriptors: the same validation and layout as the allocating batch
-  // path -- grouped by kind, so each kind's chunks form one range
-  const uint64_t chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
-  for (int i = 0; i < count; i++) {
-    const gzfp_batch_item& it = items[i];
-    if (!gzfp::batch_type_ok(it.type)) return nfail(GZFP_ERR_UNSUPPORTED, "unknown scalar type");
-    if (it.nx == 0 || (it.nz != 0 && it.ny == 0)) return nfail(GZFP_ERR_ARG, "bad dimensions");
-    if (!it.field || !it.stream) return nfail(GZFP_ERR_ARG, "null pointer");
-    if (it.maxbits < gzfp::batch_ebits(it.type) + 1 || it.maxbits > (1u << 20))
-      return nfail(GZFP_ERR_ARG, "bits per block out of range");
-    const gzfp::Geom g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-    if (g.nblocks >= (1ull << 32)) return nfail(GZFP_ERR_ARG, "too many blocks");
-    if (it.stream_capacity < (g.nblocks * it.maxbits + 63) / 64 * 8)
-      return nfail(decode ? GZFP_ERR_ARG : GZFP_ERR_CAPACITY, "stream buffer too small");
-  }
-  uint64_t nchunks = 0;
-  // per kind: staged items in [lo, mid), the others in [mid, hi), as the
-  // allocating path groups them
-  uint64_t lo[gzfp::kBatchKinds], mid[gzfp::kBatchKinds], hi[gzfp::kBatchKinds];
-  uint32_t sw = 0;  // staging depth, as the allocating path chooses it
-  int slot = 0;
-  for (int k = 0; k < gzfp::kBatchKinds; k++) {
-    lo[k] = mid[k] = nchunks;
-    for (int pass = 0; pass < 2; pass++) {
-      if (pass == 1) mid[k] = nchunks;
-      for (int i = 0; i < count; i++) {
-      const gzfp_batch_item& it = items[i];
-      const int dims = it.nz ? 3 : it.ny ? 2 : 1;
-      const uint32_t kind = gzfp::batch_kind(it.type, dims);
-      if (kind != gzfp::kBatchKind[k]) continue;
-      if ((gzfp::batch_item_staged_w(decode, it.maxbits) != 0) != (pass == 0)) continue;
-      gzfp::BatchDesc& d = g_host[slot++];
-      d.g = gzfp::make_geom_blocks(it.nx, it.ny ? it.ny : 1, it.nz ? it.nz : 1);
-      d.g.vec =
-          (it.nx % 4 == 0 && (uintptr_t)it.field % gzfp::batch_row_align(it.type) == 0) ? 1u : 0u;
-      d.nwords = (d.g.nblocks * it.maxbits + 63) / 64;
-      d.maxbits = it.maxbits;
-      d.kind = kind;
-      d.in = decode ? it.stream : it.field;
-      d.out = decode ? it.field : it.stream;
-      d.first_chunk = nchunks;
-      nchunks += (d.g.nblocks + chunk_blocks - 1) / chunk_blocks;
-      const uint32_t w = gzfp::batch_item_staged_w(decode, it.maxbits);
-      sw = w > sw ? w : sw;
-      }
-    }
-    hi[k] = nchunks;
-  }
+  // descriptors: the allocating batch path's validation and layout, into
+  // the host array
+  gzfp::bhost::Layout L;
+  const int st = gzfp::bhost::layout(items, count, decode,
+                                     (uint64_t)cfg.threads * cfg.blocks_per_thread, g_host, L);
+  if (st) return st;
+  const uint64_t nchunks = L.nchunks, chunk_blocks = (uint64_t)cfg.threads * cfg.blocks_per_thread;
+  const uint64_t *lo = L.lo, *mid = L.mid, *hi = L.hi;
+  const uint32_t sw = L.staged_w;
   if (nchunks > kMaxChunks) {
     char msg[160];
     snprintf(msg, sizeof msg, "batch needs %llu chunks of %llu blocks; the no-alloc scratch holds %llu",

@@ -217,7 +217,7 @@ int gzfp_serve_run(const gzfp_serve_request* reqs, int count, const gzfp_serve_c
           if ((st = gzfp::bhost::prepare(items[d].data(), (int)items[d].size(), d == 1, bc, p)))
             break;
           // the slot is free, so nothing in flight still reads its work list
-          if ((e = wl.reserve(p.descs.size(), p.nchunks))) {
+          if ((e = wl.reserve(p.descs.size(), p.lay.nchunks))) {
             st = scuda(e, "slot work list");
             break;
           }

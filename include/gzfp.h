@@ -314,10 +314,11 @@ int gzfp_batch_autotune(const gzfp_batch_item* items, int count, int decompress,
    blocks = 2^26 blocks at the default shape); larger batches are rejected
    with GZFP_ERR_CAPACITY and a message naming the limit, before any GPU work.
 
-   Set-up: the first call on each device, with that device current, looks up
-   the array's device address (cudaGetSymbolAddress); with lazy module loading
-   this is also when the driver loads the module, so make the first call
-   before any stream capture.  No graph-capture support is claimed.
+   Set-up: every call looks up the array's device address in the current
+   context (cudaGetSymbolAddress); with lazy module loading the first call on
+   a device is also when the driver loads the module.  A call on a stream
+   that is being captured into a CUDA graph is refused with GZFP_ERR_ARG
+   before any work is queued.
 
    The call waits on the host for earlier work on `cuda_stream` (the
    descriptor upload is a pageable copy) and then queues its work

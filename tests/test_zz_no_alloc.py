@@ -101,3 +101,26 @@ def test_noalloc_rejects_oversized_batches(gz, cuda):
     cfg = gz.BatchConfig(64, 1, 1, 0)
     assert run(one, 1, 0, ctypes.byref(cfg), None) == gz.GZFP_ERR_CAPACITY
     assert b"chunks" in gz._lib.gzfp_batch_last_error()
+
+
+def test_noalloc_rejects_stream_capture(gz, cuda):
+    """A call on a capturing stream is refused before any work is queued
+    (a captured pageable upload from the shared host array would replay
+    whatever a later call left there); the capture itself still ends
+    cleanly."""
+    import torch
+    run = _bind(gz)
+    f = torch.zeros((16, 16, 16), dtype=torch.float32, device=cuda)
+    w = gz.batch_stream_buffers([f], [8.0])
+    items = gz.batch_items([f], w, [8.0])
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        st = run(items, 1, 0, None, ctypes.c_void_p(s.cuda_stream))
+        f.add_(1.0)  # the capture records something of its own
+    assert st == gz.GZFP_ERR_ARG
+    assert b"captured" in gz._lib.gzfp_batch_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(f[0, 0, 0]) == 1.0  # the captured add ran once, at the replay
