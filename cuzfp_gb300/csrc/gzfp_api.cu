@@ -74,6 +74,29 @@ bool is_device_pointer(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The device address of host memory that the kernels may read and write in
+// place, else null: memory pinned or registered with CUDA, on a device whose
+// host link is hardware-coherent (it uses the host's page tables, as a
+// Grace-Blackwell part's chip-to-chip link does).  There the kernels reach
+// the link's bandwidth (measured on GB300: 211 GB/s host to device and 193
+// GB/s back, the copy engines' figures), so no slab pipeline is needed.
+void* direct_host_alias(const void* p) {
+  int dev = 0, coherent = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (!coherent) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Host-staged calls are cut into slabs of whole block layers along the
 // slowest axis (z in 3D, y in 2D, x in 1D).  A slab's values are one
 // contiguous run of the array and its blocks one contiguous run of the
@@ -361,10 +384,23 @@ int gzfp_compress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsigned
   cudaStream_t s = (cudaStream_t)cuda_stream;
   const bool dev_data = is_device_pointer(data);
   const bool dev_stream = is_device_pointer(stream);
-  if (!dev_data || !dev_stream)
+  cudaError_t e;
+  if (!dev_data || !dev_stream) {
+    // pinned host memory on a coherent link: the kernel codes it in place
+    // (blocks of whole words only: shared words are merged with atomics,
+    // which stay in device memory); the call returns when it is done
+    const void* hd = dev_data ? data : direct_host_alias(data);
+    void* hs = dev_stream ? stream : direct_host_alias(stream);
+    if (hd && hs && maxbits % 64 == 0) {
+      g.vec = rows_vectorizable(hd, nx, type);
+      if ((e = encode_launch(type, dims, hd, g, maxbits, (uint64_t*)hs, nwords, s)))
+        return cuda_fail(e, "encode kernel launch");
+      if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "encode kernel");
+      return GZFP_OK;
+    }
     return staged(false, type, dims, g, maxbits, (void*)data, dev_data, (uint64_t*)stream,
                   dev_stream, s);
-  cudaError_t e;
+  }
   if (maxbits % 64 != 0) {
     // blocks share boundary words, which the kernel ORs into a zeroed stream
     if ((e = cudaMemsetAsync(stream, 0, bytes, s))) return cuda_fail(e, "cudaMemsetAsync(stream)");
@@ -390,10 +426,22 @@ int gzfp_decompress_bits(int type, unsigned nx, unsigned ny, unsigned nz, unsign
   cudaStream_t s = (cudaStream_t)cuda_stream;
   const bool dev_data = is_device_pointer(data);
   const bool dev_stream = is_device_pointer(stream);
-  if (!dev_data || !dev_stream)
+  cudaError_t e;
+  if (!dev_data || !dev_stream) {
+    // pinned host memory on a coherent link: decoded in place (see above)
+    void* hd = dev_data ? data : direct_host_alias(data);
+    const void* hs = dev_stream ? stream : direct_host_alias(stream);
+    if (hd && hs) {
+      g.vec = rows_vectorizable(hd, nx, type);
+      if ((e = decode_launch(type, dims, (const uint64_t*)hs, nwords, g, maxbits, hd, s)))
+        return cuda_fail(e, "decode kernel launch");
+      if ((e = cudaStreamSynchronize(s))) return cuda_fail(e, "decode kernel");
+      return GZFP_OK;
+    }
     return staged(true, type, dims, g, maxbits, data, dev_data, (uint64_t*)stream, dev_stream, s);
+  }
   g.vec = rows_vectorizable(data, nx, type);
-  cudaError_t e = decode_launch(type, dims, (const uint64_t*)stream, nwords, g, maxbits, data, s);
+  e = decode_launch(type, dims, (const uint64_t*)stream, nwords, g, maxbits, data, s);
   if (e) return cuda_fail(e, "decode kernel launch");
   return GZFP_OK;
 }

@@ -159,12 +159,16 @@ def test_testzfp_pins(gz, cuda, dt, d):
         assert float(np.max(np.abs(f - g))) <= tol
 
 
-def test_host_and_pinned_pointers(gz, orc, cuda):
-    """cuZFP's host-pointer path: arrays and streams in host memory."""
+@pytest.mark.parametrize("rate", [12.0, 7.3])
+def test_host_and_pinned_pointers(gz, orc, cuda, rate):
+    """cuZFP's host-pointer path: arrays and streams in host memory.  On a
+    coherent host link pinned buffers are coded in place by the kernels
+    (rate 12: whole-word blocks), or staged through device memory (rate
+    7.3: blocks that share words, compression only); pageable buffers are
+    always staged."""
     import torch
     rng = np.random.default_rng(3)
     a = rng.standard_normal((19, 23, 29)).astype(np.float64)
-    rate = 12.0
     s_ref = orc.compress(a, rate)
     for pinned in (False, True):
         src = torch.from_numpy(a)
