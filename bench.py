@@ -937,8 +937,8 @@ def run(args, rank, world, local):
                "ms_per_step": round(e_ms, 3),
                "h2d_bytes_per_step": nbytes + sbytes, "d2h_bytes_per_step": sbytes + nbytes}
 
-    # the batched workload's summary (512 mixed arrays, graph-captured
-    # persistent launches against plain launches), so that one run records it
+    # the batched workload's summary (512 mixed arrays, graph-captured batch
+    # launches against plain launches), so that one run records it
     batched = None
     if not args.no_batched:
         bargs = argparse.Namespace(**vars(args))
@@ -993,6 +993,13 @@ def run(args, rank, world, local):
         cpu = {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"the whole {nbytes >> 20} MiB field, compress+decompress, best of 2",
                "compress_gbs": round(c_gbs, 4), "decompress_gbs": round(d_gbs, 4)}
+        # zfp 0.5.0 as shipped is serial: one thread on the first 64 z-planes
+        part = host[: min(64, host.shape[0])]
+        g1, c1, d1, _, _ = cpu_measure(part, RATE, 1)
+        cpu["single_thread"] = {"value": round(g1, 4), "compress_gbs": round(c1, 4),
+                                "decompress_gbs": round(d1, 4), "cores": 1,
+                                "sample": f"the first {part.shape[0]} z-planes "
+                                          f"({part.nbytes >> 20} MiB), compress+decompress"}
         # the CPU leg coded the very field the GPU coded: compare the whole
         # stream and the whole decoded array bit for bit, for the timed
         # device-buffer run and for the host-buffer (e2e) run
