@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--workload", default="plain3d",
                    choices=["plain3d", "batched", "serving", "accuracy", "edges"],
                    help="plain3d: the 1 GiB 3D float64 field (default); batched: 512 mixed "
-                        "3D arrays in one persistent launch vs 512 plain launches; serving: "
+                        "3D arrays in one graph-captured batch vs 512 plain launches; serving: "
                         "Poisson request arrivals through the request server; accuracy: the "
                         "plain3d field in zfp's fixed-accuracy mode; edges: the 1D and 2D "
                         "fields with partial edge blocks at rates 4, 12 and 24")
@@ -270,9 +270,23 @@ def batched_arrays(n_arrays: int, seed: int = 0):
     return specs
 
 
+def batch_launches(gz, specs, cfg, decompress: bool) -> int:
+    """Kernels one batch launches: the chunk table, and per kind present one
+    persistent kernel (ctas_per_sm > 0) or one grid kernel per non-empty
+    range of its items, those staged in shared memory (whole 64-bit words,
+    at most 32 per block to decode, 16 to encode) and the others."""
+    ranges = set()
+    for _, dt, r, _ in specs:
+        t = gz._type_of(dt)
+        mb = gz._lib.gzfp_rate_to_maxbits(int(t), 3, r)
+        staged = mb % 64 == 0 and mb // 64 <= (32 if decompress else 16)
+        ranges.add((dt, staged if cfg.ctas_per_sm == 0 else None))
+    return 1 + len(ranges)
+
+
 def run_batched(args, rank, world, local, emit=True):
-    """512 mixed arrays: one graph-captured persistent launch per direction
-    against 512 plain launches per direction (same stream, device buffers).
+    """512 mixed arrays: one graph-captured batch per direction against 512
+    plain launches per direction (same stream, device buffers).
     Prints the result line when `emit`, and returns it (on rank 0)."""
     import torch
 
@@ -390,9 +404,11 @@ def run_batched(args, rank, world, local, emit=True):
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round((2 * nbytes + 2 * sbytes) / (batch_ms * 1e-3) / 1e9 / peak, 4),
                      "traffic": None},
-        # per step and direction: the chunk-table kernel and one persistent
-        # kernel per kind (all arrays are 3D: one kind per scalar type)
-        "gpu_launches": 2 * (1 + len({dt for _, dt, _, _ in specs})) * args.steps,
+        # per step and direction: the chunk-table kernel, and per kind (all
+        # arrays are 3D: one kind per scalar type) one persistent kernel or a
+        # grid kernel per non-empty range (staged items, the others)
+        "gpu_launches": (batch_launches(gz, specs, cfg_c, False) +
+                         batch_launches(gz, specs, cfg_d, True)) * args.steps,
         "clocks": clk.summary(),
     }
     if emit:
@@ -511,8 +527,9 @@ def run_serving(args, rank, world, local, emit=True):
                                             shape=(e, e, e), dtype=dts[dt], copy_to=cp))
         return out
 
-    # the device-queue server (one persistent kernel drains published
-    # requests) and, beside it, the slot server (a batch per free slot)
+    # the device-queue server (a persistent scheduler drains published
+    # requests and launches each from the device) and, beside it, the slot
+    # server (a batch per free slot)
     qcfg = gz.default_serve_config()
     qcfg.budget_bytes = 40 << 30
     qcfg.max_batch = args.max_batch

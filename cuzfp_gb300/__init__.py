@@ -867,7 +867,7 @@ def batch_stream_buffers(fields, rates):
 
 def compress_batch(fields, rates, streams=None, config: Optional[BatchConfig] = None,
                    cuda_stream: Any = None):
-    """Compress many CUDA arrays with one persistent kernel; returns the
+    """Compress many CUDA arrays with the batched kernels; returns the
     stream word tensors (one per array)."""
     if streams is None:
         streams = batch_stream_buffers(fields, rates)

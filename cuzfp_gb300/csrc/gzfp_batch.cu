@@ -1,7 +1,7 @@
 // gzfp_batch.cu -- host side of the batched path (include/gzfp.h, "batch").
 //
 // Builds the device work list of a batch (array descriptors and the
-// chunk -> array table), launches the persistent kernel, captures the whole
+// chunk -> array table), launches the per-kind kernels, captures the whole
 // batch in a CUDA graph ("plans") and tunes the launch shape.
 #include <stdio.h>
 #include <string.h>
@@ -162,7 +162,7 @@ void WorkList::release() {
 }
 
 // Queue everything one batch needs on stream s: zeroing of shared-word
-// streams, descriptor upload, chunk table, counter reset, persistent kernel.
+// streams, descriptor upload, chunk table, counter reset, per-kind kernels.
 cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_batch_config& cfg,
                     cudaStream_t s) {
   cudaError_t e;

@@ -1,4 +1,4 @@
-// Persistent batch kernels: decode, 128 threads per CTA, one kernel per
+// Batch kernels (grid and persistent): decode, 128 threads per CTA, one kernel per
 // integer kind.
 #include "gzfp_batch_launch.h"
 

@@ -1,4 +1,4 @@
-// Persistent batch kernels: decode, 64 threads per CTA, one kernel per
+// Batch kernels (grid and persistent): decode, 64 threads per CTA, one kernel per
 // floating-point kind.
 #include "gzfp_batch_launch.h"
 

@@ -73,7 +73,7 @@ struct WorkList {
 
 // Queue one prepared batch on stream s: zeroing, descriptor upload from
 // wl.host (which must already hold p.descs), chunk table, counter reset and
-// the persistent kernel.
+// the per-kind kernels.
 cudaError_t enqueue(const Prepared& p, WorkList& wl, bool decode, const gzfp_batch_config& cfg,
                     cudaStream_t s);
 

@@ -40,10 +40,11 @@ inline uint32_t batch_kind(int type, int dims) {
                                              cudaStream_t s);                                  \
   int batch_occupancy_##dir##_##nt##grp(int kind_index, uint32_t staged_w);
 
-// Launch the persistent kernel of kind `kind_index` (into kBatchKind) over
-// chunks [lo, hi) with 64, 128 or 256 threads per CTA on `grid` CTAs, and
-// report its resident CTAs per SM (staged_w: decode staging depth in words
-// per block, 0 for none).  Defined in gzfp_batch_{enc,dec}_<threads>.cu
+// Launch the kernel of kind `kind_index` (into kBatchKind) over chunks
+// [lo, hi) with 64, 128 or 256 threads per CTA: the persistent kernel on
+// `grid` CTAs, or the grid kernel for grid == 0 (launch_batch_kind in
+// gzfp_batch.cuh); and report the persistent kernel's resident CTAs per SM
+// (staged_w: staging depth in words per block, 0 for none).  Defined in gzfp_batch_{enc,dec}_<threads>.cu
 // (floating-point kinds) and gzfp_batch_{enc,dec}_<threads>_int.cu
 // (integer kinds).
 GZFP_BATCH_DECL(enc, 64, )

@@ -1,5 +1,5 @@
 // gzfp_batch_noalloc.cu -- gzfp_batch_run_noalloc (include/gzfp.h): the
-// batched persistent codec with its work list in a fixed, file-scope device
+// batched codec with its work list in a fixed, file-scope device
 // array instead of memory allocated per call.
 //
 // The kernels are the batch path's own (gzfp_batch.cuh); only where their

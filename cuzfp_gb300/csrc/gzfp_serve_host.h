@@ -1,6 +1,6 @@
 // gzfp_serve_host.h -- host-side pieces shared by the request server's two
 // modes (gzfp_serve.cu: batches on slots; gzfp_serve_queue.cu: a device
-// request queue drained by one persistent kernel).
+// request queue drained by a persistent scheduler kernel).
 #pragma once
 
 #include <stddef.h>
