@@ -215,9 +215,11 @@ def test_mixed_pointers(gz, orc, cuda):
     (((1 << 24) + 3,), np.float32, 12.0),  # 48-bit blocks, 4 blocks per 3 words
 ])
 def test_staged_slabs(gz, cuda, shape, dtype, rate):
-    """Host buffers larger than one staging slab: the slab pipeline gives the
-    stream and array of the all-device call (which the oracle pins), for
-    pinned and pageable host memory and for mixed pointers."""
+    """Host buffers larger than one staging slab give the stream and array of
+    the all-device call (which the oracle pins), for pinned and pageable
+    host memory and for mixed pointers: pageable memory, and compression at
+    rates whose blocks share words, go through the slab pipeline; pinned
+    memory on a coherent host link is otherwise coded in place."""
     import torch
     rng = np.random.default_rng(17)
     a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).astype(dtype).reshape(shape)
