@@ -1662,7 +1662,10 @@ GZ_HD uint32_t block_bits(R& r, const General& mode) {
   }
   const uint32_t budget = bits;
   uint32_t n = 0;
-  uncode_planes<BS>(P - 1, kmin, n, bits, r, [](int, uint64_t) {});
+  if constexpr (BS == 64)  // the decoder's token loop for 4^3 blocks
+    uncode_flat64(P - 1, kmin, n, bits, r, [](int, uint64_t) {});
+  else
+    uncode_planes<BS>(P - 1, kmin, n, bits, r, [](int, uint64_t) {});
   const uint32_t used = hdr + (budget - bits);
   return used < mode.minbits ? mode.minbits : used;
 }
