@@ -109,3 +109,47 @@ extern "C" int hc_decompress(int type, unsigned nx, unsigned ny, unsigned nz, do
   if (type == 4) dec_t<double>(dims, in, words, g, maxbits, data);
   return 1;
 }
+
+namespace {
+
+template <int D, typename T>
+uint64_t walk(const uint64_t* in, uint64_t words, uint64_t nblocks, const gzfp::General& mode,
+              uint64_t* offsets) {
+  HostWords w{nullptr, in, words};
+  uint64_t pos = 0;
+  for (uint64_t b = 0; b < nblocks; b++) {
+    offsets[b] = pos;
+    gzfp::BitReader<HostWords> r(w, pos);
+    pos += gzfp::block_bits<D, T>(r, mode);
+  }
+  return pos;
+}
+
+template <typename T>
+uint64_t walk_t(int dims, const uint64_t* in, uint64_t words, uint64_t nblocks,
+                const gzfp::General& mode, uint64_t* offsets) {
+  if (dims == 1) return walk<1, T>(in, words, nblocks, mode, offsets);
+  if (dims == 2) return walk<2, T>(in, words, nblocks, mode, offsets);
+  return walk<3, T>(in, words, nblocks, mode, offsets);
+}
+
+}  // namespace
+
+// The start bit of every block of a general-mode stream (zfp's minbits,
+// maxbits, maxprec, minexp) by the kernels' block-length parse
+// (gzfp::block_bits), as the device index walks it; returns the bit after
+// the last block, 0 on bad arguments.
+extern "C" uint64_t hc_block_offsets(int type, unsigned nx, unsigned ny, unsigned nz,
+                                     unsigned minbits, unsigned maxbits, unsigned maxprec,
+                                     int minexp, const uint64_t* in, size_t bytes,
+                                     uint64_t* offsets) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
+  const gzfp::General mode{minbits, maxbits, maxprec, minexp};
+  const uint64_t words = bytes / 8;
+  if (type == 1) return walk_t<int32_t>(dims, in, words, g.nblocks, mode, offsets);
+  if (type == 2) return walk_t<int64_t>(dims, in, words, g.nblocks, mode, offsets);
+  if (type == 3) return walk_t<float>(dims, in, words, g.nblocks, mode, offsets);
+  return walk_t<double>(dims, in, words, g.nblocks, mode, offsets);
+}

@@ -96,3 +96,28 @@ def test_integer_fields(hostcodec, orc):
         d = orc.decompress(s, a.shape, a.dtype, rate)
         h = hc_decompress(hostcodec, orc, s, a.shape, a.dtype, rate)
         assert np.array_equal(d, h), (a.shape, a.dtype, rate)
+
+
+def test_block_offsets_general_modes(hostcodec, orc):
+    """The kernels' block-length parse (what the device index walks), run on
+    the host over oracle streams of zfp's fixed-precision and
+    fixed-accuracy modes: every block's start bit equals the oracle
+    compressor's, for all four scalar types and 1D / 2D / 3D."""
+    rng = np.random.default_rng(31)
+    shapes = ((1000,), (37, 29), (13, 11, 10))
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        for shape in shapes:
+            a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+            a = (a * 5000).astype(dt) if np.dtype(dt).kind == "i" else a.astype(dt)
+            modes = [orc.mode_precision(dt, p) for p in (5, 16, 40)]
+            if np.dtype(dt).kind == "f":
+                modes += [orc.mode_accuracy(dt, t) for t in (1e-1, 1e-4, 1e-9)]
+            for params in modes:
+                s, offs = orc.compress_params(a, params, with_offsets=True)
+                s = np.ascontiguousarray(s)
+                nx, ny, nz = orc.dims3(shape)
+                got = np.zeros(offs.size, np.uint64)
+                end = hostcodec.hc_block_offsets(orc.type_code(dt), nx, ny, nz, *params,
+                                                 s.ctypes.data, s.nbytes, got.ctypes.data)
+                assert np.array_equal(got, offs), (dt, shape, params)
+                assert end <= s.nbytes * 8, (dt, shape, params)
