@@ -55,9 +55,12 @@ def hostcodec():
     lib.hc_compress.argtypes = A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.hc_decompress.restype = ctypes.c_int
     lib.hc_decompress.argtypes = A + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
-    lib.hc_block_offsets.restype = ctypes.c_uint64
-    lib.hc_block_offsets.argtypes = ([ctypes.c_int] + [ctypes.c_uint] * 6 + [ctypes.c_int] +
-                                     [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p])
+    G = [ctypes.c_int] + [ctypes.c_uint] * 6 + [ctypes.c_int]  # type, dims, zfp parameters
+    for fn in (lib.hc_block_offsets, lib.hc_compress_params, lib.hc_decompress_params):
+        fn.restype = ctypes.c_uint64
+    lib.hc_block_offsets.argtypes = G + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.hc_compress_params.argtypes = G + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.hc_decompress_params.argtypes = G + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     return lib
 
 

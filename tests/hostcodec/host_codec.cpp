@@ -153,3 +153,93 @@ extern "C" uint64_t hc_block_offsets(int type, unsigned nx, unsigned ny, unsigne
   if (type == 3) return walk_t<float>(dims, in, words, g.nblocks, mode, offsets);
   return walk_t<double>(dims, in, words, g.nblocks, mode, offsets);
 }
+
+namespace {
+
+// General-mode coding block after block (the per-block code of the mode
+// kernels, encode_block_mode / decode_block_mode): each block's bits follow
+// the previous block's at once, as zfp writes them.
+template <int D, typename T>
+uint64_t enc_general(const void* data, const gzfp::Geom& g, const gzfp::General& mode,
+                     uint64_t* out, uint64_t words) {
+  typedef typename gzfp::FT<T>::UInt UInt;
+  HostWords w{out, nullptr, words};
+  gzfp::LocalPlanes ps;
+  uint64_t pos = 0;
+  for (uint64_t b = 0; b < g.nblocks; b++) {
+    uint32_t ix, iy, iz;
+    gzfp::block_coords(g, b, ix, iy, iz);
+    UInt raw[1 << (2 * D)];
+    gzfp::gather<D, T>((const T*)data, g, ix, iy, iz, raw);
+    gzfp::BitWriter<HostWords> bw(w, pos, mode.maxbits);
+    pos += gzfp::encode_block_mode<D, T>(raw, mode, bw, ps);
+    bw.finish();
+  }
+  return pos;
+}
+
+template <int D, typename T>
+uint64_t dec_general(const uint64_t* in, uint64_t words, const gzfp::Geom& g,
+                     const gzfp::General& mode, void* data) {
+  typedef typename gzfp::FT<T>::UInt UInt;
+  HostWords w{nullptr, in, words};
+  gzfp::LocalPlanes ps;
+  uint64_t pos = 0;
+  for (uint64_t b = 0; b < g.nblocks; b++) {
+    uint32_t ix, iy, iz;
+    gzfp::block_coords(g, b, ix, iy, iz);
+    gzfp::BitReader<HostWords> r(w, pos);
+    UInt raw[1 << (2 * D)];
+    pos += gzfp::decode_block_mode<D, T>(r, mode, raw, ps);
+    gzfp::scatter<D, T>((T*)data, g, ix, iy, iz, raw);
+  }
+  return pos;
+}
+
+template <typename T>
+uint64_t general_t(bool decode, int dims, const void* data, const gzfp::Geom& g,
+                   const gzfp::General& mode, uint64_t* words, uint64_t nwords) {
+  if (decode) {
+    if (dims == 1) return dec_general<1, T>(words, nwords, g, mode, (void*)data);
+    if (dims == 2) return dec_general<2, T>(words, nwords, g, mode, (void*)data);
+    return dec_general<3, T>(words, nwords, g, mode, (void*)data);
+  }
+  if (dims == 1) return enc_general<1, T>(data, g, mode, words, nwords);
+  if (dims == 2) return enc_general<2, T>(data, g, mode, words, nwords);
+  return enc_general<3, T>(data, g, mode, words, nwords);
+}
+
+uint64_t general(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, unsigned minbits,
+                 unsigned maxbits, unsigned maxprec, int minexp, const void* data,
+                 uint64_t* words, size_t bytes) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
+  const gzfp::General mode{minbits, maxbits, maxprec, minexp};
+  if (!decode) memset(words, 0, bytes);
+  const uint64_t n = bytes / 8;
+  if (type == 1) return general_t<int32_t>(decode, dims, data, g, mode, words, n);
+  if (type == 2) return general_t<int64_t>(decode, dims, data, g, mode, words, n);
+  if (type == 3) return general_t<float>(decode, dims, data, g, mode, words, n);
+  return general_t<double>(decode, dims, data, g, mode, words, n);
+}
+
+}  // namespace
+
+// General-mode compression into a zeroed buffer of `bytes` (at least the
+// stream's size); returns the stream's bits, 0 on bad arguments.
+extern "C" uint64_t hc_compress_params(int type, unsigned nx, unsigned ny, unsigned nz,
+                                       unsigned minbits, unsigned maxbits, unsigned maxprec,
+                                       int minexp, const void* data, uint64_t* out,
+                                       size_t bytes) {
+  return general(false, type, nx, ny, nz, minbits, maxbits, maxprec, minexp, data, out, bytes);
+}
+
+// General-mode decompression; returns the bits read, 0 on bad arguments.
+extern "C" uint64_t hc_decompress_params(int type, unsigned nx, unsigned ny, unsigned nz,
+                                         unsigned minbits, unsigned maxbits, unsigned maxprec,
+                                         int minexp, const uint64_t* in, size_t bytes,
+                                         void* data) {
+  return general(true, type, nx, ny, nz, minbits, maxbits, maxprec, minexp, data,
+                 (uint64_t*)in, bytes);
+}
