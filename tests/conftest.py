@@ -55,6 +55,8 @@ def hostcodec():
     lib.hc_compress.argtypes = A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.hc_decompress.restype = ctypes.c_int
     lib.hc_decompress.argtypes = A + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.hc_compress_aligned.restype = ctypes.c_size_t
+    lib.hc_compress_aligned.argtypes = A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     G = [ctypes.c_int] + [ctypes.c_uint] * 6 + [ctypes.c_int]  # type, dims, zfp parameters
     for fn in (lib.hc_block_offsets, lib.hc_compress_params, lib.hc_decompress_params):
         fn.restype = ctypes.c_uint64

@@ -243,3 +243,46 @@ extern "C" uint64_t hc_decompress_params(int type, unsigned nx, unsigned ny, uns
   return general(true, type, nx, ny, nz, minbits, maxbits, maxprec, minexp, data,
                  (uint64_t*)in, bytes);
 }
+
+namespace {
+
+template <int D, typename T>
+void enc_aligned(const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out,
+                 uint64_t words) {
+  HostWords w{out, nullptr, words};
+  gzfp::LocalPlanes ps;
+  for (uint64_t b = 0; b < g.nblocks; b++)
+    gzfp::encode_one<D, T, true>((const T*)data, g, b, maxbits, w, ps);
+}
+
+template <typename T>
+void aligned_t(int dims, const void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* out,
+               uint64_t words) {
+  if (dims == 1) enc_aligned<1, T>(data, g, maxbits, out, words);
+  if (dims == 2) enc_aligned<2, T>(data, g, maxbits, out, words);
+  if (dims == 3) enc_aligned<3, T>(data, g, maxbits, out, words);
+}
+
+}  // namespace
+
+// hc_compress through the encoder's aligned writer (whole words stored, no
+// shared words merged), as the GPU kernels use it for blocks of whole 64-bit
+// words; 0 when the rate's blocks are not whole words.  The output is
+// filled with ones first, so a word the writer skips shows.
+extern "C" size_t hc_compress_aligned(int type, unsigned nx, unsigned ny, unsigned nz,
+                                      double rate, const void* data, uint64_t* out,
+                                      size_t cap) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
+  const unsigned maxbits = maxbits_for(type, dims, rate);
+  if (!maxbits || maxbits % 64) return 0;
+  const uint64_t words = g.nblocks * maxbits / 64;
+  if (cap < words * 8) return 0;
+  memset(out, 0xff, words * 8);
+  if (type == 1) aligned_t<int32_t>(dims, data, g, maxbits, out, words);
+  if (type == 2) aligned_t<int64_t>(dims, data, g, maxbits, out, words);
+  if (type == 3) aligned_t<float>(dims, data, g, maxbits, out, words);
+  if (type == 4) aligned_t<double>(dims, data, g, maxbits, out, words);
+  return words * 8;
+}

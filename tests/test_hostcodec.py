@@ -155,3 +155,24 @@ def test_general_modes_against_oracle(hostcodec, orc):
                 assert used == bits, (dt, shape, params)
                 ref = orc.decompress_params(s, shape, dt, params)
                 assert np.array_equal(out.view(np.uint8), ref.view(np.uint8)), (dt, shape, params)
+
+
+def test_aligned_writer(hostcodec, orc):
+    """The encoder's aligned writer (what the GPU kernels use for blocks of
+    whole 64-bit words: every word stored, none merged), run on the host
+    into a buffer of ones: the stream is the oracle's, so every word is
+    written in full."""
+    rng = np.random.default_rng(33)
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        for shape, rates in (((1003,), (16, 32, 48)), ((37, 29), (4, 8, 12)),
+                             ((13, 11, 10), (1, 2, 8, 16))):
+            a = np.cumsum(rng.standard_normal(int(np.prod(shape)))).reshape(shape)
+            a = (a * 5000).astype(dt) if np.dtype(dt).kind == "i" else a.astype(dt)
+            nx, ny, nz = orc.dims3(shape)
+            for rate in rates:
+                s = orc.compress(a, rate)
+                out = np.zeros(s.size + 1, np.uint64)
+                n = hostcodec.hc_compress_aligned(orc.type_code(dt), nx, ny, nz, float(rate),
+                                                  a.ctypes.data, out.ctypes.data, out.nbytes)
+                assert n == s.nbytes, (dt, shape, rate, n, s.nbytes)
+                assert np.array_equal(out[: s.size], s), (dt, shape, rate)
