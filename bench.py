@@ -1001,7 +1001,9 @@ def run(args, rank, world, local):
         traffic = None
     cpu = None
     parity = {"checked": False}
-    if not args.no_cpu:
+    # the CPU leg (baseline and whole-field parity) runs at N = 1 only: with
+    # more ranks, rank 0 would hold the others' GPUs idle while it codes
+    if not args.no_cpu and world == 1:
         from oracle import oracle
         oracle.port()
         host = field.cpu().numpy()
