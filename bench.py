@@ -767,10 +767,10 @@ def run_accuracy(args, rank, world, local):
     enc_ms = sum(ev[3 * i].elapsed_time(ev[3 * i + 1]) for i in range(args.steps)) / args.steps
     dec_ms = sum(ev[3 * i + 1].elapsed_time(ev[3 * i + 2]) for i in range(args.steps)) / args.steps
     ms_per_step = max_over_ranks(enc_ms + dec_ms, world, dev)
-    # the serial walk, on a small field (too few blocks for the parallel
-    # index), and the parallel index of the whole stream, checked against
-    # the compressor's start bits
-    small = synth.sinusoids_device((64, 64, 64), 16, 32, seed=rank, dtype=torch.float64,
+    # the serial walk, on a small field (15^3 = 3,375 blocks: too few for
+    # the parallel index, which starts at 4,096), and the parallel index of
+    # the whole stream, checked against the compressor's start bits
+    small = synth.sinusoids_device((60, 60, 60), 16, 32, seed=rank, dtype=torch.float64,
                                    device=dev)
     sw = gz.compress_mode(small, mode, cuda_stream=stream)
     gz.index_blocks(sw, small.shape, torch.float64, mode, cuda_stream=stream)
@@ -779,7 +779,7 @@ def run_accuracy(args, rank, world, local):
     gz.index_blocks(sw, small.shape, torch.float64, mode, cuda_stream=stream)
     b.record(stream)
     b.synchronize()
-    walk_us = a.elapsed_time(b) * 1e3 / (16 ** 3)
+    walk_us = a.elapsed_time(b) * 1e3 / (15 ** 3)
     idx = gz.index_blocks(words, SHAPE, torch.float64, mode, cuda_stream=stream)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

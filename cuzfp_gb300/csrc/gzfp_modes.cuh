@@ -114,9 +114,14 @@ __global__ void index_blocks_kernel(const uint64_t* __restrict__ in, uint64_t nw
 
 GZ_HD uint64_t index_step_bits(uint32_t bits) { return bits ? bits : 1; }
 
+// One walker per warp: lane 0 walks, the other lanes leave at once.  Walkers
+// sharing a warp diverge on every block (each parses a different one), so a
+// lone lane walks about 5x faster than 32 lanes in lockstep.
 template <int D, typename T>
 __global__ void index_walk_kernel(IndexJob j, bool extend) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt & 31) return;
+  const uint32_t s = gt >> 5;
   if (s >= j.nseg) return;
   const uint64_t total = j.nwords * 64;
   const DevWords words{nullptr, j.in, j.nwords};
@@ -259,8 +264,8 @@ cudaError_t launch_decode_mode(int dims, const uint64_t* in, uint64_t nwords,
 
 template <int D, typename T>
 cudaError_t launch_index_walk_t(const IndexJob& j, bool extend, cudaStream_t s) {
-  const unsigned threads = 64;
-  index_walk_kernel<D, T><<<(j.nseg + threads - 1) / threads, threads, 0, s>>>(j, extend);
+  const unsigned threads = 64;  // two walkers per CTA, one per warp
+  index_walk_kernel<D, T><<<(j.nseg * 32 + threads - 1) / threads, threads, 0, s>>>(j, extend);
   return cudaGetLastError();
 }
 
