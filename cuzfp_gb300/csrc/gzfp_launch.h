@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "gzfp_array.cuh"
+#include "gzfp_index_host.h"
 
 namespace gzfp {
 
@@ -84,13 +85,6 @@ struct IndexJob {
   unsigned long long* exits;     // per segment: the walker's first start past its end
   unsigned long long* info;      // per segment: extension steps, merge segment, merge
                                  // index, status (0 merged, 1 stream end, 2 failed)
-};
-struct IndexPiece {
-  unsigned long long src;    // list piece: entry index in `lists`
-  unsigned long long count;  // starts in the piece
-  unsigned long long dst;    // index of its first start in the offsets
-  unsigned long long seg;    // walk piece: the segment whose extension it re-walks
-  unsigned long long walk;   // 1: walk piece, 0: list piece
 };
 template <typename T>
 cudaError_t launch_index_walk(int dims, const IndexJob& j, bool extend, cudaStream_t s);

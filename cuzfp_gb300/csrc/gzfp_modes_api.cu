@@ -166,26 +166,7 @@ bool parallel_index(ModeSpace& ms, int type, int dims, const uint64_t* words, ui
   const unsigned long long* info = state.data() + 2 * nseg;
   // follow the true chain from segment 0 (whose walker starts at block 0)
   std::vector<gzfp::IndexPiece> pieces;
-  uint64_t dst = 0, seg = 0, start = 0;
-  for (size_t it = 0; it <= nseg && dst < nblocks; it++) {
-    const unsigned long long n = counts[seg];
-    if (n > j.cap) return false;
-    if (n > start) {
-      pieces.push_back(gzfp::IndexPiece{seg * j.cap + start, n - start, dst, 0, 0});
-      dst += n - start;
-    }
-    const unsigned long long* inf = info + 4 * seg;
-    if (inf[3] == 2) return false;  // no merge within the extension's cap
-    if (inf[0]) {
-      pieces.push_back(gzfp::IndexPiece{0, inf[0], dst, seg, 1});
-      dst += inf[0];
-    }
-    if (inf[3] == 1) break;  // the chain ran to the end of the stream
-    if (inf[1] <= seg) return false;
-    seg = inf[1];
-    start = inf[2];
-  }
-  if (dst < nblocks) return false;  // fewer starts than blocks: the serial walk reports it
+  if (!gzfp::index_pieces(nseg, j.cap, counts, info, nblocks, pieces)) return false;
   if ((err = reserve(ms.pieces, ms.pieces_cap, pieces.size() * sizeof(gzfp::IndexPiece))) ||
       (err = reserve(ms.offsets, ms.offsets_cap, (size_t)nblocks * 8)) ||
       (err = reserve(ms.sums, ms.sums_cap, 64)) ||
