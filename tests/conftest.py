@@ -55,6 +55,12 @@ def hostcodec():
     lib.hc_compress.argtypes = A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.hc_decompress.restype = ctypes.c_int
     lib.hc_decompress.argtypes = A + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    S = [ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint] + [ctypes.c_longlong] * 3 + \
+        [ctypes.c_double]
+    lib.hc_compress_strided.restype = ctypes.c_size_t
+    lib.hc_compress_strided.argtypes = S + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.hc_decompress_strided.restype = ctypes.c_size_t
+    lib.hc_decompress_strided.argtypes = S + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     lib.hc_compress_aligned.restype = ctypes.c_size_t
     lib.hc_compress_aligned.argtypes = A + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     G = [ctypes.c_int] + [ctypes.c_uint] * 6 + [ctypes.c_int]  # type, dims, zfp parameters

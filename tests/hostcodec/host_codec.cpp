@@ -286,3 +286,63 @@ extern "C" size_t hc_compress_aligned(int type, unsigned nx, unsigned ny, unsign
   if (type == 4) aligned_t<double>(dims, data, g, maxbits, out, words);
   return words * 8;
 }
+
+namespace {
+
+template <int D, typename T>
+void strided(bool decode, void* data, const gzfp::Geom& g, unsigned maxbits, uint64_t* words,
+             uint64_t nwords) {
+  HostWords w{decode ? nullptr : words, decode ? words : nullptr, nwords};
+  gzfp::LocalPlanes ps;
+  for (uint64_t b = 0; b < g.nblocks; b++) {
+    if (decode)
+      gzfp::decode_one<D, T>((T*)data, g, b, maxbits, w, ps);
+    else
+      gzfp::encode_one<D, T>((const T*)data, g, b, maxbits, w, ps);
+  }
+}
+
+template <typename T>
+void strided_t(bool decode, int dims, void* data, const gzfp::Geom& g, unsigned maxbits,
+               uint64_t* words, uint64_t nwords) {
+  if (dims == 1) strided<1, T>(decode, data, g, maxbits, words, nwords);
+  if (dims == 2) strided<2, T>(decode, data, g, maxbits, words, nwords);
+  if (dims == 3) strided<3, T>(decode, data, g, maxbits, words, nwords);
+}
+
+// a strided field: `data` is the address of value (0, 0, 0), value (x, y, z)
+// at data + x sx + y sy + z sz elements (signed strides, 0 = contiguous)
+size_t strided_call(bool decode, int type, unsigned nx, unsigned ny, unsigned nz, long long sx,
+                    long long sy, long long sz, double rate, void* data, uint64_t* words,
+                    size_t bytes) {
+  gzfp::Geom g;
+  int dims;
+  if (!geom(nx, ny, nz, g, dims) || type < 1 || type > 4) return 0;
+  g.sx = sx ? sx : 1;
+  g.sy = sy ? sy : (long long)nx;
+  g.sz = sz ? sz : (long long)nx * (ny ? ny : 1);
+  g.vec = 0;  // value by value: only the index arithmetic matters on the host
+  const unsigned maxbits = maxbits_for(type, dims, rate);
+  const uint64_t nwords = (g.nblocks * maxbits + 63) / 64;
+  if (bytes < nwords * 8) return 0;
+  if (!decode) memset(words, 0, nwords * 8);
+  if (type == 1) strided_t<int32_t>(decode, dims, data, g, maxbits, words, nwords);
+  if (type == 2) strided_t<int64_t>(decode, dims, data, g, maxbits, words, nwords);
+  if (type == 3) strided_t<float>(decode, dims, data, g, maxbits, words, nwords);
+  if (type == 4) strided_t<double>(decode, dims, data, g, maxbits, words, nwords);
+  return nwords * 8;
+}
+
+}  // namespace
+
+// hc_compress / hc_decompress of a strided field (zfp_field sx/sy/sz)
+extern "C" size_t hc_compress_strided(int type, unsigned nx, unsigned ny, unsigned nz,
+                                      long long sx, long long sy, long long sz, double rate,
+                                      const void* data, uint64_t* out, size_t cap) {
+  return strided_call(false, type, nx, ny, nz, sx, sy, sz, rate, (void*)data, out, cap);
+}
+extern "C" size_t hc_decompress_strided(int type, unsigned nx, unsigned ny, unsigned nz,
+                                        long long sx, long long sy, long long sz, double rate,
+                                        const uint64_t* in, size_t bytes, void* data) {
+  return strided_call(true, type, nx, ny, nz, sx, sy, sz, rate, data, (uint64_t*)in, bytes);
+}

@@ -176,3 +176,41 @@ def test_aligned_writer(hostcodec, orc):
                                                   a.ctypes.data, out.ctypes.data, out.nbytes)
                 assert n == s.nbytes, (dt, shape, rate, n, s.nbytes)
                 assert np.array_equal(out[: s.size], s), (dt, shape, rate)
+
+
+def test_strided_views(hostcodec, orc):
+    """Strided fields (zfp_field sx/sy/sz): transposed, reversed and stepped
+    views, and sub-arrays, through the kernels' per-block code on the host:
+    the stream is the oracle's strided stream, and decoding into a strided
+    view writes exactly the oracle's values there and nothing else."""
+    rng = np.random.default_rng(34)
+    for dt in (np.float32, np.float64, np.int32, np.int64):
+        base3 = np.cumsum(rng.standard_normal(23 * 19 * 17)).reshape(23, 19, 17)
+        base2 = np.cumsum(rng.standard_normal(41 * 37)).reshape(41, 37)
+        base1 = np.cumsum(rng.standard_normal(301))
+        if np.dtype(dt).kind == "i":
+            base3, base2, base1 = base3 * 5000, base2 * 5000, base1 * 5000
+        b3, b2, b1 = base3.astype(dt), base2.astype(dt), base1.astype(dt)
+        views = [b3.transpose(2, 0, 1), b3[::-1, :, ::2], b3[3:20, 1::3, ::-1],
+                 b2.T, b2[::-2, 5:30], b1[::-3], b1[200:7:-1]]
+        for v in views:
+            for rate in (5.5, 16.0):
+                s = orc.compress_view(v, rate)
+                (nx, ny, nz), (sx, sy, sz), addr = orc.view_geometry(v)
+                t = orc.type_code(dt)
+                out = np.zeros(s.size + 1, np.uint64)
+                n = hostcodec.hc_compress_strided(t, nx, ny, nz, sx, sy, sz, rate, addr,
+                                                  out.ctypes.data, out.nbytes)
+                assert n == s.nbytes and np.array_equal(out[: s.size], s), (dt, v.shape, rate)
+                # decode into the same view of two copies of its buffer
+                base = b3 if v.ndim == 3 else b2 if v.ndim == 2 else b1
+                mine, theirs = base.copy(), base.copy()
+                off = addr - base.__array_interface__["data"][0]  # bytes to value (0, 0, 0)
+                s = np.ascontiguousarray(s)
+                m_addr = mine.__array_interface__["data"][0] + off
+                got = hostcodec.hc_decompress_strided(t, nx, ny, nz, sx, sy, sz, rate,
+                                                      s.ctypes.data, s.nbytes, m_addr)
+                assert got == s.nbytes
+                tv = np.ndarray(v.shape, dt, theirs, off, v.strides)
+                orc.decompress_into(s, tv, rate)
+                assert np.array_equal(mine.view(np.uint8), theirs.view(np.uint8)), (dt, v.shape, rate)
