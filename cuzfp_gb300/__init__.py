@@ -940,7 +940,7 @@ class ServeRequest(ctypes.Structure):
 
 class ServeResult(ctypes.Structure):
     """gzfp_serve_result: host times of admission and completion; in the
-    device-queue mode also the device-clock span of the request's chunks."""
+    device-queue mode also the device-clock span of the request's CTAs."""
     _fields_ = [("admitted", ctypes.c_double), ("completed", ctypes.c_double),
                 ("output_bytes", _SZ), ("batch", _I), ("status", _I),
                 ("device_start", ctypes.c_double), ("device_end", ctypes.c_double)]
