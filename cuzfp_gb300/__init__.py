@@ -956,6 +956,10 @@ class ServeConfig(ctypes.Structure):
 
 
 class ServeStats(ctypes.Structure):
+    """gzfp_serve_stats: wall time to the last completion, batches and
+    requests per batch (device queue: publications), peak arena use, busy
+    fraction, kernels launched, requests on the device when one is
+    admitted, and (device queue) scheduler launches."""
     _fields_ = [("wall", ctypes.c_double), ("batches", _I), ("mean_batch", ctypes.c_double),
                 ("peak_bytes", _SZ), ("busy", ctypes.c_double), ("kernels", _I),
                 ("mean_inflight", ctypes.c_double), ("schedulers", _I)]
